@@ -1,0 +1,145 @@
+"""ctypes binding of libfd2d.so (include/fd2d.h).
+
+The library is built in-tree by :mod:`fd2d_noise_gb300.build`.  There is no
+fallback: if the shared library is missing or fails to load, importing the
+solvers raises, and every solve runs on the GPU through this library.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from .config import FD2DConfig, FD2DSizes
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfd2d.so")
+
+FD2D_OK = 0
+STATUS_NAMES = {
+    0: "FD2D_OK", 1: "FD2D_ERR_ARG", 2: "FD2D_ERR_SHAPE", 3: "FD2D_ERR_ORDER",
+    4: "FD2D_ERR_OOM", 5: "FD2D_ERR_CUDA", 6: "FD2D_ERR_TIMEOUT", 7: "FD2D_ERR_INDEX",
+    8: "FD2D_ERR_NO_DEVICE", 9: "FD2D_ERR_UNSUPPORTED",
+}
+PREC_FP64, PREC_FP32 = 0, 1
+MEM_HOST, MEM_DEVICE = 0, 1
+
+# Every symbol include/fd2d.h declares (checked by the CPU test suite).
+EXPORTED = [
+    "fd2d_abi_version", "fd2d_ctx_create", "fd2d_ctx_destroy", "fd2d_ctx_set_stream",
+    "fd2d_ctx_set_memspace", "fd2d_ctx_set_precision", "fd2d_ctx_synchronize",
+    "fd2d_ctx_kernel_launches", "fd2d_last_error", "fd2d_query_sizes",
+    "fd2d_forward1_green", "fd2d_forward2_correlation", "fd2d_noise_adjoint",
+]
+
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_cfgp = ctypes.POINTER(FD2DConfig)
+
+
+class FD2DError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(path: str = LIB_PATH):
+    """Load libfd2d.so and declare the C prototypes (raises if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise ImportError(
+                f"{path} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+                "(the GPU path has no CPU fallback)")
+        L = ctypes.CDLL(path)
+        L.fd2d_abi_version.restype = _i32
+        L.fd2d_ctx_create.argtypes = [_i32, _i32, ctypes.POINTER(_vp)]
+        L.fd2d_ctx_destroy.argtypes = [_vp]
+        L.fd2d_ctx_set_stream.argtypes = [_vp, _vp]
+        L.fd2d_ctx_set_memspace.argtypes = [_vp, _i32]
+        L.fd2d_ctx_set_precision.argtypes = [_vp, _i32]
+        L.fd2d_ctx_synchronize.argtypes = [_vp]
+        L.fd2d_ctx_kernel_launches.argtypes = [_vp]
+        L.fd2d_ctx_kernel_launches.restype = _i64
+        L.fd2d_last_error.argtypes = [_vp]
+        L.fd2d_last_error.restype = ctypes.c_char_p
+        L.fd2d_query_sizes.argtypes = [_cfgp, _i32, ctypes.POINTER(FD2DSizes)]
+        L.fd2d_forward1_green.argtypes = [
+            _vp, _cfgp, _vp, _vp, _vp, _i32, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp]
+        L.fd2d_forward2_correlation.argtypes = [
+            _vp, _cfgp, _vp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _i32, _vp, _i32, _i32, _vp,
+            _vp, _i32, _vp, _vp]
+        L.fd2d_noise_adjoint.argtypes = [
+            _vp, _cfgp, _vp, _vp, _vp, _i32, _vp, _vp, ctypes.POINTER(_i64), _vp, _i32, _vp, _i32,
+            _vp, _i32, _vp, _i32, _vp, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp]
+        for name in EXPORTED:
+            if name not in ("fd2d_abi_version", "fd2d_ctx_kernel_launches", "fd2d_last_error"):
+                getattr(L, name).restype = _i32
+        _lib = L
+        return L
+
+
+def check(status: int, ctx=None):
+    if status != FD2D_OK:
+        L = load()
+        msg = L.fd2d_last_error(ctx).decode(errors="replace")
+        raise FD2DError(status, msg)
+
+
+class Context:
+    """Owns an ``fd2d_ctx`` (one CUDA device, one stream, cached workspace)."""
+
+    def __init__(self, device: int = 0, precision: int = PREC_FP32):
+        self.L = load()
+        h = _vp()
+        check(self.L.fd2d_ctx_create(int(device), int(precision), ctypes.byref(h)))
+        self.h = h
+        self.device = device
+        self.precision = precision
+        self.memspace = MEM_HOST
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fd2d_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_precision(self, precision: int):
+        if precision != self.precision:
+            check(self.L.fd2d_ctx_set_precision(self.h, int(precision)), self.h)
+            self.precision = precision
+
+    def set_memspace(self, memspace: int):
+        if memspace != self.memspace:
+            check(self.L.fd2d_ctx_set_memspace(self.h, int(memspace)), self.h)
+            self.memspace = memspace
+
+    def set_stream(self, stream_ptr: int):
+        check(self.L.fd2d_ctx_set_stream(self.h, _vp(stream_ptr or None)), self.h)
+
+    def synchronize(self):
+        check(self.L.fd2d_ctx_synchronize(self.h), self.h)
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.L.fd2d_ctx_kernel_launches(self.h))
+
+
+def query_sizes(cfg, nr: int) -> FD2DSizes:
+    L = load()
+    out = FD2DSizes()
+    c = cfg.to_c()
+    check(L.fd2d_query_sizes(ctypes.byref(c), int(nr), ctypes.byref(out)))
+    return out

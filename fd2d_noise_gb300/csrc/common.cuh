@@ -1,0 +1,165 @@
+// common.cuh -- shared internals of libfd2d: status plumbing, device buffers,
+// launch accounting and the host-side problem setup (grid, taper, indices,
+// coefficient tables) of the fd2d_noise solvers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fd2d.h"
+
+namespace fd2d {
+
+// ---- errors -------------------------------------------------------------------
+struct Error {
+  fd2d_status code;
+  std::string msg;
+};
+
+#define FD2D_TRY(expr)                                  \
+  do {                                                  \
+    fd2d_status _s = (expr);                            \
+    if (_s != FD2D_OK) return _s;                       \
+  } while (0)
+
+// Records the message on the context and returns the status.
+fd2d_status set_error(fd2d_ctx* ctx, fd2d_status s, const std::string& msg);
+
+#define FD2D_CUDA(ctx, expr)                                                        \
+  do {                                                                              \
+    cudaError_t _e = (expr);                                                        \
+    if (_e != cudaSuccess)                                                          \
+      return ::fd2d::set_error((ctx), _e == cudaErrorMemoryAllocation ? FD2D_ERR_OOM \
+                                                                      : FD2D_ERR_CUDA, \
+                               std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+// ---- host problem setup ---------------------------------------------------------
+// Everything a solver needs from fd2d_config, derived once on the host.
+struct Geometry {
+  int nx = 0, nz = 0, nt = 0, ntc = 0, order = 4, r = 2, K = 0, fs = 1, fw = 1, nb = 0;
+  double Lx = 0, Lz = 0, dt = 0, dx = 0, dz = 0, dw = 0;
+  std::vector<double> x, z, w, absbound;  // absbound nx*nz column-major
+  double c[4] = {0, 0, 0, 0};             // staggered coefficients c_1..c_r
+  std::vector<double> t_fwd, t_corr;      // time axes (0:dt:(nt-1)dt and -(nt-1)dt:dt:(nt-1)dt)
+  int64_t npts() const { return (int64_t)nx * nz; }
+};
+
+std::vector<double> matlab_colon(double a, double d, double b);
+int nearest_node(const std::vector<double>& x, double p);
+fd2d_status make_geometry(const fd2d_config* cfg, Geometry& g, std::string& err);
+// interpol_matrix (K-by-max(nb,1), column-major): code/run_forward2_correlation.m:121-165
+fd2d_status make_interpol_matrix(int K, int nb, std::vector<double>& M, std::string& err);
+// 1/sqrt(2 pi) * exp(1i*th) * scale  (evaluated in the reference's order)
+inline void dft_coeff(double th, double scale, double& re, double& im) {
+  const double s = 1 / std::sqrt(2 * M_PI);
+  re = (s * std::cos(th)) * scale;
+  im = (s * std::sin(th)) * scale;
+}
+
+// ---- device buffers ---------------------------------------------------------------
+// A grow-only device allocation owned by a context.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace fd2d
+
+// Context (opaque in the C ABI).
+struct fd2d_ctx {
+  int device = 0;
+  int precision = FD2D_PREC_FP32;
+  int memspace = FD2D_MEM_HOST;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int64_t launches = 0;
+  std::string last_error;
+  int sm_count = 0;
+  // named workspace buffers
+  std::vector<std::pair<std::string, fd2d::DevBuf>> bufs;
+  // device-side error flag of bounded waits (int32)
+  int* d_err = nullptr;
+};
+
+namespace fd2d {
+
+// Returns a device buffer of at least `bytes` under `name` (grown when needed).
+fd2d_status workspace(fd2d_ctx* ctx, const char* name, size_t bytes, void** out);
+template <typename T>
+fd2d_status workspace_t(fd2d_ctx* ctx, const char* name, size_t count, T** out) {
+  return workspace(ctx, name, count * sizeof(T) + 256, reinterpret_cast<void**>(out));
+}
+// Release every workspace buffer of the context.
+void free_workspace(fd2d_ctx* ctx);
+
+// Checks the last launch and counts it.
+fd2d_status after_launch(fd2d_ctx* ctx, const char* what);
+
+// Copies an input array to the device (host memspace) or passes it through.
+// n == 0 or src == nullptr gives nullptr.
+fd2d_status stage_in(fd2d_ctx* ctx, const char* name, const void* src, size_t bytes,
+                     const void** dev);
+// Output buffer on the device: the caller's pointer (device memspace) or a
+// workspace buffer whose content is copied back by stage_out.
+fd2d_status out_buffer(fd2d_ctx* ctx, const char* name, void* user, size_t bytes, void** dev);
+fd2d_status stage_out(fd2d_ctx* ctx, void* user, const void* dev, size_t bytes);
+
+// Uploads a host vector into a named workspace buffer (async on the ctx stream).
+template <typename T>
+fd2d_status upload(fd2d_ctx* ctx, const char* name, const std::vector<T>& v, T** dev) {
+  FD2D_TRY(workspace_t<T>(ctx, name, v.size() ? v.size() : 1, dev));
+  if (!v.empty()) {
+    cudaError_t e = cudaMemcpyAsync(*dev, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                    ctx->stream);
+    if (e != cudaSuccess) return set_error(ctx, FD2D_ERR_CUDA, std::string("upload ") + name + ": " + cudaGetErrorString(e));
+  }
+  return FD2D_OK;
+}
+
+// Arguments of one solve, already validated (pointers are device pointers).
+struct SolveArgs {
+  const double *mu = nullptr, *rho = nullptr, *dmu = nullptr;
+  // point sources (indices into the nx*nz grid) and receivers
+  std::vector<int> src_idx, rec_idx;
+  int mode = 0;
+  // forward1
+  const float* G_in = nullptr;
+  int n_G_in = 0;
+  double *G_re = nullptr, *G_im = nullptr;  // outputs (fwd1) or inputs (corr/adj)
+  float* G_out = nullptr;
+  // correlation / adjoint
+  const double *Gin_re = nullptr, *Gin_im = nullptr;
+  int n_G = 0;
+  const double* spectrum = nullptr;  // K x n_src
+  int n_src = 0;
+  const double* source_dist = nullptr;
+  int n_dist = 0;
+  const float* C_in = nullptr;  // Born snapshots (C_in or u_in)
+  int n_C_in = 0;
+  float* C_out = nullptr;  // C_out or u_out
+  // adjoint
+  const float* u_fwd = nullptr;
+  int n_u_fwd = 0;
+  const double *stf_re = nullptr, *stf_im = nullptr;
+  int64_t stf_dims[3] = {0, 0, 0};
+  double* Kout = nullptr;
+  double *sf_re = nullptr, *sf_im = nullptr;
+  double* seis = nullptr;
+};
+
+// Precision-specific drivers (solver_fp64.cu / solver_fp32.cu).
+fd2d_status fp64_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
+fd2d_status fp64_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
+fd2d_status fp64_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
+fd2d_status fp32_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
+fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
+fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
+
+}  // namespace fd2d

@@ -1,0 +1,525 @@
+// fd2d_api.cu -- the C ABI of libfd2d (include/fd2d.h): contexts, argument
+// validation, host<->device staging and dispatch to the FP64 / FP32 drivers.
+//
+// Validation mirrors what the MATLAB solvers would reject (an index past the end
+// of an array, mismatched reshape sizes) so callers get an error code where the
+// reference raises a MATLAB error.
+#include "common.cuh"
+
+#include <algorithm>
+#include <mutex>
+
+namespace fd2d {
+
+static std::mutex g_err_mu;
+static std::string g_global_err;
+
+fd2d_status set_error(fd2d_ctx* ctx, fd2d_status s, const std::string& msg) {
+  if (ctx) {
+    ctx->last_error = msg;
+  } else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_global_err = msg;
+  }
+  return s;
+}
+
+fd2d_status workspace(fd2d_ctx* ctx, const char* name, size_t bytes, void** out) {
+  for (auto& kv : ctx->bufs) {
+    if (kv.first == name) {
+      if (kv.second.bytes >= bytes) {
+        *out = kv.second.ptr;
+        return FD2D_OK;
+      }
+      // grow: the stream must not be using the old buffer any more
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(kv.second.ptr);
+      kv.second.ptr = nullptr;
+      kv.second.bytes = 0;
+      cudaError_t e = cudaMalloc(&kv.second.ptr, bytes);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(ctx, FD2D_ERR_OOM, std::string("cudaMalloc(") + name + ", " +
+                                                std::to_string(bytes) + " B): " + cudaGetErrorString(e));
+      }
+      kv.second.bytes = bytes;
+      *out = kv.second.ptr;
+      return FD2D_OK;
+    }
+  }
+  DevBuf b;
+  cudaError_t e = cudaMalloc(&b.ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(ctx, FD2D_ERR_OOM, std::string("cudaMalloc(") + name + ", " +
+                                            std::to_string(bytes) + " B): " + cudaGetErrorString(e));
+  }
+  b.bytes = bytes;
+  ctx->bufs.emplace_back(name, b);
+  *out = b.ptr;
+  return FD2D_OK;
+}
+
+void free_workspace(fd2d_ctx* ctx) {
+  for (auto& kv : ctx->bufs) cudaFree(kv.second.ptr);
+  ctx->bufs.clear();
+}
+
+fd2d_status after_launch(fd2d_ctx* ctx, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(ctx, FD2D_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  ++ctx->launches;
+  return FD2D_OK;
+}
+
+fd2d_status stage_in(fd2d_ctx* ctx, const char* name, const void* src, size_t bytes, const void** dev) {
+  if (!src || bytes == 0) {
+    *dev = nullptr;
+    return FD2D_OK;
+  }
+  if (ctx->memspace == FD2D_MEM_DEVICE) {
+    *dev = src;
+    return FD2D_OK;
+  }
+  void* d = nullptr;
+  FD2D_TRY(workspace(ctx, name, bytes, &d));
+  FD2D_CUDA(ctx, cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  *dev = d;
+  return FD2D_OK;
+}
+
+fd2d_status out_buffer(fd2d_ctx* ctx, const char* name, void* user, size_t bytes, void** dev) {
+  if (!user || bytes == 0) {
+    *dev = nullptr;
+    return FD2D_OK;
+  }
+  if (ctx->memspace == FD2D_MEM_DEVICE) {
+    *dev = user;
+    return FD2D_OK;
+  }
+  return workspace(ctx, name, bytes, dev);
+}
+
+fd2d_status stage_out(fd2d_ctx* ctx, void* user, const void* dev, size_t bytes) {
+  if (!user || !dev || bytes == 0 || ctx->memspace == FD2D_MEM_DEVICE) return FD2D_OK;
+  FD2D_CUDA(ctx, cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return FD2D_OK;
+}
+
+static fd2d_status finish(fd2d_ctx* ctx) {
+  if (ctx->memspace == FD2D_MEM_HOST) FD2D_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  int herr = 0;
+  if (ctx->memspace == FD2D_MEM_HOST && ctx->d_err) {
+    FD2D_CUDA(ctx, cudaMemcpy(&herr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+      cudaMemset(ctx->d_err, 0, sizeof(int));
+      return set_error(ctx, FD2D_ERR_TIMEOUT, "a bounded device-side wait gave up (code " + std::to_string(herr) + ")");
+    }
+  }
+  return FD2D_OK;
+}
+
+static fd2d_status point_indices(fd2d_ctx* ctx, const Geometry& g, const double* pts_host, int n,
+                                 const char* what, std::vector<int>& idx) {
+  idx.resize(n);
+  if (n == 0) return FD2D_OK;
+  if (!pts_host) return set_error(ctx, FD2D_ERR_ARG, std::string(what) + " is NULL");
+  for (int i = 0; i < n; ++i) {
+    int ix = nearest_node(g.x, pts_host[i]);
+    int iz = nearest_node(g.z, pts_host[n + i]);
+    idx[i] = ix + g.nx * iz;
+  }
+  return FD2D_OK;
+}
+
+// Positions (src, rec) are small: read them on the host in either memspace.
+static fd2d_status host_points(fd2d_ctx* ctx, const double* p, int n, std::vector<double>& out) {
+  out.assign((size_t)2 * n, 0.0);
+  if (n == 0 || !p) return FD2D_OK;
+  if (ctx->memspace == FD2D_MEM_DEVICE) {
+    FD2D_CUDA(ctx, cudaMemcpyAsync(out.data(), p, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    FD2D_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  } else {
+    std::memcpy(out.data(), p, sizeof(double) * 2 * n);
+  }
+  return FD2D_OK;
+}
+
+static fd2d_status check_ctx(fd2d_ctx* ctx) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return set_error(ctx, FD2D_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  ctx->last_error.clear();
+  return FD2D_OK;
+}
+
+}  // namespace fd2d
+
+using namespace fd2d;
+
+extern "C" {
+
+int32_t fd2d_abi_version(void) { return FD2D_ABI_VERSION; }
+
+fd2d_status fd2d_ctx_create(int32_t device, int32_t precision, fd2d_ctx** out) {
+  if (!out) return set_error(nullptr, FD2D_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return set_error(nullptr, FD2D_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  }
+  if (device < 0 || device >= n) return set_error(nullptr, FD2D_ERR_ARG, "device index out of range");
+  if (precision != FD2D_PREC_FP64 && precision != FD2D_PREC_FP32)
+    return set_error(nullptr, FD2D_ERR_ARG, "precision must be FD2D_PREC_FP64 or FD2D_PREC_FP32");
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return set_error(nullptr, FD2D_ERR_CUDA, cudaGetErrorString(e));
+  fd2d_ctx* c = new fd2d_ctx();
+  c->device = device;
+  c->precision = precision;
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->d_err, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return set_error(nullptr, FD2D_ERR_CUDA, cudaGetErrorString(e));
+  }
+  c->own_stream = true;
+  *out = c;
+  return FD2D_OK;
+}
+
+fd2d_status fd2d_ctx_destroy(fd2d_ctx* ctx) {
+  if (!ctx) return FD2D_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_workspace(ctx);
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return FD2D_OK;
+}
+
+fd2d_status fd2d_ctx_set_stream(fd2d_ctx* ctx, void* stream) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  if (stream) {
+    if (ctx->own_stream && ctx->stream) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaStreamDestroy(ctx->stream);
+    }
+    ctx->stream = (cudaStream_t)stream;
+    ctx->own_stream = false;
+  } else if (!ctx->own_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return set_error(ctx, FD2D_ERR_CUDA, cudaGetErrorString(e));
+    ctx->own_stream = true;
+  }
+  return FD2D_OK;
+}
+
+fd2d_status fd2d_ctx_set_memspace(fd2d_ctx* ctx, int32_t memspace) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  if (memspace != FD2D_MEM_HOST && memspace != FD2D_MEM_DEVICE)
+    return set_error(ctx, FD2D_ERR_ARG, "memspace must be FD2D_MEM_HOST or FD2D_MEM_DEVICE");
+  ctx->memspace = memspace;
+  return FD2D_OK;
+}
+
+fd2d_status fd2d_ctx_set_precision(fd2d_ctx* ctx, int32_t precision) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  if (precision != FD2D_PREC_FP64 && precision != FD2D_PREC_FP32)
+    return set_error(ctx, FD2D_ERR_ARG, "precision must be FD2D_PREC_FP64 or FD2D_PREC_FP32");
+  ctx->precision = precision;
+  return FD2D_OK;
+}
+
+fd2d_status fd2d_ctx_synchronize(fd2d_ctx* ctx) {
+  FD2D_TRY(check_ctx(ctx));
+  FD2D_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  int herr = 0;
+  FD2D_CUDA(ctx, cudaMemcpy(&herr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) {
+    cudaMemset(ctx->d_err, 0, sizeof(int));
+    return set_error(ctx, FD2D_ERR_TIMEOUT, "a bounded device-side wait gave up (code " + std::to_string(herr) + ")");
+  }
+  return FD2D_OK;
+}
+
+int64_t fd2d_ctx_kernel_launches(const fd2d_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+const char* fd2d_last_error(const fd2d_ctx* ctx) {
+  if (ctx) return ctx->last_error.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  thread_local std::string copy;
+  copy = g_global_err;
+  return copy.c_str();
+}
+
+fd2d_status fd2d_query_sizes(const fd2d_config* cfg, int32_t nr, fd2d_sizes* out) {
+  if (!out) return set_error(nullptr, FD2D_ERR_ARG, "out is NULL");
+  if (nr < 0) return set_error(nullptr, FD2D_ERR_ARG, "nr < 0");
+  Geometry g;
+  std::string err;
+  fd2d_status s = make_geometry(cfg, g, err);
+  if (s != FD2D_OK) return set_error(nullptr, s, err);
+  const int64_t np = g.npts();
+  int nfw = 0;
+  for (int n = g.nt; n <= 2 * g.nt - 1; ++n) nfw += (n % g.fw == 0);
+  out->ntc = g.ntc;
+  out->n_fw_green = nfw;
+  out->n_fw_corr = g.ntc / g.fw;
+  out->n_kernel_planes = g.nb == 0 ? 2 : g.nb + 1;
+  out->npts = np;
+  out->G_fft = np * g.K;
+  out->G_out = np * nfw;
+  out->seis_green = (int64_t)nr * g.nt;
+  out->C_out = np * out->n_fw_corr;
+  out->seis_corr = (int64_t)nr * g.ntc;
+  out->K = np * out->n_kernel_planes;
+  return FD2D_OK;
+}
+
+fd2d_status fd2d_forward1_green(fd2d_ctx* ctx, const fd2d_config* cfg, const double* mu,
+                                const double* rho, const double* src, int32_t ns,
+                                const double* rec, int32_t nr, int32_t mode, const double* dmu,
+                                const float* G_in, int32_t n_G_in, double* G_fft_re,
+                                double* G_fft_im, float* G_out, double* seismograms) {
+  FD2D_TRY(check_ctx(ctx));
+  Geometry g;
+  std::string err;
+  fd2d_status s = make_geometry(cfg, g, err);
+  if (s != FD2D_OK) return set_error(ctx, s, err);
+  if (!mu || !rho) return set_error(ctx, FD2D_ERR_ARG, "mu and rho are required");
+  if (ns < 0 || nr < 0 || n_G_in < 0) return set_error(ctx, FD2D_ERR_ARG, "negative count");
+  if (!G_fft_re || !G_fft_im) return set_error(ctx, FD2D_ERR_ARG, "G_fft output planes are required");
+  if (nr > 0 && !seismograms) return set_error(ctx, FD2D_ERR_ARG, "seismograms output is required");
+  int nfw = 0;
+  for (int n = g.nt; n <= 2 * g.nt - 1; ++n) nfw += (n % g.fw == 0);
+  if (mode != 0 && nfw > 0 && !G_out) return set_error(ctx, FD2D_ERR_ARG, "G_out output is required when mode != 0");
+  if (dmu && (!G_in || n_G_in < g.nt))
+    return set_error(ctx, FD2D_ERR_INDEX, "Born run needs G_in with at least nt snapshots (G_in(:,:,i_fw_in) for i_fw_in = 1..nt)");
+  const size_t np = (size_t)g.npts();
+  SolveArgs a;
+  a.mode = mode;
+  std::vector<double> hp;
+  FD2D_TRY(host_points(ctx, src, ns, hp));
+  FD2D_TRY(point_indices(ctx, g, hp.data(), ns, "src", a.src_idx));
+  FD2D_TRY(host_points(ctx, rec, nr, hp));
+  FD2D_TRY(point_indices(ctx, g, hp.data(), nr, "rec", a.rec_idx));
+  const void* p;
+  FD2D_TRY(stage_in(ctx, "in.mu", mu, np * 8, &p)); a.mu = (const double*)p;
+  FD2D_TRY(stage_in(ctx, "in.rho", rho, np * 8, &p)); a.rho = (const double*)p;
+  FD2D_TRY(stage_in(ctx, "in.dmu", dmu, dmu ? np * 8 : 0, &p)); a.dmu = (const double*)p;
+  if (dmu) {
+    FD2D_TRY(stage_in(ctx, "in.G_in", G_in, np * 4 * (size_t)g.nt, &p));
+    a.G_in = (const float*)p;
+    a.n_G_in = g.nt;
+  }
+  void* q;
+  FD2D_TRY(out_buffer(ctx, "out.G_re", G_fft_re, np * 8 * g.K, &q)); a.G_re = (double*)q;
+  FD2D_TRY(out_buffer(ctx, "out.G_im", G_fft_im, np * 8 * g.K, &q)); a.G_im = (double*)q;
+  if (mode != 0 && nfw > 0) {
+    FD2D_TRY(out_buffer(ctx, "out.G_out", G_out, np * 4 * nfw, &q));
+    a.G_out = (float*)q;
+  }
+  FD2D_TRY(out_buffer(ctx, "out.seis", seismograms, (size_t)nr * g.nt * 8, &q)); a.seis = (double*)q;
+  s = ctx->precision == FD2D_PREC_FP64 ? fp64_forward1(ctx, g, a) : fp32_forward1(ctx, g, a);
+  if (s != FD2D_OK) return s;
+  FD2D_TRY(stage_out(ctx, G_fft_re, a.G_re, np * 8 * g.K));
+  FD2D_TRY(stage_out(ctx, G_fft_im, a.G_im, np * 8 * g.K));
+  if (a.G_out) FD2D_TRY(stage_out(ctx, G_out, a.G_out, np * 4 * nfw));
+  FD2D_TRY(stage_out(ctx, seismograms, a.seis, (size_t)nr * g.nt * 8));
+  return finish(ctx);
+}
+
+fd2d_status fd2d_forward2_correlation(fd2d_ctx* ctx, const fd2d_config* cfg, const double* mu,
+                                      const double* rho, const double* G_fft_re,
+                                      const double* G_fft_im, int32_t n_G, const double* spectrum,
+                                      int32_t n_noise_sources, const double* source_dist,
+                                      int32_t n_dist, const double* rec, int32_t nr, int32_t mode,
+                                      const double* dmu, const float* C_in, int32_t n_C_in,
+                                      double* seismograms, float* C_out) {
+  FD2D_TRY(check_ctx(ctx));
+  Geometry g;
+  std::string err;
+  fd2d_status s = make_geometry(cfg, g, err);
+  if (s != FD2D_OK) return set_error(ctx, s, err);
+  if (!mu || !rho) return set_error(ctx, FD2D_ERR_ARG, "mu and rho are required");
+  if (nr < 0 || n_G < 0 || n_C_in < 0 || n_dist < 0) return set_error(ctx, FD2D_ERR_ARG, "negative count");
+  if (!G_fft_re || !G_fft_im) return set_error(ctx, FD2D_ERR_ARG, "G_fft is required");
+  if (n_G < g.K) return set_error(ctx, FD2D_ERR_INDEX, "G_fft has fewer than n_sample planes");
+  if (!spectrum || n_noise_sources < 1) return set_error(ctx, FD2D_ERR_ARG, "spectrum is required");
+  if (g.nb == 0 && n_noise_sources != 1)
+    return set_error(ctx, FD2D_ERR_SHAPE, "with n_basis_fct == 0 the reference handles one noise source (interpol_matrix * distribution needs one plane)");
+  if (!source_dist || n_dist != (g.nb == 0 ? n_noise_sources : g.nb))
+    return set_error(ctx, FD2D_ERR_SHAPE, "source_dist must have n_noise_sources (n_basis_fct == 0) or n_basis_fct planes");
+  if (nr > 0 && !seismograms) return set_error(ctx, FD2D_ERR_ARG, "seismograms output is required");
+  const int nfw = g.ntc / g.fw;
+  if (mode != 0 && nfw > 0 && !C_out) return set_error(ctx, FD2D_ERR_ARG, "C_out output is required when mode != 0");
+  if (dmu && (!C_in || n_C_in < g.ntc))
+    return set_error(ctx, FD2D_ERR_INDEX, "Born run needs C_in with 2*nt-1 snapshots (C_in(:,:,n+1))");
+  const size_t np = (size_t)g.npts();
+  SolveArgs a;
+  a.mode = mode;
+  std::vector<double> hp;
+  FD2D_TRY(host_points(ctx, rec, nr, hp));
+  FD2D_TRY(point_indices(ctx, g, hp.data(), nr, "rec", a.rec_idx));
+  const void* p;
+  FD2D_TRY(stage_in(ctx, "in.mu", mu, np * 8, &p)); a.mu = (const double*)p;
+  FD2D_TRY(stage_in(ctx, "in.rho", rho, np * 8, &p)); a.rho = (const double*)p;
+  FD2D_TRY(stage_in(ctx, "in.dmu", dmu, dmu ? np * 8 : 0, &p)); a.dmu = (const double*)p;
+  FD2D_TRY(stage_in(ctx, "in.G_re", G_fft_re, np * 8 * g.K, &p)); a.Gin_re = (const double*)p;
+  FD2D_TRY(stage_in(ctx, "in.G_im", G_fft_im, np * 8 * g.K, &p)); a.Gin_im = (const double*)p;
+  a.n_G = g.K;
+  FD2D_TRY(stage_in(ctx, "in.spectrum", spectrum, (size_t)g.K * n_noise_sources * 8, &p));
+  a.spectrum = (const double*)p;
+  a.n_src = n_noise_sources;
+  FD2D_TRY(stage_in(ctx, "in.source_dist", source_dist, np * 8 * n_dist, &p));
+  a.source_dist = (const double*)p;
+  a.n_dist = n_dist;
+  if (dmu) {
+    FD2D_TRY(stage_in(ctx, "in.C_in", C_in, np * 4 * (size_t)g.ntc, &p));
+    a.C_in = (const float*)p;
+    a.n_C_in = g.ntc;
+  }
+  // The host copy of spectrum is needed by both drivers (effective spectrum per k).
+  void* q;
+  if (mode != 0 && nfw > 0) {
+    FD2D_TRY(out_buffer(ctx, "out.C_out", C_out, np * 4 * nfw, &q));
+    a.C_out = (float*)q;
+  }
+  FD2D_TRY(out_buffer(ctx, "out.seis", seismograms, (size_t)nr * g.ntc * 8, &q)); a.seis = (double*)q;
+  s = ctx->precision == FD2D_PREC_FP64 ? fp64_correlation(ctx, g, a) : fp32_correlation(ctx, g, a);
+  if (s != FD2D_OK) return s;
+  if (a.C_out) FD2D_TRY(stage_out(ctx, C_out, a.C_out, np * 4 * nfw));
+  FD2D_TRY(stage_out(ctx, seismograms, a.seis, (size_t)nr * g.ntc * 8));
+  return finish(ctx);
+}
+
+fd2d_status fd2d_noise_adjoint(fd2d_ctx* ctx, const fd2d_config* cfg, const double* mu,
+                               const double* rho, const float* u_fwd, int32_t n_u_fwd,
+                               const double* stf_re, const double* stf_im,
+                               const int64_t stf_dims[3], const double* src, int32_t ns,
+                               const double* rec, int32_t nr, const double* spectrum,
+                               int32_t n_noise_sources, const double* source_dist, int32_t n_dist,
+                               const double* G_fft_re, const double* G_fft_im, int32_t n_G,
+                               int32_t mode, const double* dmu, const float* u_in, int32_t n_u_in,
+                               double* K, double* stf_fft_re, double* stf_fft_im, float* u_out,
+                               double* seismograms) {
+  FD2D_TRY(check_ctx(ctx));
+  Geometry g;
+  std::string err;
+  fd2d_status s = make_geometry(cfg, g, err);
+  if (s != FD2D_OK) return set_error(ctx, s, err);
+  if (!mu || !rho) return set_error(ctx, FD2D_ERR_ARG, "mu and rho are required");
+  if (ns < 0 || nr < 0 || n_G < 0 || n_u_in < 0 || n_u_fwd < 0 || n_dist < 0 || n_noise_sources < 0)
+    return set_error(ctx, FD2D_ERR_ARG, "negative count");
+  if (!(mode == 0 || mode == 1 || mode == 10 || mode == 11 || mode == 12 || mode == 13))
+    return set_error(ctx, FD2D_ERR_ARG, "mode must be 0, 1, 10, 11, 12 or 13");
+  if (!K || !stf_fft_re || !stf_fft_im) return set_error(ctx, FD2D_ERR_ARG, "K and stf_fft outputs are required");
+  if (nr > 0 && !seismograms) return set_error(ctx, FD2D_ERR_ARG, "seismograms output is required");
+  const size_t np = (size_t)g.npts();
+  const int nfw = g.ntc / g.fw;
+  const bool save_u = mode == 11 || mode == 13;
+  if (save_u && nfw > 0 && !u_out) return set_error(ctx, FD2D_ERR_ARG, "u_out output is required for modes 11 and 13");
+  SolveArgs a;
+  a.mode = mode;
+  int64_t d0 = 0, d1 = 0, d2 = 0;
+  if (stf_dims) { d0 = stf_dims[0]; d1 = stf_dims[1]; d2 = stf_dims[2]; }
+  if (d0 < 0 || d1 < 0 || d2 < 0) return set_error(ctx, FD2D_ERR_ARG, "negative stf dimension");
+  const bool stf_empty = !stf_re || d0 * d1 * d2 == 0;
+  const int64_t size3 = stf_empty ? 1 : d2;
+  if (!stf_empty) {
+    if (size3 == 1) {
+      if (d0 < ns) return set_error(ctx, FD2D_ERR_INDEX, "stf has fewer rows than adjoint sources");
+      int nt_loop = g.ntc;
+      if (d1 < nt_loop && ns > 0) return set_error(ctx, FD2D_ERR_INDEX, "stf has fewer columns than time steps");
+    } else {
+      if (d0 != g.nx || d1 != g.nz) return set_error(ctx, FD2D_ERR_SHAPE, "field stf must be nx-by-nz-by-n_sample");
+      if (d2 < g.K) return set_error(ctx, FD2D_ERR_INDEX, "field stf has fewer than n_sample planes");
+    }
+  }
+  const bool have_dist = source_dist && n_dist > 0;
+  if (have_dist) {
+    if (!spectrum || n_noise_sources < 1) return set_error(ctx, FD2D_ERR_SHAPE, "source_dist needs a spectrum");
+    if (g.nb == 0 && n_noise_sources != 1)
+      return set_error(ctx, FD2D_ERR_SHAPE, "with n_basis_fct == 0 the reference handles one noise source");
+    if (n_dist != (g.nb == 0 ? n_noise_sources : g.nb))
+      return set_error(ctx, FD2D_ERR_SHAPE, "source_dist must have n_noise_sources (n_basis_fct == 0) or n_basis_fct planes");
+  }
+  const bool Gvalid = G_fft_re && n_G == g.K;
+  if (Gvalid && (!G_fft_im || !spectrum || n_noise_sources != 1))
+    return set_error(ctx, FD2D_ERR_SHAPE, "the source kernel needs G_fft planes and a one-column spectrum");
+  // i_ftc is shared by the field-source injection and the stf_fft DFT
+  // (code/run_noise_adjoint.m:265,343): both active overruns the table.
+  if (!stf_empty && size3 != 1 && (mode == 1 || mode == 12 || mode == 13)) {
+    int nt_loop = (mode == 1) ? g.nt : g.ntc;
+    int steps = nt_loop / g.fs;
+    if (2 * steps > g.ntc / g.fs)
+      return set_error(ctx, FD2D_ERR_INDEX, "field source together with stf_fft (modes 1/12/13) overruns fft_coeff, as in the reference");
+  }
+  std::vector<double> hp;
+  FD2D_TRY(host_points(ctx, src, ns, hp));
+  FD2D_TRY(point_indices(ctx, g, hp.data(), ns, "src", a.src_idx));
+  FD2D_TRY(host_points(ctx, rec, nr, hp));
+  FD2D_TRY(point_indices(ctx, g, hp.data(), nr, "rec", a.rec_idx));
+  const void* p;
+  FD2D_TRY(stage_in(ctx, "in.mu", mu, np * 8, &p)); a.mu = (const double*)p;
+  FD2D_TRY(stage_in(ctx, "in.rho", rho, np * 8, &p)); a.rho = (const double*)p;
+  const bool born = dmu && u_in && n_u_in == g.ntc;
+  if (born) {
+    FD2D_TRY(stage_in(ctx, "in.dmu", dmu, np * 8, &p)); a.dmu = (const double*)p;
+    FD2D_TRY(stage_in(ctx, "in.C_in", u_in, np * 4 * (size_t)g.ntc, &p)); a.C_in = (const float*)p;
+    a.n_C_in = g.ntc;
+  }
+  if (u_fwd && n_u_fwd > 0) {
+    FD2D_TRY(stage_in(ctx, "in.u_fwd", u_fwd, np * 4 * (size_t)n_u_fwd, &p));
+    a.u_fwd = (const float*)p;
+    a.n_u_fwd = n_u_fwd;
+  }
+  if (!stf_empty) {
+    a.stf_dims[0] = d0; a.stf_dims[1] = d1; a.stf_dims[2] = d2;
+    const size_t n_stf = (size_t)(d0 * d1 * d2);
+    FD2D_TRY(stage_in(ctx, "in.stf_re", stf_re, n_stf * 8, &p)); a.stf_re = (const double*)p;
+    if (stf_im) { FD2D_TRY(stage_in(ctx, "in.stf_im", stf_im, n_stf * 8, &p)); a.stf_im = (const double*)p; }
+  }
+  if (spectrum && n_noise_sources > 0) {
+    FD2D_TRY(stage_in(ctx, "in.spectrum", spectrum, (size_t)g.K * n_noise_sources * 8, &p));
+    a.spectrum = (const double*)p;
+    a.n_src = n_noise_sources;
+  }
+  if (have_dist) {
+    FD2D_TRY(stage_in(ctx, "in.source_dist", source_dist, np * 8 * n_dist, &p));
+    a.source_dist = (const double*)p;
+    a.n_dist = n_dist;
+  }
+  if (Gvalid) {
+    FD2D_TRY(stage_in(ctx, "in.G_re", G_fft_re, np * 8 * g.K, &p)); a.Gin_re = (const double*)p;
+    FD2D_TRY(stage_in(ctx, "in.G_im", G_fft_im, np * 8 * g.K, &p)); a.Gin_im = (const double*)p;
+    a.n_G = g.K;
+  }
+  const int nkp = g.nb == 0 ? 2 : g.nb + 1;
+  void* q;
+  FD2D_TRY(out_buffer(ctx, "out.K", K, np * 8 * nkp, &q)); a.Kout = (double*)q;
+  FD2D_TRY(out_buffer(ctx, "out.sf_re", stf_fft_re, np * 8 * g.K, &q)); a.sf_re = (double*)q;
+  FD2D_TRY(out_buffer(ctx, "out.sf_im", stf_fft_im, np * 8 * g.K, &q)); a.sf_im = (double*)q;
+  if (save_u && nfw > 0) {
+    FD2D_TRY(out_buffer(ctx, "out.u_out", u_out, np * 4 * nfw, &q));
+    a.C_out = (float*)q;
+  }
+  FD2D_TRY(out_buffer(ctx, "out.seis", seismograms, (size_t)nr * g.ntc * 8, &q)); a.seis = (double*)q;
+  s = ctx->precision == FD2D_PREC_FP64 ? fp64_adjoint(ctx, g, a) : fp32_adjoint(ctx, g, a);
+  if (s != FD2D_OK) return s;
+  FD2D_TRY(stage_out(ctx, K, a.Kout, np * 8 * nkp));
+  FD2D_TRY(stage_out(ctx, stf_fft_re, a.sf_re, np * 8 * g.K));
+  FD2D_TRY(stage_out(ctx, stf_fft_im, a.sf_im, np * 8 * g.K));
+  if (a.C_out) FD2D_TRY(stage_out(ctx, u_out, a.C_out, np * 4 * nfw));
+  FD2D_TRY(stage_out(ctx, seismograms, a.seis, (size_t)nr * g.ntc * 8));
+  return finish(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,212 @@
+/*
+ * fd2d.h -- C ABI of the GB300 fd2d_noise wave-propagation library (libfd2d.so).
+ *
+ * The three solver entry points replace the MATLAB solvers of fd2d_noise,
+ * which its callers reach under the MATLAB-Coder names run_*_mex:
+ *
+ *   fd2d_forward1_green        <- code/run_forward1_green.m:1
+ *   fd2d_forward2_correlation  <- code/run_forward2_correlation.m:1
+ *   fd2d_noise_adjoint         <- code/run_noise_adjoint.m:1
+ *
+ * Argument order and meaning follow the MATLAB signatures and the codegen type
+ * specification in code/mex_functions/compile_all.m:5-34.  The MATLAB solvers
+ * read their configuration from input_parameters(), input_interferometry() and
+ * absorb_specs() (input/input_parameters.m:2-88, input/input_interferometry.m:2-21,
+ * input/absorb_specs.m:2-15); here that configuration travels explicitly in
+ * fd2d_config.
+ *
+ * Conventions
+ *  - Arrays are column-major with x fastest, exactly as MATLAB stores them:
+ *    element (ix, iz, k) of an nx-by-nz-by-K array is at ix + nx*(iz + nz*k)
+ *    (0-based).  A 2-D n-by-m array (src, rec, spectrum, seismograms) has
+ *    element (i, j) at i + n*j.
+ *  - Complex arrays are split into separate real and imaginary planes (the
+ *    non-interleaved MEX convention).
+ *  - A NULL pointer (with count 0) stands for the MATLAB empty array [] /
+ *    single([]) / complex([]).
+ *  - Outputs are caller-allocated; fd2d_query_sizes() gives their sizes.  The
+ *    library never frees caller memory.
+ *  - By default every pointer is a HOST pointer and a call is synchronous.
+ *    After fd2d_ctx_set_memspace(ctx, FD2D_MEM_DEVICE) every array pointer is a
+ *    device pointer of the context's GPU and the call is asynchronous on the
+ *    context's stream (scalars and fd2d_config.f_sample stay on the host).
+ *  - Errors are returned as fd2d_status; fd2d_last_error() gives the message.
+ *    The library never exits or aborts.
+ */
+#ifndef FD2D_H
+#define FD2D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FD2D_ABI_VERSION 1
+
+typedef enum fd2d_status {
+  FD2D_OK = 0,
+  FD2D_ERR_ARG = 1,       /* NULL where an array is required, bad scalar      */
+  FD2D_ERR_SHAPE = 2,     /* array sizes inconsistent with the configuration   */
+  FD2D_ERR_ORDER = 3,     /* finite-difference order not in {2, 4, 6, 8}       */
+  FD2D_ERR_OOM = 4,       /* device memory exhausted                           */
+  FD2D_ERR_CUDA = 5,      /* CUDA runtime or launch error                      */
+  FD2D_ERR_TIMEOUT = 6,   /* a bounded device-side wait gave up                */
+  FD2D_ERR_INDEX = 7,     /* the MATLAB solver would index out of range here   */
+  FD2D_ERR_NO_DEVICE = 8, /* no usable CUDA device                             */
+  FD2D_ERR_UNSUPPORTED = 9
+} fd2d_status;
+
+typedef enum fd2d_precision {
+  FD2D_PREC_FP64 = 0, /* plain FP64 form: the reference arithmetic on the GPU  */
+  FD2D_PREC_FP32 = 1  /* FP32 stencil + split-TF32 tensor-core contractions     */
+} fd2d_precision;
+
+typedef enum fd2d_memspace { FD2D_MEM_HOST = 0, FD2D_MEM_DEVICE = 1 } fd2d_memspace;
+
+/* Hidden inputs of the MATLAB solvers, made explicit. */
+typedef struct fd2d_config {
+  /* input_parameters() -- input/input_parameters.m:2-88 */
+  double Lx, Lz;          /* domain extent [m]                                  */
+  int32_t nx, nz;         /* grid points                                        */
+  double dt;              /* time step [s]                                      */
+  int32_t nt;             /* forward time steps                                 */
+  int32_t order;          /* FD order: 2 and 4 as in the reference; 6 and 8 are
+                             the staggered-grid extension (no reference analogue) */
+  int32_t n_basis_fct;    /* frequency bands of the source model (0 = none)     */
+  int32_t fw_nth;         /* store every fw_nth step of the forward field       */
+  /* input_interferometry() -- input/input_interferometry.m:16-21 */
+  int32_t n_sample;       /* number of frequencies                              */
+  const double* f_sample; /* n_sample frequencies [Hz], evenly spaced (host)    */
+  int32_t freq_samp;      /* DFT / injection decimation                         */
+  /* absorb_specs() -- input/absorb_specs.m:8-15 */
+  double absorb_width;    /* taper width [m]                                    */
+  int32_t absorb_left, absorb_right, absorb_top, absorb_bottom;
+} fd2d_config;
+
+/* Output sizes (in elements) for a configuration and receiver count. */
+typedef struct fd2d_sizes {
+  int32_t ntc;            /* 2*nt-1: correlation / adjoint time steps          */
+  int32_t n_fw_green;     /* G_out planes (code/run_forward1_green.m:98-103)   */
+  int32_t n_fw_corr;      /* C_out / u_out planes: floor(ntc/fw_nth)           */
+  int32_t n_kernel_planes;/* K planes: n_basis_fct+1, or 2 when n_basis_fct==0 */
+  int64_t npts;           /* nx*nz                                             */
+  int64_t G_fft;          /* nx*nz*n_sample (per real/imag plane set)          */
+  int64_t G_out;          /* nx*nz*n_fw_green                                  */
+  int64_t seis_green;     /* nr*nt                                             */
+  int64_t C_out;          /* nx*nz*n_fw_corr                                   */
+  int64_t seis_corr;      /* nr*ntc                                            */
+  int64_t K;              /* nx*nz*n_kernel_planes                             */
+} fd2d_sizes;
+
+typedef struct fd2d_ctx fd2d_ctx;
+
+/* ---- context --------------------------------------------------------------- */
+int32_t fd2d_abi_version(void);
+/* Create a context on CUDA device `device` computing in `precision`. */
+fd2d_status fd2d_ctx_create(int32_t device, int32_t precision, fd2d_ctx** out);
+fd2d_status fd2d_ctx_destroy(fd2d_ctx* ctx);
+/* Use `stream` (a cudaStream_t) for all work of this context; NULL = own stream. */
+fd2d_status fd2d_ctx_set_stream(fd2d_ctx* ctx, void* stream);
+fd2d_status fd2d_ctx_set_memspace(fd2d_ctx* ctx, int32_t memspace);
+fd2d_status fd2d_ctx_set_precision(fd2d_ctx* ctx, int32_t precision);
+/* Wait for all work queued on the context's stream. */
+fd2d_status fd2d_ctx_synchronize(fd2d_ctx* ctx);
+/* Kernels launched by this context since creation (instrumentation). */
+int64_t fd2d_ctx_kernel_launches(const fd2d_ctx* ctx);
+/* Message of the last error on this context ("" if none). ctx may be NULL for
+   errors raised before a context existed. */
+const char* fd2d_last_error(const fd2d_ctx* ctx);
+
+/* Validate a configuration and compute output sizes (no GPU needed). */
+fd2d_status fd2d_query_sizes(const fd2d_config* cfg, int32_t nr, fd2d_sizes* out);
+
+/* ---- solvers ----------------------------------------------------------------
+ * [G_fft, G_out, seismograms] = run_forward1_green(mu, rho, src, rec, mode, dmu, G_in)
+ * code/run_forward1_green.m:1-201.
+ *   mu, rho      nx*nz
+ *   src          ns-by-2 (x, z) [m]      rec   nr-by-2
+ *   mode         0: no wavefield output; otherwise G_out is stored
+ *   dmu          nx*nz or NULL; when given the run is the Born (dG) run driven
+ *                by dt*dmu*grad(G_in) and the point source is off
+ *   G_in         nx*nz*n_G_in single, needs n_G_in >= nt when dmu is given
+ *   G_fft_re/im  out, nx*nz*n_sample, returned conjugated as the reference does
+ *   G_out        out, nx*nz*n_fw_green single (only written when mode != 0)
+ *   seismograms  out, nr*nt (velocity at the receivers)                       */
+fd2d_status fd2d_forward1_green(fd2d_ctx* ctx, const fd2d_config* cfg,
+                                const double* mu, const double* rho,
+                                const double* src, int32_t ns,
+                                const double* rec, int32_t nr,
+                                int32_t mode,
+                                const double* dmu,
+                                const float* G_in, int32_t n_G_in,
+                                double* G_fft_re, double* G_fft_im,
+                                float* G_out,
+                                double* seismograms);
+
+/* [seismograms, C_out] = run_forward2_correlation(mu, rho, G_fft, spectrum,
+ *                                   source_dist, rec, mode, dmu, C_in)
+ * code/run_forward2_correlation.m:1-254.
+ *   G_fft_re/im  nx*nz*n_G (n_G >= n_sample): conjugated Green spectrum
+ *   spectrum     n_sample-by-n_noise_sources
+ *   source_dist  nx*nz*n_dist: n_dist == n_noise_sources when n_basis_fct == 0
+ *                (the reference only runs with one), n_dist == n_basis_fct
+ *                otherwise
+ *   dmu, C_in    Born term -dmu*grad(C_in(n) - C_in(n+1)); C_in needs ntc planes
+ *   seismograms  out, nr*ntc: displacement at the receivers = the correlations
+ *   C_out        out, nx*nz*n_fw_corr single (only written when mode != 0)    */
+fd2d_status fd2d_forward2_correlation(fd2d_ctx* ctx, const fd2d_config* cfg,
+                                      const double* mu, const double* rho,
+                                      const double* G_fft_re, const double* G_fft_im,
+                                      int32_t n_G,
+                                      const double* spectrum, int32_t n_noise_sources,
+                                      const double* source_dist, int32_t n_dist,
+                                      const double* rec, int32_t nr,
+                                      int32_t mode,
+                                      const double* dmu,
+                                      const float* C_in, int32_t n_C_in,
+                                      double* seismograms,
+                                      float* C_out);
+
+/* [K, stf_fft, u_out, seismograms] = run_noise_adjoint(mu, rho, u_fwd, stf, src,
+ *                 rec, spectrum, source_dist, G_fft, mode, dmu, u_in)
+ * code/run_noise_adjoint.m:1-368.
+ *   u_fwd        nx*nz*n_u_fwd single forward snapshots (NULL = none: no K_mu)
+ *   stf_re/im    stf_dims = {d0, d1, d2}.  d2 == 1: point adjoint sources,
+ *                d0 >= ns rows by d1 >= ntc columns (only the real part is used).
+ *                d2 > 1: field source, nx*nz*d2 with d2 >= n_sample.
+ *                NULL / d0*d1*d2 == 0: no source.
+ *   src          ns-by-2 adjoint source positions
+ *   spectrum     n_sample-by-n_noise_sources (NULL if unused)
+ *   source_dist  nx*nz*n_dist (NULL: no field source)
+ *   G_fft_re/im  nx*nz*n_G; the source kernel is built when n_G == n_sample
+ *   mode         0, 1, 10, 11, 12, 13 as in code/run_noise_adjoint.m:17-22
+ *   dmu, u_in    Born term; active when u_in has exactly ntc planes
+ *   K            out, nx*nz*n_kernel_planes: source kernel planes then K_mu
+ *   stf_fft_re/im out, nx*nz*n_sample (written for modes 1, 12, 13; zero else)
+ *   u_out        out, nx*nz*n_fw_corr single (modes 11 and 13)
+ *   seismograms  out, nr*ntc                                                   */
+fd2d_status fd2d_noise_adjoint(fd2d_ctx* ctx, const fd2d_config* cfg,
+                               const double* mu, const double* rho,
+                               const float* u_fwd, int32_t n_u_fwd,
+                               const double* stf_re, const double* stf_im,
+                               const int64_t stf_dims[3],
+                               const double* src, int32_t ns,
+                               const double* rec, int32_t nr,
+                               const double* spectrum, int32_t n_noise_sources,
+                               const double* source_dist, int32_t n_dist,
+                               const double* G_fft_re, const double* G_fft_im,
+                               int32_t n_G,
+                               int32_t mode,
+                               const double* dmu,
+                               const float* u_in, int32_t n_u_in,
+                               double* K,
+                               double* stf_fft_re, double* stf_fft_im,
+                               float* u_out,
+                               double* seismograms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FD2D_H */
