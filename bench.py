@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Benchmark of the fd2d_noise wave-propagation hot path on GB300.
+
+Metric: grid-point updates per second (one (ix,iz) node advanced one time step
+of one solve; a reference station costs nx*nz*(nt + 2nt-1) updates: its Green
+run plus its correlation run) of the FP32 form, beside the plain FP64 GPU form
+and the CPU restatement of the reference (the oracle).
+
+One step = every reference station of the workload: run_forward1_green (mode 0)
+followed by run_forward2_correlation (mode 0), i.e. code/calculate_data.m:189-202.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun every rank runs the full workload on its own GPU (independent
+replicas, weak scaling); the timed region is bracketed by a barrier and a
+device synchronisation and the max over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+B_STEP_V = 36   # algorithmic bytes per update, Green step: read v,sxy,szy,dt/rho,taper,dt*mu; write v,sxy,szy
+B_STEP_VU = 44  # correlation step: + read/write u
+METRIC = "Gpt-updates/s batched FP32 vs plain FP64 GPU at <=1e-4 rel L2; p50/p99 latency"
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == kernel and parts[1] == workload:
+                try:
+                    return float(parts[2])
+                except ValueError:
+                    return None
+    return None
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clk", suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                c = [x.strip() for x in line.split(",")]
+                if len(c) >= 9:
+                    rows.append(c)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_sample(w, nt_cpu: int, threads: int):
+    """Times the FP64 CPU oracle on a truncated-nt sample of the same workload."""
+    from oracle import pyoracle
+    pyoracle.build()
+    pyoracle.set_threads(threads)
+    cfg = w.cfg.replace(nt=nt_cpu)
+    t0 = time.perf_counter()
+    G, _, _ = pyoracle.forward1_green(cfg, w.mu, w.rho, w.ref_stations[:1], w.receivers, 0)
+    pyoracle.forward2_correlation(cfg, w.mu, w.rho, G, w.spectrum, w.source_dist, w.receivers, 0)
+    dt = time.perf_counter() - t0
+    gpt = cfg.npts * (cfg.nt + cfg.ntc)
+    return gpt / dt / 1e9, dt, gpt, cfg
+
+
+def run_reference(args, w, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    vals = []
+    dts = []
+    for _ in range(args.warmup):
+        cpu_sample(w, args.cpu_nt, threads)
+    for _ in range(args.steps):
+        v, dt, gpt, cfg = cpu_sample(w, args.cpu_nt, threads)
+        vals.append(v)
+        dts.append(dt)
+    value = statistics.median(vals)
+    sample = (f"one reference station of {w.name} with nt truncated to {args.cpu_nt}: "
+              f"Green {cfg.nt} + correlation {cfg.ntc} steps on {cfg.nx}x{cfg.nz}, K={cfg.n_sample}")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpt-updates/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.median(dts), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "nx": w.cfg.nx, "nz": w.cfg.nz, "nt": args.cpu_nt,
+                   "order": w.cfg.order, "n_sample": w.cfg.n_sample},
+        "cpu_baseline": {"value": value, "unit": "Gpt-updates/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Gpt-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference's MATLAB solvers (MATLAB unavailable), OpenMP over grid points",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="single_600_o8")
+    ap.add_argument("--cpu-nt", type=int, default=120)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+
+    from fd2d_noise_gb300.workloads import WORKLOADS
+    w = WORKLOADS[args.workload]()
+    if args.impl == "reference":
+        run_reference(args, w, world, rank)
+        return
+
+    import numpy as np
+    import torch
+    from fd2d_noise_gb300 import _lib
+    from fd2d_noise_gb300.build import build
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+
+    build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = local
+    cfg = w.cfg
+    np_, K, nr = cfg.npts, cfg.n_sample, w.receivers.shape[0]
+    n_ref = w.ref_stations.shape[0]
+
+    sess = DeviceSession(cfg, dev, "fp32")
+    mu = to_device(w.mu, np.float64, dev)
+    rho = to_device(w.rho, np.float64, dev)
+    spec = to_device(w.spectrum, np.float64, dev)
+    sd = to_device(w.source_dist, np.float64, dev)
+    rec = to_device(w.receivers, np.float64, dev)
+    refs = [to_device(w.ref_stations[i:i + 1], np.float64, dev) for i in range(n_ref)]
+    G_re, G_im, _, seis_g = sess.green_outputs(nr)
+    seis_c = [sess.zeros(nr * cfg.ntc, torch.float64) for _ in range(n_ref)]
+
+    def step(s: DeviceSession, outs):
+        for i in range(n_ref):
+            s.forward1_green(mu, rho, refs[i], 1, rec, nr, G_re, G_im, seis_g)
+            s.forward2_correlation(mu, rho, G_re, G_im, spec, 1, sd, 1, rec, nr, outs[i])
+
+    gpt_step = n_ref * w.gpt_per_station()
+    for _ in range(max(args.warmup, 0)):
+        step(sess, seis_c)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = Clocks(dev)
+    launches0 = sess.ctx.kernel_launches
+    sess.ctx.timing()  # reset
+    sess.ctx.set_timing(True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record()
+    for _ in range(args.steps):
+        step(sess, seis_c)
+    ev1.record()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    sess.ctx.set_timing(False)
+    tim = sess.ctx.timing()
+    launches = sess.ctx.kernel_launches - launches0
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * gpt_step * args.steps / (ms / 1e3) / 1e9
+
+    # roofline of the dominant kernel (the fused stencil step), live CUDA-event durations
+    (msV, nV, uV), (msVU, nVU, uVU), (msC, nC, uC) = tim
+    peak, peak_kind = measured_peaks()
+    st_ms = msV + msVU
+    achieved = (B_STEP_V * uV + B_STEP_VU * uVU) / (st_ms / 1e3) / 1e9 if st_ms > 0 else None
+    traffic = profiled_traffic("k32_step", w.name)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+            "kernel": "k32_step<R> (fused velocity/stress stencil)",
+            "peak_source": f"{peak_kind} hbm_gbs (burst)",
+            "stencil_ms_per_launch": st_ms / max(nV + nVU, 1),
+            "stencil_share_of_step": st_ms / ms if ms else None,
+            "contract_ms": msC, "contract_tflops": (2 * uC / (msC / 1e3) / 1e12) if msC else None}
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "Gpt-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": w.name, "nx": cfg.nx, "nz": cfg.nz, "nt": cfg.nt, "ntc": cfg.ntc,
+                   "order": cfg.order, "n_sample": K, "freq_samp": cfg.freq_samp,
+                   "reference_stations": n_ref, "receivers": nr,
+                   "gpt_per_step": gpt_step, "parallelism": f"replicas x{world}",
+                   "l2": "inputs > L2 per step (FP64 Green spectra %.2f GB, injection planes %.2f GB)"
+                         % (2 * np_ * K * 8 / 1e9, (cfg.ntc // cfg.freq_samp) * np_ * 4 / 1e9)},
+        "roofline": roof, "gpu_launches": launches, "clocks": clk,
+    }
+
+    if rank == 0 and not args.no_fp64:
+        # plain FP64 GPU form, one station, and the FP32 error against it
+        s64 = DeviceSession(cfg, dev, "fp64")
+        out64 = [sess.zeros(nr * cfg.ntc, torch.float64)]
+        s64.forward1_green(mu, rho, refs[0], 1, rec, nr, G_re, G_im, seis_g)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        s64.forward1_green(mu, rho, refs[0], 1, rec, nr, G_re, G_im, seis_g)
+        s64.forward2_correlation(mu, rho, G_re, G_im, spec, 1, sd, 1, rec, nr, out64[0])
+        e1.record()
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        v64 = w.gpt_per_station() / (ms64 / 1e3) / 1e9
+        c32 = seis_c[0].double()
+        c64 = out64[0]
+        rel = float(torch.linalg.norm(c32 - c64) / torch.linalg.norm(c64))
+        result["fp64_plain"] = {"value": v64, "unit": "Gpt-updates/s", "ms_per_station": ms64,
+                                "speedup_fp32_over_fp64": value / world / v64,
+                                "rel_l2_correlations_fp32_vs_fp64": rel}
+        s64.ctx.close()
+
+    if rank == 0 and not args.no_e2e:
+        result["e2e"] = e2e(args, w, dev)
+
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, dt, gpt, ccfg = cpu_sample(w, args.cpu_nt, threads)
+        result["cpu_baseline"] = {
+            "value": v, "unit": "Gpt-updates/s", "cores": threads, "kind": "port",
+            "sample": f"one station, nt truncated to {ccfg.nt} ({gpt:.3g} updates, {dt:.1f} s): "
+                      "FP64 C++ restatement of the reference solvers, MATLAB unavailable"}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def e2e(args, w, dev):
+    """Same metric through the C ABI with host buffers (pinned), copies inside the timed region."""
+    import ctypes
+    import numpy as np
+    import torch
+    from fd2d_noise_gb300 import _lib
+
+    cfg = w.cfg
+    np_, K, nr = cfg.npts, cfg.n_sample, w.receivers.shape[0]
+    n_ref = w.ref_stations.shape[0]
+
+    def pinned(a, dtype):
+        a = np.asarray(a, dtype=dtype).ravel(order="F")
+        t = torch.empty(a.size, dtype=torch.from_numpy(a[:1].copy()).dtype, pin_memory=True)
+        t.numpy()[:] = a
+        return t
+
+    def p(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    ctx = _lib.Context(dev, _lib.PREC_FP32)
+    mu, rho = pinned(w.mu, np.float64), pinned(w.rho, np.float64)
+    spec, sd = pinned(w.spectrum, np.float64), pinned(w.source_dist, np.float64)
+    rec = pinned(w.receivers, np.float64)
+    refs = [pinned(w.ref_stations[i:i + 1], np.float64) for i in range(n_ref)]
+    G_re = torch.empty(np_ * K, dtype=torch.float64, pin_memory=True)
+    G_im = torch.empty(np_ * K, dtype=torch.float64, pin_memory=True)
+    seis_g = torch.empty(nr * cfg.nt, dtype=torch.float64, pin_memory=True)
+    seis_c = torch.empty(nr * cfg.ntc, dtype=torch.float64, pin_memory=True)
+    c = cfg.to_c()
+    L = ctx.L
+
+    def step():
+        for i in range(n_ref):
+            _lib.check(L.fd2d_forward1_green(ctx.h, ctypes.byref(c), p(mu), p(rho), p(refs[i]), 1,
+                                             p(rec), nr, 0, None, None, 0, p(G_re), p(G_im), None,
+                                             p(seis_g)), ctx.h)
+            _lib.check(L.fd2d_forward2_correlation(ctx.h, ctypes.byref(c), p(mu), p(rho), p(G_re),
+                                                   p(G_im), K, p(spec), 1, p(sd), 1, p(rec), nr, 0,
+                                                   None, None, 0, p(seis_c), None), ctx.h)
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    gpt = n_ref * w.gpt_per_station() * args.steps
+    h2d = n_ref * (2 * (2 * np_ * 8) + 16 + 2 * nr * 16 + 2 * np_ * K * 8 + K * 8 + np_ * 8)
+    d2h = n_ref * (2 * np_ * K * 8 + nr * cfg.nt * 8 + nr * cfg.ntc * 8)
+    ctx.close()
+    return {"value": gpt / dt / 1e9, "unit": "Gpt-updates/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * dt / args.steps,
+            "path": "fd2d_forward1_green + fd2d_forward2_correlation, host (pinned) buffers"}
+
+
+if __name__ == "__main__":
+    main()

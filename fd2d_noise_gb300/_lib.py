@@ -30,7 +30,9 @@ EXPORTED = [
     "fd2d_ctx_set_memspace", "fd2d_ctx_set_precision", "fd2d_ctx_synchronize",
     "fd2d_ctx_kernel_launches", "fd2d_last_error", "fd2d_query_sizes",
     "fd2d_forward1_green", "fd2d_forward2_correlation", "fd2d_noise_adjoint",
+    "fd2d_ctx_set_timing", "fd2d_ctx_timing",
 ]
+TIMER_STEP_V, TIMER_STEP_VU, TIMER_CONTRACT, TIMER_COUNT = 0, 1, 2, 3
 
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
@@ -71,6 +73,9 @@ def load(path: str = LIB_PATH):
         L.fd2d_last_error.argtypes = [_vp]
         L.fd2d_last_error.restype = ctypes.c_char_p
         L.fd2d_query_sizes.argtypes = [_cfgp, _i32, ctypes.POINTER(FD2DSizes)]
+        L.fd2d_ctx_set_timing.argtypes = [_vp, _i32]
+        L.fd2d_ctx_timing.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i64),
+                                      ctypes.POINTER(_i64)]
         L.fd2d_forward1_green.argtypes = [
             _vp, _cfgp, _vp, _vp, _vp, _i32, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp]
         L.fd2d_forward2_correlation.argtypes = [
@@ -135,6 +140,17 @@ class Context:
     @property
     def kernel_launches(self) -> int:
         return int(self.L.fd2d_ctx_kernel_launches(self.h))
+
+    def set_timing(self, enable: bool):
+        check(self.L.fd2d_ctx_set_timing(self.h, 1 if enable else 0), self.h)
+
+    def timing(self):
+        """Per timer class: (milliseconds, launches, units); resets the counters."""
+        ms = (ctypes.c_double * TIMER_COUNT)()
+        n = (_i64 * TIMER_COUNT)()
+        u = (_i64 * TIMER_COUNT)()
+        check(self.L.fd2d_ctx_timing(self.h, ms, n, u), self.h)
+        return [(float(ms[c]), int(n[c]), int(u[c])) for c in range(TIMER_COUNT)]
 
 
 def query_sizes(cfg, nr: int) -> FD2DSizes:

@@ -86,6 +86,15 @@ struct fd2d_ctx {
   std::vector<std::pair<std::string, fd2d::DevBuf>> bufs;
   // device-side error flag of bounded waits (int32)
   int* d_err = nullptr;
+  // instrumentation (fd2d_ctx_set_timing)
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  struct TimerRec { int a, b, cls; int64_t units; };
+  std::vector<TimerRec> recs;
+  double t_ms[FD2D_TIMER_COUNT] = {0, 0, 0};
+  int64_t t_cnt[FD2D_TIMER_COUNT] = {0, 0, 0};
+  int64_t t_units[FD2D_TIMER_COUNT] = {0, 0, 0};
 };
 
 namespace fd2d {
@@ -98,6 +107,10 @@ fd2d_status workspace_t(fd2d_ctx* ctx, const char* name, size_t count, T** out) 
 }
 // Release every workspace buffer of the context.
 void free_workspace(fd2d_ctx* ctx);
+
+// Brackets the next launch(es) with timing events when instrumentation is on.
+int timer_begin(fd2d_ctx* ctx, cudaStream_t stream);
+void timer_end(fd2d_ctx* ctx, cudaStream_t stream, int begin, int cls, int64_t units);
 
 // Checks the last launch and counts it.
 fd2d_status after_launch(fd2d_ctx* ctx, const char* what);

@@ -71,7 +71,9 @@ __global__ __launch_bounds__(NT) void k_contract_simt(ContractArgs a) {
 fd2d_status contract(fd2d_ctx* ctx, cudaStream_t stream, const ContractArgs& a) {
   if (a.M <= 0 || a.N <= 0 || a.Kd <= 0) return FD2D_OK;
   dim3 grid((a.M + BM - 1) / BM, (a.N + BN - 1) / BN);
+  const int t0 = timer_begin(ctx, stream);
   k_contract_simt<<<grid, NT, 0, stream>>>(a);
+  timer_end(ctx, stream, t0, FD2D_TIMER_CONTRACT, (int64_t)a.M * a.N * a.Kd);
   return after_launch(ctx, "k_contract_simt");
 }
 

@@ -72,6 +72,30 @@ fd2d_status after_launch(fd2d_ctx* ctx, const char* what) {
   return FD2D_OK;
 }
 
+static int next_event(fd2d_ctx* ctx) {
+  if (ctx->ev_used == ctx->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return -1;
+    ctx->ev_pool.push_back(e);
+  }
+  return (int)ctx->ev_used++;
+}
+
+int timer_begin(fd2d_ctx* ctx, cudaStream_t stream) {
+  if (!ctx->timing) return -1;
+  int i = next_event(ctx);
+  if (i >= 0) cudaEventRecord(ctx->ev_pool[i], stream);
+  return i;
+}
+
+void timer_end(fd2d_ctx* ctx, cudaStream_t stream, int begin, int cls, int64_t units) {
+  if (!ctx->timing || begin < 0) return;
+  int i = next_event(ctx);
+  if (i < 0) return;
+  cudaEventRecord(ctx->ev_pool[i], stream);
+  ctx->recs.push_back({begin, i, cls, units});
+}
+
 fd2d_status stage_in(fd2d_ctx* ctx, const char* name, const void* src, size_t bytes, const void** dev) {
   if (!src || bytes == 0) {
     *dev = nullptr;
@@ -197,6 +221,7 @@ fd2d_status fd2d_ctx_destroy(fd2d_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   free_workspace(ctx);
+  for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -245,6 +270,37 @@ fd2d_status fd2d_ctx_synchronize(fd2d_ctx* ctx) {
   if (herr) {
     cudaMemset(ctx->d_err, 0, sizeof(int));
     return set_error(ctx, FD2D_ERR_TIMEOUT, "a bounded device-side wait gave up (code " + std::to_string(herr) + ")");
+  }
+  return FD2D_OK;
+}
+
+fd2d_status fd2d_ctx_set_timing(fd2d_ctx* ctx, int32_t enable) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  ctx->timing = enable != 0;
+  return FD2D_OK;
+}
+
+fd2d_status fd2d_ctx_timing(fd2d_ctx* ctx, double* ms, int64_t* launches, int64_t* units) {
+  FD2D_TRY(check_ctx(ctx));
+  FD2D_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (const auto& r : ctx->recs) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, ctx->ev_pool[r.a], ctx->ev_pool[r.b]) == cudaSuccess) {
+      ctx->t_ms[r.cls] += t;
+      ctx->t_cnt[r.cls] += 1;
+      ctx->t_units[r.cls] += r.units;
+    }
+  }
+  cudaGetLastError();
+  ctx->recs.clear();
+  ctx->ev_used = 0;
+  for (int c = 0; c < FD2D_TIMER_COUNT; ++c) {
+    if (ms) ms[c] = ctx->t_ms[c];
+    if (launches) launches[c] = ctx->t_cnt[c];
+    if (units) units[c] = ctx->t_units[c];
+    ctx->t_ms[c] = 0;
+    ctx->t_cnt[c] = 0;
+    ctx->t_units[c] = 0;
   }
   return FD2D_OK;
 }

@@ -328,12 +328,14 @@ struct Run {
 };
 
 fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, const Step32& s) {
+  const int t0 = timer_begin(ctx, ctx->stream);
   switch (r.R) {
     case 1: k32_step<1><<<r.sgrid, NT, 0, ctx->stream>>>(r.G, r.F, s); break;
     case 2: k32_step<2><<<r.sgrid, NT, 0, ctx->stream>>>(r.G, r.F, s); break;
     case 3: k32_step<3><<<r.sgrid, NT, 0, ctx->stream>>>(r.G, r.F, s); break;
     default: k32_step<4><<<r.sgrid, NT, 0, ctx->stream>>>(r.G, r.F, s); break;
   }
+  timer_end(ctx, ctx->stream, t0, s.has_u ? FD2D_TIMER_STEP_VU : FD2D_TIMER_STEP_V, r.np);
   return after_launch(ctx, "k32_step");
 }
 

@@ -1,0 +1,103 @@
+"""Named synthetic workloads (seeded) with the shapes of the benchmark configurations.
+
+* ``plain_cpu_300``      -- 300x300, dt 0.1, nt 1200, order 4, 200 frequencies in
+                            0.01-0.2 Hz, Gaussian spectrum (0.1 Hz, 0.03 Hz),
+                            Gaussian-patch distribution, +-5 % smoothed mu,
+                            10 receivers, one reference station, taper 20 points.
+* ``single_600_o8``      -- 600x600, dt 0.05, nt 3000, order 8, 300 frequencies,
+                            2 reference stations, 40 receivers, random media
+                            (10 % std, 20 km correlation length), ring source.
+* ``structure_512``      -- 512x512, nt 2500, snapshots every 5 steps, 200
+                            frequencies, 1 reference station, 20 receivers.
+
+The domain is 4e5 m square in every workload (the reference's "small setup").
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import Callable, Dict
+
+import numpy as np
+
+from .config import Config, matlab_colon
+from .media import interior_points, random_media, smoothed_perturbation
+from .noise_source import make_noise_source
+
+L = 4.0e5
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    cfg: Config
+    mu: np.ndarray
+    rho: np.ndarray
+    ref_stations: np.ndarray   # n_ref-by-2
+    receivers: np.ndarray      # nr-by-2
+    spectrum: np.ndarray       # K-by-n_src
+    source_dist: np.ndarray    # nx-by-nz-by-n_dist
+
+    def gpt_green(self) -> int:
+        return self.cfg.npts * self.cfg.nt
+
+    def gpt_correlation(self) -> int:
+        return self.cfg.npts * self.cfg.ntc
+
+    def gpt_per_station(self) -> int:
+        return self.gpt_green() + self.gpt_correlation()
+
+
+def _freqs(f0, f1, K):
+    return matlab_colon(f0, (f1 - f0) / (K - 1), f1)[:K] if K > 1 else np.array([f0])
+
+
+def plain_cpu_300(nt: int = 1200) -> Workload:
+    nx = 300
+    dx = L / (nx - 1)
+    cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.1, nt=nt, order=4, f_sample=_freqs(0.01, 0.2, 200),
+                 freq_samp=5, fw_nth=1, absorb_width=20 * dx, source_type="gaussian")
+    mu, rho = smoothed_perturbation(cfg, 0.05, seed=1)
+    sd, spec = make_noise_source("gaussian", 0, cfg,
+                                 spectrum_kw=dict(f_peak=[0.1], bandwidth=[0.03], strength=[1.0]),
+                                 x_c=[0.3 * L], z_c=[0.6 * L], width=[0.1 * L], magnitude=[6.0])
+    rec = interior_points(cfg, 10, seed=2, margin_frac=0.25)
+    ref = interior_points(cfg, 1, seed=12, margin_frac=0.3)
+    return Workload("plain_cpu_300", cfg, mu, rho, ref, rec, spec, sd)
+
+
+def single_600_o8(nt: int = 3000, K: int = 300) -> Workload:
+    nx = 600
+    dx = L / (nx - 1)
+    cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.05, nt=nt, order=8, f_sample=_freqs(0.01, 0.2, K),
+                 freq_samp=5, fw_nth=1, absorb_width=20 * dx, source_type="ring")
+    mu, rho = random_media(cfg, std=0.10, corr_len=2.0e4, seed=1)
+    s = L / 2.0e6  # the reference's ring is laid out on a 2e6 m domain
+    sd, spec = make_noise_source("ring", 0, cfg,
+                                 spectrum_kw=dict(f_peak=[0.1], bandwidth=[0.03], strength=[1.0]),
+                                 x_r=1.0e6 * s, z_r=1.0e6 * s, radius=6.8e5 * s, thickness=1e5 * s,
+                                 radial_scale=9e8 * s * s)
+    rec = interior_points(cfg, 40, seed=3, margin_frac=0.2)
+    ref = interior_points(cfg, 2, seed=13, margin_frac=0.3)
+    return Workload("single_600_o8", cfg, mu, rho, ref, rec, spec, sd)
+
+
+def structure_512(nt: int = 2500) -> Workload:
+    nx = 512
+    dx = L / (nx - 1)
+    cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.5 * dx / 4000.0 * 0.9, nt=nt, order=4,
+                 f_sample=_freqs(0.01, 0.2, 200), freq_samp=5, fw_nth=5, absorb_width=20 * dx)
+    mu, rho = random_media(cfg, std=0.05, corr_len=2.0e4, seed=5)
+    sd, spec = make_noise_source("gaussian", 0, cfg,
+                                 spectrum_kw=dict(f_peak=[0.1], bandwidth=[0.03], strength=[1.0]),
+                                 x_c=[0.3 * L], z_c=[0.6 * L], width=[0.1 * L], magnitude=[6.0])
+    ref = np.array([[0.5 * L, 0.5 * L]])
+    ang = np.linspace(0, 2 * np.pi, 20, endpoint=False)
+    rec = np.stack([0.5 * L + 0.25 * L * np.cos(ang), 0.5 * L + 0.25 * L * np.sin(ang)], axis=1)
+    return Workload("structure_512", cfg, mu, rho, ref, rec, spec, sd)
+
+
+WORKLOADS: Dict[str, Callable[..., Workload]] = {
+    "plain_cpu_300": plain_cpu_300,
+    "single_600_o8": single_600_o8,
+    "structure_512": structure_512,
+}

@@ -114,6 +114,19 @@ fd2d_status fd2d_ctx_set_precision(fd2d_ctx* ctx, int32_t precision);
 fd2d_status fd2d_ctx_synchronize(fd2d_ctx* ctx);
 /* Kernels launched by this context since creation (instrumentation). */
 int64_t fd2d_ctx_kernel_launches(const fd2d_ctx* ctx);
+/* Device-time instrumentation.  When enabled, every launch of the classes
+ * below is bracketed by CUDA events on the context's stream; fd2d_ctx_timing()
+ * waits for the stream, returns per class the summed milliseconds, the launch
+ * count and the work units (grid-point updates for stencils, multiply-adds for
+ * contractions), then resets the counters. */
+enum {
+  FD2D_TIMER_STEP_V = 0,   /* stencil step without displacement (Green run)  */
+  FD2D_TIMER_STEP_VU = 1,  /* stencil step with u (correlation / adjoint)    */
+  FD2D_TIMER_CONTRACT = 2, /* DFT / injection contractions                   */
+  FD2D_TIMER_COUNT = 3
+};
+fd2d_status fd2d_ctx_set_timing(fd2d_ctx* ctx, int32_t enable);
+fd2d_status fd2d_ctx_timing(fd2d_ctx* ctx, double* ms, int64_t* launches, int64_t* units);
 /* Message of the last error on this context ("" if none). ctx may be NULL for
    errors raised before a context existed. */
 const char* fd2d_last_error(const fd2d_ctx* ctx);
