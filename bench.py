@@ -169,14 +169,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="single_600_o8")
     ap.add_argument("--cpu-nt", type=int, default=120)
+    ap.add_argument("--nt", type=int, default=0, help="override the workload's nt (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-timing", action="store_true",
+                    help="do not bracket kernels with CUDA events (no roofline)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
 
     from fd2d_noise_gb300.workloads import WORKLOADS
-    w = WORKLOADS[args.workload]()
+    w = WORKLOADS[args.workload](**({"nt": args.nt} if args.nt else {}))
     if args.impl == "reference":
         run_reference(args, w, world, rank)
         return
@@ -213,6 +216,8 @@ def main():
             s.forward2_correlation(mu, rho, G_re, G_im, spec, 1, sd, 1, rec, nr, outs[i])
 
     gpt_step = n_ref * w.gpt_per_station()
+    torch.cuda.synchronize()
+    stream = sess.stream
     for _ in range(max(args.warmup, 0)):
         step(sess, seis_c)
     torch.cuda.synchronize()
@@ -225,16 +230,16 @@ def main():
     clocks = Clocks(dev)
     launches0 = sess.ctx.kernel_launches
     sess.ctx.timing()  # reset
-    sess.ctx.set_timing(True)
+    sess.ctx.set_timing(not args.no_timing)
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
     clocks.start()
-    ev0.record()
+    ev0.record(stream)
     for _ in range(args.steps):
         step(sess, seis_c)
-    ev1.record()
+    ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
@@ -285,10 +290,10 @@ def main():
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
+        e0.record(s64.stream)
         s64.forward1_green(mu, rho, refs[0], 1, rec, nr, G_re, G_im, seis_g)
         s64.forward2_correlation(mu, rho, G_re, G_im, spec, 1, sd, 1, rec, nr, out64[0])
-        e1.record()
+        e1.record(s64.stream)
         torch.cuda.synchronize()
         ms64 = e0.elapsed_time(e1)
         v64 = w.gpt_per_station() / (ms64 / 1e3) / 1e9

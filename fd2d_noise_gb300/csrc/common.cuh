@@ -95,6 +95,18 @@ struct fd2d_ctx {
   double t_ms[FD2D_TIMER_COUNT] = {0, 0, 0};
   int64_t t_cnt[FD2D_TIMER_COUNT] = {0, 0, 0};
   int64_t t_units[FD2D_TIMER_COUNT] = {0, 0, 0};
+  // CUDA-graph capture of time loops (fd2d::run_captured)
+  bool capturing = false;
+  std::vector<cudaEvent_t> cap_ev;    // timing events recorded inside the capture
+  std::vector<TimerRec> cap_recs;
+  struct GraphEntry {
+    uint64_t key = 0;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaEvent_t> ev;
+    std::vector<TimerRec> recs;
+    int64_t launches = 0;  // kernels inside the graph
+  };
+  std::vector<std::pair<std::string, GraphEntry>> graphs;
 };
 
 namespace fd2d {
@@ -114,6 +126,37 @@ void timer_end(fd2d_ctx* ctx, cudaStream_t stream, int begin, int cls, int64_t u
 
 // Checks the last launch and counts it.
 fd2d_status after_launch(fd2d_ctx* ctx, const char* what);
+
+// Signature of everything a captured time loop depends on (FNV-1a).
+struct Sig {
+  uint64_t h = 1469598103934665603ull;
+  void bytes(const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) { h ^= c[i]; h *= 1099511628211ull; }
+  }
+  template <typename T>
+  void add(const T& v) { bytes(&v, sizeof(T)); }
+  template <typename T>
+  void add_vec(const std::vector<T>& v) { add(v.size()); if (!v.empty()) bytes(v.data(), v.size() * sizeof(T)); }
+};
+
+// Runs `body` (a sequence of launches on ctx->stream, no allocation or host
+// synchronisation inside) as a CUDA graph.  The instantiated graph is cached
+// under `name` and replayed while `key` is unchanged; otherwise the body is
+// captured again and the executable graph updated or re-instantiated.
+template <typename F>
+fd2d_status run_captured(fd2d_ctx* ctx, const char* name, uint64_t key, F&& body);
+fd2d_status graph_begin(fd2d_ctx* ctx, const char* name, uint64_t key, bool* replayed);
+fd2d_status graph_end(fd2d_ctx* ctx, const char* name, uint64_t key, fd2d_status body_status);
+
+template <typename F>
+fd2d_status run_captured(fd2d_ctx* ctx, const char* name, uint64_t key, F&& body) {
+  bool replayed = false;
+  FD2D_TRY(graph_begin(ctx, name, key, &replayed));
+  if (replayed) return FD2D_OK;
+  fd2d_status s = body();
+  return graph_end(ctx, name, key, s);
+}
 
 // Copies an input array to the device (host memspace) or passes it through.
 // n == 0 or src == nullptr gives nullptr.

@@ -30,11 +30,18 @@ struct ContractArgs {
   double* acc1 = nullptr;
   int nsplit = 0;
   int64_t ldacc = 0;
+  int overwrite = 0;  // FP64 planes: 1 = store the result, 0 = add it to them
+  // When remap_pitch > 0 the points m are a pitched grid (m = i + remap_pitch*j)
+  // and the FP64 planes are MATLAB-layout nx-by-nz: m -> i + remap_nx*j, and
+  // points outside the grid are dropped.
+  int remap_pitch = 0, remap_nx = 0, remap_nz = 0;
   // FP32 store: out32[n*ldo + m]
   float* out32 = nullptr;
   int64_t ldo = 0;
 };
 
 fd2d_status contract(fd2d_ctx* ctx, cudaStream_t stream, const ContractArgs& a);
+// One-time kernel attributes; call before any stream capture that contracts.
+fd2d_status contract_prepare(fd2d_ctx* ctx);
 
 }  // namespace fd2d

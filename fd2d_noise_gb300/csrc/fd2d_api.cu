@@ -81,8 +81,22 @@ static int next_event(fd2d_ctx* ctx) {
   return (int)ctx->ev_used++;
 }
 
+// Inside a capture, timing events become external event-record nodes of the
+// graph and are owned by its cache entry.
+static int capture_event(fd2d_ctx* ctx, cudaStream_t stream) {
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return -1;
+  if (cudaEventRecordWithFlags(e, stream, cudaEventRecordExternal) != cudaSuccess) {
+    cudaEventDestroy(e);
+    return -1;
+  }
+  ctx->cap_ev.push_back(e);
+  return (int)ctx->cap_ev.size() - 1;
+}
+
 int timer_begin(fd2d_ctx* ctx, cudaStream_t stream) {
   if (!ctx->timing) return -1;
+  if (ctx->capturing) return capture_event(ctx, stream);
   int i = next_event(ctx);
   if (i >= 0) cudaEventRecord(ctx->ev_pool[i], stream);
   return i;
@@ -90,10 +104,116 @@ int timer_begin(fd2d_ctx* ctx, cudaStream_t stream) {
 
 void timer_end(fd2d_ctx* ctx, cudaStream_t stream, int begin, int cls, int64_t units) {
   if (!ctx->timing || begin < 0) return;
+  if (ctx->capturing) {
+    int i = capture_event(ctx, stream);
+    if (i >= 0) ctx->cap_recs.push_back({begin, i, cls, units});
+    return;
+  }
   int i = next_event(ctx);
   if (i < 0) return;
   cudaEventRecord(ctx->ev_pool[i], stream);
   ctx->recs.push_back({begin, i, cls, units});
+}
+
+static fd2d_ctx::GraphEntry* find_graph(fd2d_ctx* ctx, const char* name) {
+  for (auto& kv : ctx->graphs)
+    if (kv.first == name) return &kv.second;
+  return nullptr;
+}
+
+static void destroy_graph(fd2d_ctx::GraphEntry& g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  for (auto e : g.ev) cudaEventDestroy(e);
+  g = fd2d_ctx::GraphEntry();
+}
+
+static fd2d_status launch_graph(fd2d_ctx* ctx, fd2d_ctx::GraphEntry& g) {
+  FD2D_CUDA(ctx, cudaGraphLaunch(g.exec, ctx->stream));
+  ctx->launches += g.launches;
+  if (ctx->timing && !g.recs.empty()) {
+    // the graph's event nodes are reused by the next replay: read them now
+    FD2D_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (const auto& r : g.recs) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, g.ev[r.a], g.ev[r.b]) == cudaSuccess) {
+        ctx->t_ms[r.cls] += t;
+        ctx->t_cnt[r.cls] += 1;
+        ctx->t_units[r.cls] += r.units;
+      }
+    }
+    cudaGetLastError();
+  }
+  return FD2D_OK;
+}
+
+static thread_local int64_t g_launches_at_capture = 0;
+
+fd2d_status graph_begin(fd2d_ctx* ctx, const char* name, uint64_t key, bool* replayed) {
+  *replayed = false;
+  key ^= ctx->timing ? 0x9e3779b97f4a7c15ull : 0;
+  fd2d_ctx::GraphEntry* g = find_graph(ctx, name);
+  if (g && g->exec && g->key == key) {
+    *replayed = true;
+    return launch_graph(ctx, *g);
+  }
+  ctx->cap_ev.clear();
+  ctx->cap_recs.clear();
+  g_launches_at_capture = ctx->launches;
+  FD2D_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  ctx->capturing = true;
+  return FD2D_OK;
+}
+
+fd2d_status graph_end(fd2d_ctx* ctx, const char* name, uint64_t key, fd2d_status body_status) {
+  key ^= ctx->timing ? 0x9e3779b97f4a7c15ull : 0;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+  ctx->capturing = false;
+  const int64_t n_kernels = ctx->launches - g_launches_at_capture;
+  ctx->launches = g_launches_at_capture;
+  auto drop_events = [&]() {
+    for (auto ev : ctx->cap_ev) cudaEventDestroy(ev);
+    ctx->cap_ev.clear();
+    ctx->cap_recs.clear();
+  };
+  if (body_status != FD2D_OK || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    drop_events();
+    cudaGetLastError();
+    if (body_status != FD2D_OK) return body_status;
+    return set_error(ctx, FD2D_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e));
+  }
+  fd2d_ctx::GraphEntry* g = find_graph(ctx, name);
+  if (!g) {
+    ctx->graphs.emplace_back(name, fd2d_ctx::GraphEntry());
+    g = &ctx->graphs.back().second;
+  }
+  bool updated = false;
+  if (g->exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(g->exec, graph, &info) == cudaSuccess) updated = true;
+    cudaGetLastError();
+  }
+  if (!updated) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    g->exec = nullptr;
+    e = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      drop_events();
+      g->exec = nullptr;
+      return set_error(ctx, FD2D_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    }
+  }
+  cudaGraphDestroy(graph);
+  for (auto ev : g->ev) cudaEventDestroy(ev);
+  g->ev = ctx->cap_ev;
+  g->recs = ctx->cap_recs;
+  ctx->cap_ev.clear();
+  ctx->cap_recs.clear();
+  g->key = key;
+  g->launches = n_kernels;
+  return launch_graph(ctx, *g);
 }
 
 fd2d_status stage_in(fd2d_ctx* ctx, const char* name, const void* src, size_t bytes, const void** dev) {
@@ -220,6 +340,8 @@ fd2d_status fd2d_ctx_destroy(fd2d_ctx* ctx) {
   if (!ctx) return FD2D_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  for (auto& kv : ctx->graphs) destroy_graph(kv.second);
+  ctx->graphs.clear();
   free_workspace(ctx);
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->d_err) cudaFree(ctx->d_err);

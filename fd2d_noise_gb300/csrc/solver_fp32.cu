@@ -1,15 +1,21 @@
 // solver_fp32.cu -- the FP32 form of the three solvers.
 //
-// Per time step ONE fused kernel (k32_step) advances a tile of the grid:
+// Per time step ONE fused kernel (k32_step) advances a 64x16 tile of the grid:
 //   DS  = div_s(sxy, szy) (+ point sources) (+ injected correlation source)
 //   v   = (v + DS * dt/rho) * absbound
 //   sxy += dt*mu * dx_v(v),  szy += dt*mu * dz_v(v),  u += v*dt
 // (code/run_forward1_green.m:148-172, code/run_forward2_correlation.m:190-242,
-// code/run_noise_adjoint.m:245-297).  The tile stages sxy/szy with their halos
-// in shared memory, recomputes the new v on the halo ring so the stress update
-// needs no second pass, and writes v, sxy, szy, u once: 36 B (44 B with u) of
-// HBM traffic per grid-point update.  Fields are ping-ponged between two
-// buffers so neighbouring tiles never read a half-updated halo.
+// code/run_noise_adjoint.m:245-297).  One elected thread stages the tile's
+// halo boxes (sxy, szy, v, dt/rho, taper, injection plane, dt*mu, u) into
+// shared memory with TMA tensor loads -- the hardware zero-fills everything
+// outside the grid -- while the other threads read their point sources.  The
+// CTA then recomputes the new v on the halo ring, so the stress update needs no
+// second pass, and writes v, sxy, szy, u once: 36 B (44 B with u) of HBM
+// traffic per grid-point update.  Fields are ping-ponged between two buffers
+// so neighbouring tiles never read a half-updated halo.
+//
+// Internal FP32 arrays are pitched (row pitch P = nx rounded up to 32 floats,
+// a multiple of 16 bytes as TMA requires); user arrays keep MATLAB layout.
 //
 // The dense work leaves the time loop:
 //  * the DFT of v (Green spectrum) / u (adjoint spectrum, source kernel) is a
@@ -20,226 +26,286 @@
 //    evaluated for all injection steps before the loop and read by the stencil
 //    as one plane per injection step.
 // The mu kernel accumulates in FP64 from FP32 strains; the source kernel is
-// formed once from the adjoint spectrum (see fp32_adjoint).
+// formed once from the adjoint spectrum (see fp32_adjoint).  Time loops run as
+// cached CUDA graphs (run_captured).
 #include "common.cuh"
 #include "contract.cuh"
+#include "tma.cuh"
 
 #include <algorithm>
 
 namespace fd2d {
 namespace {
 
-constexpr int TX = 64, TZ = 16, NT = 256;
+constexpr int TX = 64, TZ = 16, NT = 512;
 constexpr int MAX_BOX_SRC = 64;
 
 struct Grid32 {
-  int nx, nz;
+  int nx, nz, P;  // P: row pitch of internal arrays (floats)
   float c[4];
   float inv_dx, inv_dz, dt;
+  int* err;       // device error flag (bounded waits)
 };
 
-struct Fields32 {
-  const float *b, *taper, *dtmu;
-  float *v[2], *sxy[2], *szy[2], *u[2];
+// Shared-memory layout of one tile (floats, regions 128-byte aligned).
+template <int R>
+struct Tile {
+  static constexpr int BWc = TX + 2 * R - 1;  // computed v box width (x from x0-R+1)
+  static constexpr int BH = TZ + 2 * R - 1;   // box rows (z from z0-R+1)
+  static constexpr int SZH = TZ + 4 * R - 2;  // szy rows (z from z0-2R+1)
+  static constexpr int BWa = TX + 8;          // loaded box width (x from x0-4)
+  static constexpr int SXWa = TX + 16;        // sxy region width (x from x0-8)
+  static constexpr int al(int n) { return (n + 31) / 32 * 32; }
+  static constexpr int O_SXY = 0;
+  static constexpr int O_SZY = O_SXY + al(BH * SXWa);
+  static constexpr int O_V = O_SZY + al(SZH * BWa);
+  static constexpr int O_B = O_V + al(BH * BWa);
+  static constexpr int O_T = O_B + al(BH * BWa);
+  static constexpr int O_I = O_T + al(BH * BWa);
+  static constexpr int O_MU = O_I + al(BH * BWa);
+  static constexpr int O_U = O_MU + al(TZ * TX);
+  static constexpr int O_VN = O_U + al(TZ * TX);
+  static constexpr int TOTAL = O_VN + al(BH * BWc);
+  static constexpr int BYTES = TOTAL * 4 + 128;  // + alignment slack
+};
+
+struct alignas(64) StepMaps {
+  CUtensorMap sxy, szy, v, u, b, taper, dtmu, inj;
 };
 
 struct Step32 {
-  int par;  // read buffers [par], write [1 - par]
+  float *vo, *sxyo, *szyo, *uo;  // fields written this step (buffer 1 - par)
   int has_u;
-  const int* src_pt;
+  int inj_plane;                 // plane of the injection map, or -1
+  const int2* src_xy;
   int nsrc;
-  const double* amp;  // per-source amplitude of this step, or nullptr -> amp_const
+  const double* amp;             // per-source amplitude of this step, or nullptr -> amp_const
   float amp_const;
-  const float* inj;     // injection plane of this step (npts) or nullptr
-  float* snap_pre;      // single(old field), npts, or nullptr
+  float* snap_pre;               // single(old field) in MATLAB layout, or nullptr
   int snap_pre_u;
-  float* snap_dft;      // new field (v or u) into the DFT snapshot plane, or nullptr
-  const int* rec_pt;
+  float* snap_dft;               // new field (v or u) into the DFT snapshot plane (pitched)
+  const int2* rec_xy;
   int nrec;
-  double* seis_col;     // seismograms(:, n)
+  double* seis_col;              // seismograms(:, n)
   int rec_u;
 };
 
 template <int R>
-__global__ __launch_bounds__(NT) void k32_step(Grid32 G, Fields32 F, Step32 S) {
-  constexpr int BW = TX + 2 * R - 1, BH = TZ + 2 * R - 1;
-  constexpr int SXW = TX + 4 * R - 2, SZH = TZ + 4 * R - 2;
-  __shared__ float s_sxy[BH * SXW];
-  __shared__ float s_szy[SZH * BW];
-  __shared__ float s_v[BH * BW];
+__global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__ StepMaps M, Step32 S) {
+  using T = Tile<R>;
+  extern __shared__ __align__(128) unsigned char sm_raw[];
+  // TMA destinations: 128-byte aligned regardless of the static smem in front
+  float* sm = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm_raw) + 127) & ~uintptr_t(127));
+  __shared__ __align__(8) uint64_t bar;
   __shared__ int s_src[MAX_BOX_SRC];
   __shared__ float s_amp[MAX_BOX_SRC];
   __shared__ int s_nsrc;
 
   const int tid = threadIdx.x;
-  const int nx = G.nx, nz = G.nz;
+  const int nx = G.nx, nz = G.nz, P = G.P;
   const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
   const int bx0 = x0 - R + 1, bz0 = z0 - R + 1;
-  const int sx0 = x0 - 2 * R + 1, sz0 = z0 - 2 * R + 1;
-  const int par = S.par;
-  const float* __restrict__ sxy = F.sxy[par];
-  const float* __restrict__ szy = F.szy[par];
-  const float* __restrict__ v = F.v[par];
-  const float* __restrict__ u = F.u[par];
 
-  if (tid == 0) s_nsrc = 0;
-  for (int e = tid; e < BH * SXW; e += NT) {
-    const int rr = e / SXW, cc = e - rr * SXW;
-    const int gx = sx0 + cc, gz = bz0 + rr;
-    s_sxy[e] = (gx >= 0 && gx < nx && gz >= 0 && gz < nz) ? sxy[gx + (int64_t)nx * gz] : 0.f;
+  if (tid == 0) {
+    s_nsrc = 0;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    uint32_t bytes = 4u * (T::BH * T::SXWa + T::SZH * T::BWa + 3 * T::BH * T::BWa + TZ * TX);
+    if (S.has_u) bytes += 4u * TZ * TX;
+    if (S.inj_plane >= 0) bytes += 4u * T::BH * T::BWa;
+    mbar_expect_tx(&bar, bytes);
+    tma_load_2d(sm + T::O_SXY, &M.sxy, x0 - 8, bz0, &bar);
+    tma_load_2d(sm + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, &bar);
+    tma_load_2d(sm + T::O_V, &M.v, x0 - 4, bz0, &bar);
+    tma_load_2d(sm + T::O_B, &M.b, x0 - 4, bz0, &bar);
+    tma_load_2d(sm + T::O_T, &M.taper, x0 - 4, bz0, &bar);
+    tma_load_2d(sm + T::O_MU, &M.dtmu, x0, z0, &bar);
+    if (S.has_u) tma_load_2d(sm + T::O_U, &M.u, x0, z0, &bar);
+    if (S.inj_plane >= 0) tma_load_3d(sm + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane, &bar);
   }
-  for (int e = tid; e < SZH * BW; e += NT) {
-    const int rr = e / BW, cc = e - rr * BW;
-    const int gx = bx0 + cc, gz = sz0 + rr;
-    s_szy[e] = (gx >= 0 && gx < nx && gz >= 0 && gz < nz) ? szy[gx + (int64_t)nx * gz] : 0.f;
+  // point sources of the box (global loads overlap the TMA traffic)
+  int2 my_src = make_int2(-1 << 30, -1 << 30);
+  float my_amp = 0.f;
+  if (tid < S.nsrc) {
+    my_src = S.src_xy[tid];
+    my_amp = S.amp ? (float)S.amp[tid] : S.amp_const;
   }
-  __syncthreads();
-  for (int k = tid; k < S.nsrc; k += NT) {
-    const int p = S.src_pt[k];
-    const int gx = p % nx, gz = p / nx;
-    if (gx >= bx0 && gx < bx0 + BW && gz >= bz0 && gz < bz0 + BH) {
+  __syncthreads();  // barrier initialised, s_nsrc cleared
+  {
+    const int gx = my_src.x, gz = my_src.y;
+    if (gx >= bx0 && gx < bx0 + T::BWc && gz >= bz0 && gz < bz0 + T::BH) {
       const int slot = atomicAdd(&s_nsrc, 1);
       if (slot < MAX_BOX_SRC) {
-        s_src[slot] = (gz - bz0) * BW + (gx - bx0);
+        s_src[slot] = (gz - bz0) * T::BWc + (gx - bx0);
+        s_amp[slot] = my_amp;
+      }
+    }
+  }
+  for (int k = tid + NT; k < S.nsrc; k += NT) {  // more sources than threads: rare
+    const int2 q = S.src_xy[k];
+    if (q.x >= bx0 && q.x < bx0 + T::BWc && q.y >= bz0 && q.y < bz0 + T::BH) {
+      const int slot = atomicAdd(&s_nsrc, 1);
+      if (slot < MAX_BOX_SRC) {
+        s_src[slot] = (q.y - bz0) * T::BWc + (q.x - bx0);
         s_amp[slot] = S.amp ? (float)S.amp[k] : S.amp_const;
       }
     }
   }
-  __syncthreads();
+  const bool ok = mbar_wait_bounded(&bar, 0);
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) set_error_flag(G.err, 1);
+    return;
+  }
   const int nbs = s_nsrc;
+  const float* s_sxy = sm + T::O_SXY;
+  const float* s_szy = sm + T::O_SZY;
+  const float* s_v = sm + T::O_V;
+  const float* s_b = sm + T::O_B;
+  const float* s_t = sm + T::O_T;
+  const float* s_i = sm + T::O_I;
+  const float* s_mu = sm + T::O_MU;
+  const float* s_u = sm + T::O_U;
+  float* s_vn = sm + T::O_VN;
+  const bool inj = S.inj_plane >= 0;
 
-  // new v on the tile plus its halo ring
-  for (int e = tid; e < BH * BW; e += NT) {
-    const int rr = e / BW, cc = e - rr * BW;
+  // ---- new v on the tile plus its halo ring -----------------------------------------
+  // Threads own a column (tx) and march over rows; the 2R-1 right-fringe
+  // columns of the box are a second, short pass.
+  constexpr int NR = NT / TX, FW = T::BWc - TX;
+  const int tx0 = tid % TX, ty0 = tid / TX;
+  auto vnew = [&](int rr, int cc) {
+    const int e = rr * T::BWc + cc;
     const int gx = bx0 + cc, gz = bz0 + rr;
-    float vn = 0.f;
-    if (gx >= 0 && gx < nx && gz >= 0 && gz < nz) {
-      const int64_t p = gx + (int64_t)nx * gz;
-      float ds = 0.f;
-      if (gx >= R && gx <= nx - R - 1) {
-        const float* row = s_sxy + rr * SXW + cc + R;
-        float acc = 0.f;
+    float ds = 0.f;
+    if (gx >= R && gx <= nx - R - 1) {
+      const float* row = s_sxy + rr * T::SXWa + cc + 8 - R;  // row[m] = sxy(gx+m-1), row[1-m] = sxy(gx-m)
+      float acc = 0.f;
 #pragma unroll
-        for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (row[m - 1] - row[-m]);
-        ds = acc * G.inv_dx;
-      }
-      if (gz >= R && gz <= nz - R - 1) {
-        const float* col = s_szy + (rr + R) * BW + cc;
-        float acc = 0.f;
+      for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (row[m] - row[1 - m]);
+      ds = acc * G.inv_dx;
+    }
+    if (gz >= R && gz <= nz - R - 1) {
+      const float* col = s_szy + (rr + R) * T::BWa + cc + 5 - R;  // col[(m-1)W] = szy(gz+m-1)
+      float acc = 0.f;
 #pragma unroll
-        for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (col[(m - 1) * BW] - col[-m * BW]);
-        ds += acc * G.inv_dz;
-      }
-      if (nbs) {
-        if (nbs <= MAX_BOX_SRC) {
-          for (int k = 0; k < nbs; ++k)
-            if (s_src[k] == e) ds += s_amp[k];
-        } else {
-          for (int k = 0; k < S.nsrc; ++k)
-            if (S.src_pt[k] == p) ds += S.amp ? (float)S.amp[k] : S.amp_const;
+      for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (col[(m - 1) * T::BWa] - col[-m * T::BWa]);
+      ds += acc * G.inv_dz;
+    }
+    if (nbs) {
+      if (nbs <= MAX_BOX_SRC) {
+        for (int q = 0; q < nbs; ++q)
+          if (s_src[q] == e) ds += s_amp[q];
+      } else {
+        for (int q = 0; q < S.nsrc; ++q) {
+          const int2 w = S.src_xy[q];
+          if (w.x == gx && w.y == gz) ds += S.amp ? (float)S.amp[q] : S.amp_const;
         }
       }
-      if (S.inj) ds += S.inj[p];
-      vn = (v[p] + ds * F.b[p]) * F.taper[p];
     }
-    s_v[e] = vn;
+    const int bo = rr * T::BWa + cc + 5 - R;
+    if (inj) ds += s_i[bo];
+    s_vn[e] = (s_v[bo] + ds * s_b[bo]) * s_t[bo];
+  };
+  for (int rr = ty0; rr < T::BH; rr += NR) vnew(rr, tx0);
+  for (int f = tid; f < FW * T::BH; f += NT) {
+    const int rr = f / FW;
+    vnew(rr, TX + f - rr * FW);
   }
   __syncthreads();
 
-  float* __restrict__ vo = F.v[1 - par];
-  float* __restrict__ sxyo = F.sxy[1 - par];
-  float* __restrict__ szyo = F.szy[1 - par];
-  float* __restrict__ uo = F.u[1 - par];
+  // ---- stress, displacement and outputs on the tile -----------------------------------
+  const int tx = tx0;
 #pragma unroll
-  for (int k = 0; k < (TX * TZ) / NT; ++k) {
-    const int e = tid + k * NT;
-    const int tz = e / TX, tx = e - tz * TX;
+  for (int tz = ty0; tz < TZ; tz += NR) {
+    const int e = tz * TX + tx;
     const int i = x0 + tx, j = z0 + tz;
     if (i >= nx || j >= nz) continue;
-    const int64_t p = i + (int64_t)nx * j;
-    const int cc = tx + R - 1, rr = tz + R - 1;
-    const float vn = s_v[rr * BW + cc];
-    if (S.snap_pre) S.snap_pre[p] = S.snap_pre_u ? u[p] : v[p];
-    vo[p] = vn;
-    const float dtmu = F.dtmu[p];
+    const int p = i + P * j;
+    const int rr = tz + R - 1, cc = tx + R - 1;
+    const float* vrow = s_vn + rr * T::BWc + cc;
+    const float vn = vrow[0];
+    if (S.snap_pre) S.snap_pre[i + nx * j] = S.snap_pre_u ? s_u[e] : s_v[rr * T::BWa + tx + 4];
+    S.vo[p] = vn;
+    const float dtmu = s_mu[e];
     if (i <= nx - 2) {
-      float nw = s_sxy[rr * SXW + cc + R];
+      float nw = s_sxy[rr * T::SXWa + tx + 8];
       if (i >= R - 1 && i <= nx - R - 1) {
-        const float* row = s_v + rr * BW + cc;
         float acc = 0.f;
 #pragma unroll
-        for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (row[m] - row[1 - m]);
+        for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (vrow[m] - vrow[1 - m]);
         nw += dtmu * (acc * G.inv_dx);
       }
-      sxyo[p] = nw;
+      S.sxyo[p] = nw;
     }
     if (j <= nz - 2) {
-      float nw = s_szy[(rr + R) * BW + cc];
+      float nw = s_szy[(tz + 2 * R - 1) * T::BWa + tx + 4];
       if (j >= R - 1 && j <= nz - R - 1) {
-        const float* col = s_v + rr * BW + cc;
         float acc = 0.f;
 #pragma unroll
-        for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (col[m * BW] - col[(1 - m) * BW]);
+        for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (vrow[m * T::BWc] - vrow[(1 - m) * T::BWc]);
         nw += dtmu * (acc * G.inv_dz);
       }
-      szyo[p] = nw;
+      S.szyo[p] = nw;
     }
     float x = vn;
     if (S.has_u) {
-      x = u[p] + vn * G.dt;
-      uo[p] = x;
+      x = s_u[e] + vn * G.dt;
+      S.uo[p] = x;
     }
     if (S.snap_dft) S.snap_dft[p] = x;
   }
   if (S.nrec) {
     __syncthreads();
     for (int k = tid; k < S.nrec; k += NT) {
-      const int p = S.rec_pt[k];
-      const int gx = p % nx, gz = p / nx;
-      if (gx >= x0 && gx < x0 + TX && gz >= z0 && gz < z0 + TZ)
-        S.seis_col[k] = (double)(S.rec_u ? uo[p] : vo[p]);
+      const int2 q = S.rec_xy[k];
+      if (q.x >= x0 && q.x < x0 + TX && q.y >= z0 && q.y < z0 + TZ) {
+        const int p = q.x + P * q.y;
+        S.seis_col[k] = (double)(S.rec_u ? S.uo[p] : S.vo[p]);
+      }
     }
   }
 }
 
 // ---- point kernels ---------------------------------------------------------------
+// FP32 staggered derivatives of a field with row pitch `ld` (f, or f - g).
 template <int R>
-__device__ __forceinline__ float dx32(const Grid32& G, const float* f, const float* g, int i, int j) {
+__device__ __forceinline__ float dx32(const Grid32& G, const float* f, const float* g, int ld, int i, int j) {
   if (i < R - 1 || i > G.nx - R - 1) return 0.f;
-  const float* F = f + (int64_t)G.nx * j;
-  const float* H = g ? g + (int64_t)G.nx * j : nullptr;
+  const float* F = f + (int64_t)ld * j;
+  const float* H = g ? g + (int64_t)ld * j : nullptr;
   float acc = 0.f;
 #pragma unroll
   for (int m = 1; m <= R; ++m) {
-    float a = H ? F[i + m] - H[i + m] : F[i + m];
-    float b = H ? F[i - m + 1] - H[i - m + 1] : F[i - m + 1];
+    const float a = H ? F[i + m] - H[i + m] : F[i + m];
+    const float b = H ? F[i - m + 1] - H[i - m + 1] : F[i - m + 1];
     acc += G.c[m - 1] * (a - b);
   }
   return acc * G.inv_dx;
 }
 
 template <int R>
-__device__ __forceinline__ float dz32(const Grid32& G, const float* f, const float* g, int i, int j) {
+__device__ __forceinline__ float dz32(const Grid32& G, const float* f, const float* g, int ld, int i, int j) {
   if (j < R - 1 || j > G.nz - R - 1) return 0.f;
   float acc = 0.f;
 #pragma unroll
   for (int m = 1; m <= R; ++m) {
-    const int64_t qa = i + (int64_t)G.nx * (j + m), qb = i + (int64_t)G.nx * (j - m + 1);
-    float a = g ? f[qa] - g[qa] : f[qa];
-    float b = g ? f[qb] - g[qb] : f[qb];
+    const int64_t qa = i + (int64_t)ld * (j + m), qb = i + (int64_t)ld * (j - m + 1);
+    const float a = g ? f[qa] - g[qa] : f[qa];
+    const float b = g ? f[qb] - g[qb] : f[qb];
     acc += G.c[m - 1] * (a - b);
   }
   return acc * G.inv_dz;
 }
 
-// forward1 Born source before div_s: sxy += dt*dmu*dx_v(G_in(:,:,i))  (in place on the read buffers)
+// forward1 Born source before div_s: sxy += dt*dmu*dx_v(G_in(:,:,i)), on the read buffers
 template <int R>
 __global__ void k32_born_pre(Grid32 G, float* sxy, float* szy, const float* dtdmu, const float* Gs) {
   const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
   if (i >= G.nx || j >= G.nz) return;
-  const int64_t p = i + (int64_t)G.nx * j;
-  if (i <= G.nx - 2) sxy[p] += dtdmu[p] * dx32<R>(G, Gs, nullptr, i, j);
-  if (j <= G.nz - 2) szy[p] += dtdmu[p] * dz32<R>(G, Gs, nullptr, i, j);
+  const int64_t p = i + (int64_t)G.P * j;
+  const float dm = dtdmu[p];
+  if (i <= G.nx - 2) sxy[p] += dm * dx32<R>(G, Gs, nullptr, G.nx, i, j);
+  if (j <= G.nz - 2) szy[p] += dm * dz32<R>(G, Gs, nullptr, G.nx, i, j);
 }
 
 // correlation / adjoint Born term after the stress update: -= dmu*dx_v(C(n) - C(n+1))
@@ -247,9 +313,9 @@ template <int R>
 __global__ void k32_born_post(Grid32 G, float* sxy, float* szy, const float* dmu, const float* Ca, const float* Cb) {
   const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
   if (i >= G.nx || j >= G.nz) return;
-  const int64_t p = i + (int64_t)G.nx * j;
-  if (i <= G.nx - 2) sxy[p] -= dmu[p] * dx32<R>(G, Ca, Cb, i, j);
-  if (j <= G.nz - 2) szy[p] -= dmu[p] * dz32<R>(G, Ca, Cb, i, j);
+  const int64_t p = i + (int64_t)G.P * j;
+  if (i <= G.nx - 2) sxy[p] -= dmu[p] * dx32<R>(G, Ca, Cb, G.nx, i, j);
+  if (j <= G.nz - 2) szy[p] -= dmu[p] * dz32<R>(G, Ca, Cb, G.nx, i, j);
 }
 
 // K_mu -= dx_v(u).*dx_v(u_fwd)*fw ; K_mu -= dz_v(u).*dz_v(u_fwd)*fw   (FP32 strains, FP64 sum)
@@ -259,44 +325,55 @@ __global__ void k32_kmu(Grid32 G, const float* u, const float* uf, double* Kmu, 
   if (i >= G.nx || j >= G.nz) return;
   const int64_t p = i + (int64_t)G.nx * j;
   double k = Kmu[p];
-  if (i <= G.nx - 2) k -= (double)(dx32<R>(G, u, nullptr, i, j) * dx32<R>(G, uf, nullptr, i, j) * fw);
-  if (j <= G.nz - 2) k -= (double)(dz32<R>(G, u, nullptr, i, j) * dz32<R>(G, uf, nullptr, i, j) * fw);
+  if (i <= G.nx - 2) k -= (double)(dx32<R>(G, u, nullptr, G.P, i, j) * dx32<R>(G, uf, nullptr, G.nx, i, j) * fw);
+  if (j <= G.nz - 2) k -= (double)(dz32<R>(G, u, nullptr, G.P, i, j) * dz32<R>(G, uf, nullptr, G.nx, i, j) * fw);
   Kmu[p] = k;
 }
 
-__global__ void k32_prep(const double* mu, const double* rho, const double* ab, double dt,
-                         float* b, float* taper, float* dtmu, int64_t n) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  b[p] = (float)(dt / rho[p]);
-  taper[p] = (float)ab[p];
-  dtmu[p] = (float)(dt * mu[p]);
+// dt/rho, taper, dt*mu into pitched FP32 arrays (zero in the pitch padding).
+__global__ void k32_prep(const double* mu, const double* rho, const double* ab, double dt, int nx, int nz, int P,
+                         float* b, float* taper, float* dtmu) {
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+  if (i >= P || j >= nz) return;
+  const int64_t q = i + (int64_t)P * j;
+  if (i >= nx) {
+    b[q] = taper[q] = dtmu[q] = 0.f;
+    return;
+  }
+  const int64_t p = i + (int64_t)nx * j;
+  b[q] = (float)(dt / rho[p]);
+  taper[q] = (float)ab[p];
+  dtmu[q] = (float)(dt * mu[p]);
 }
 
-__global__ void k32_scale_f(const double* a, double s, float* out, int64_t n) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p < n) out[p] = (float)(s * a[p]);
-}
-
-__global__ void k32_f_from_d(const double* a, float* out, int64_t n) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p < n) out[p] = (float)a[p];
+// FP32 copy of an FP64 MATLAB-layout array into a pitched array, scaled.
+__global__ void k32_pitched(const double* a, double s, int nx, int nz, int P, float* out) {
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+  if (i >= P || j >= nz) return;
+  out[i + (int64_t)P * j] = i < nx ? (float)(s * a[i + (int64_t)nx * j]) : 0.f;
 }
 
 // P planes of the field source: P_k = spec(k) * (sum_b M(k,b) sd_b) * (Xre_k + i*sign*Xim_k)
-// written as 2K float planes [Re P_0..Re P_{K-1}, Im P_0..Im P_{K-1}].
+// as 2K pitched float planes [Re P_0..Re P_{K-1}, Im P_0..Im P_{K-1}], plane stride ps.
 __global__ void k32_make_P(int K, int ncol, const double* M, const double* sd, const double* spec,
-                           const double* Xre, const double* Xim, double sign, float* P, int64_t np) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= np) return;
-  double sdv[16];
-  for (int b = 0; b < ncol && b < 16; ++b) sdv[b] = sd[p + np * b];
+                           const double* Xre, const double* Xim, double sign, int nx, int nz, int P,
+                           int64_t ps, float* Pl) {
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+  if (i >= P || j >= nz) return;
+  const int64_t q = i + (int64_t)P * j;
+  if (i >= nx) {
+    for (int k = 0; k < 2 * K; ++k) Pl[q + ps * k] = 0.f;
+    return;
+  }
+  const int64_t np = (int64_t)nx * nz, p = i + (int64_t)nx * j;
+  double sdv[8];
+  for (int b = 0; b < ncol && b < 8; ++b) sdv[b] = sd[p + np * b];
   for (int k = 0; k < K; ++k) {
     double dist = 0.0;
-    for (int b = 0; b < ncol; ++b) dist += M[k + (int64_t)K * b] * (b < 16 ? sdv[b] : sd[p + np * b]);
-    const double R = spec[k] * dist;
-    P[p + np * k] = (float)(R * Xre[p + np * k]);
-    P[p + np * (K + k)] = (float)(R * sign * (Xim ? Xim[p + np * k] : 0.0));
+    for (int b = 0; b < ncol; ++b) dist += M[k + (int64_t)K * b] * (b < 8 ? sdv[b] : sd[p + np * b]);
+    const double Rk = spec[k] * dist;
+    Pl[q + ps * k] = (float)(Rk * Xre[p + np * k]);
+    Pl[q + ps * (K + k)] = (float)(Rk * sign * (Xim ? Xim[p + np * k] : 0.0));
   }
 }
 
@@ -319,21 +396,45 @@ __global__ void k32_source_kernel(int K, int ncol, const double* M, const double
 // ---- host side ---------------------------------------------------------------------
 struct Run {
   Grid32 G{};
-  Fields32 F{};
+  float *b = nullptr, *taper = nullptr, *dtmu = nullptr;
+  float *v[2] = {}, *sxy[2] = {}, *szy[2] = {}, *u[2] = {};
+  StepMaps maps[2];  // read buffers 0 / 1
   dim3 sgrid, pgrid, pblock{32, 8};
   int R = 2;
-  int* rec_pt = nullptr;
-  int* src_pt = nullptr;
-  int64_t np = 0;
+  int2* rec_xy = nullptr;
+  int2* src_xy = nullptr;
+  int64_t np = 0;   // nx*nz
+  int64_t ps = 0;   // pitched plane size P*nz rounded up to 128
 };
 
-fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, const Step32& s) {
+template <int R>
+void launch_step_r(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
+  k32_step<R><<<r.sgrid, NT, Tile<R>::BYTES, ctx->stream>>>(r.G, r.maps[par], s);
+}
+
+// Opt the step kernels in to their dynamic shared memory (once, before any capture).
+fd2d_status step_attributes(fd2d_ctx* ctx) {
+  static bool done = false;
+  if (done) return FD2D_OK;
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<1>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<2>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<3>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<4>::BYTES));
+  done = true;
+  return FD2D_OK;
+}
+
+fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, int par, Step32 s) {
+  s.vo = r.v[1 - par];
+  s.sxyo = r.sxy[1 - par];
+  s.szyo = r.szy[1 - par];
+  s.uo = r.u[1 - par];
   const int t0 = timer_begin(ctx, ctx->stream);
   switch (r.R) {
-    case 1: k32_step<1><<<r.sgrid, NT, 0, ctx->stream>>>(r.G, r.F, s); break;
-    case 2: k32_step<2><<<r.sgrid, NT, 0, ctx->stream>>>(r.G, r.F, s); break;
-    case 3: k32_step<3><<<r.sgrid, NT, 0, ctx->stream>>>(r.G, r.F, s); break;
-    default: k32_step<4><<<r.sgrid, NT, 0, ctx->stream>>>(r.G, r.F, s); break;
+    case 1: launch_step_r<1>(ctx, r, par, s); break;
+    case 2: launch_step_r<2>(ctx, r, par, s); break;
+    case 3: launch_step_r<3>(ctx, r, par, s); break;
+    default: launch_step_r<4>(ctx, r, par, s); break;
   }
   timer_end(ctx, ctx->stream, t0, s.has_u ? FD2D_TIMER_STEP_VU : FD2D_TIMER_STEP_V, r.np);
   return after_launch(ctx, "k32_step");
@@ -347,51 +448,81 @@ fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, const Step32& s) {
     default: KERNEL<4><<<r.pgrid, r.pblock, 0, ctx->stream>>>(__VA_ARGS__); break;       \
   }
 
+fd2d_status make_maps(fd2d_ctx* ctx, Run& r) {
+  const int nx = r.G.nx, nz = r.G.nz, P = r.G.P, R = r.R;
+  const int BH = TZ + 2 * R - 1, SZH = TZ + 4 * R - 2, BWa = TX + 8, SXWa = TX + 16;
+  for (int q = 0; q < 2; ++q) {
+    StepMaps& m = r.maps[q];
+    FD2D_TRY(make_tmap_f32(ctx, &m.sxy, r.sxy[q], nx, nz, P, SXWa, BH));
+    FD2D_TRY(make_tmap_f32(ctx, &m.szy, r.szy[q], nx, nz, P, BWa, SZH));
+    FD2D_TRY(make_tmap_f32(ctx, &m.v, r.v[q], nx, nz, P, BWa, BH));
+    FD2D_TRY(make_tmap_f32(ctx, &m.u, r.u[q] ? r.u[q] : r.v[q], nx, nz, P, TX, TZ));
+    FD2D_TRY(make_tmap_f32(ctx, &m.b, r.b, nx, nz, P, BWa, BH));
+    FD2D_TRY(make_tmap_f32(ctx, &m.taper, r.taper, nx, nz, P, BWa, BH));
+    FD2D_TRY(make_tmap_f32(ctx, &m.dtmu, r.dtmu, nx, nz, P, TX, TZ));
+    FD2D_TRY(make_tmap_f32(ctx, &m.inj, r.b, nx, nz, P, BWa, BH));  // replaced when planes exist
+  }
+  return FD2D_OK;
+}
+
+fd2d_status set_inj_map(fd2d_ctx* ctx, Run& r, const float* planes, int n_planes) {
+  const int BH = TZ + 2 * r.R - 1, BWa = TX + 8;
+  for (int q = 0; q < 2; ++q)
+    FD2D_TRY(make_tmap_f32(ctx, &r.maps[q].inj, planes, r.G.nx, r.G.nz, r.G.P, BWa, BH, n_planes, r.ps));
+  return FD2D_OK;
+}
+
 fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, bool with_u, Run& r) {
-  const int64_t np = g.npts();
-  r.np = np;
+  const int nx = g.nx, nz = g.nz;
+  const int P = (nx + 31) / 32 * 32;
+  r.np = g.npts();
+  r.ps = ((int64_t)P * nz + 127) / 128 * 128;
   r.R = g.r;
-  r.G.nx = g.nx;
-  r.G.nz = g.nz;
+  r.G.nx = nx;
+  r.G.nz = nz;
+  r.G.P = P;
   for (int m = 0; m < 4; ++m) r.G.c[m] = (float)g.c[m];
   r.G.inv_dx = (float)(1.0 / g.dx);
   r.G.inv_dz = (float)(1.0 / g.dz);
   r.G.dt = (float)g.dt;
-  float *b, *taper, *dtmu;
-  FD2D_TRY(workspace_t(ctx, "f32.b", np, &b));
-  FD2D_TRY(workspace_t(ctx, "f32.taper", np, &taper));
-  FD2D_TRY(workspace_t(ctx, "f32.dtmu", np, &dtmu));
+  r.G.err = ctx->d_err;
+  r.pblock = dim3(32, 8);
+  const size_t ps = (size_t)r.ps;
+  FD2D_TRY(workspace_t(ctx, "f32.b", ps, &r.b));
+  FD2D_TRY(workspace_t(ctx, "f32.taper", ps, &r.taper));
+  FD2D_TRY(workspace_t(ctx, "f32.dtmu", ps, &r.dtmu));
   double* ab;
   FD2D_TRY(upload(ctx, "f32.absbound64", g.absbound, &ab));
-  k32_prep<<<(unsigned)((np + 255) / 256), 256, 0, ctx->stream>>>(a.mu, a.rho, ab, g.dt, b, taper, dtmu, np);
+  dim3 pg((P + 31) / 32, (nz + 7) / 8);
+  k32_prep<<<pg, r.pblock, 0, ctx->stream>>>(a.mu, a.rho, ab, g.dt, nx, nz, P, r.b, r.taper, r.dtmu);
   FD2D_TRY(after_launch(ctx, "k32_prep"));
-  r.F.b = b;
-  r.F.taper = taper;
-  r.F.dtmu = dtmu;
   static const char* names[2][4] = {{"f32.v0", "f32.sxy0", "f32.szy0", "f32.u0"},
                                     {"f32.v1", "f32.sxy1", "f32.szy1", "f32.u1"}};
   for (int q = 0; q < 2; ++q) {
-    FD2D_TRY(workspace_t(ctx, names[q][0], np, &r.F.v[q]));
-    FD2D_TRY(workspace_t(ctx, names[q][1], np, &r.F.sxy[q]));
-    FD2D_TRY(workspace_t(ctx, names[q][2], np, &r.F.szy[q]));
-    FD2D_CUDA(ctx, cudaMemsetAsync(r.F.v[q], 0, np * 4, ctx->stream));
-    FD2D_CUDA(ctx, cudaMemsetAsync(r.F.sxy[q], 0, np * 4, ctx->stream));
-    FD2D_CUDA(ctx, cudaMemsetAsync(r.F.szy[q], 0, np * 4, ctx->stream));
+    FD2D_TRY(workspace_t(ctx, names[q][0], ps, &r.v[q]));
+    FD2D_TRY(workspace_t(ctx, names[q][1], ps, &r.sxy[q]));
+    FD2D_TRY(workspace_t(ctx, names[q][2], ps, &r.szy[q]));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.v[q], 0, ps * 4, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.sxy[q], 0, ps * 4, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.szy[q], 0, ps * 4, ctx->stream));
     if (with_u) {
-      FD2D_TRY(workspace_t(ctx, names[q][3], np, &r.F.u[q]));
-      FD2D_CUDA(ctx, cudaMemsetAsync(r.F.u[q], 0, np * 4, ctx->stream));
-    } else {
-      r.F.u[q] = nullptr;
+      FD2D_TRY(workspace_t(ctx, names[q][3], ps, &r.u[q]));
+      FD2D_CUDA(ctx, cudaMemsetAsync(r.u[q], 0, ps * 4, ctx->stream));
     }
   }
-  std::vector<int> rec(a.rec_idx), src(a.src_idx);
-  if (rec.empty()) rec.push_back(0);
-  if (src.empty()) src.push_back(0);
-  FD2D_TRY(upload(ctx, "f32.rec", rec, &r.rec_pt));
-  FD2D_TRY(upload(ctx, "f32.src", src, &r.src_pt));
-  r.sgrid = dim3((g.nx + TX - 1) / TX, (g.nz + TZ - 1) / TZ);
-  r.pgrid = dim3((g.nx + 31) / 32, (g.nz + 7) / 8);
-  return FD2D_OK;
+  auto xy = [&](const std::vector<int>& idx) {
+    std::vector<int2> out;
+    for (int p : idx) out.push_back(make_int2(p % nx, p / nx));
+    if (out.empty()) out.push_back(make_int2(-1 << 30, -1 << 30));
+    return out;
+  };
+  FD2D_TRY(upload(ctx, "f32.rec", xy(a.rec_idx), &r.rec_xy));
+  FD2D_TRY(upload(ctx, "f32.src", xy(a.src_idx), &r.src_xy));
+  r.sgrid = dim3((nx + TX - 1) / TX, (nz + TZ - 1) / TZ);
+  r.pgrid = dim3((nx + 31) / 32, (nz + 7) / 8);
+  FD2D_TRY(step_attributes(ctx));
+  FD2D_TRY(contract_prepare(ctx));
+  return make_maps(ctx, r);
 }
 
 // Frequency-band weights (interpol_matrix) on the device.
@@ -415,26 +546,26 @@ fd2d_status spectrum_eff(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, d
 }
 
 // Injection planes for the listed coefficient rows (ifft rows, one per event).
-// Builds P from X (G or conj(stf)) and evaluates inj[j] = Re sum_k P_k c_{row_j,k}.
 struct Injection {
   std::vector<int> step_of_event;  // 1-based step n of event j
   std::vector<int> row_of_event;   // coefficient row used by event j
-  float* planes = nullptr;         // [chunk][np]
+  float* planes = nullptr;         // [chunk][ps]
   int chunk = 0, first = 0, count = 0;  // events [first, first+count) resident
-  float* P = nullptr;
+  float* P = nullptr;              // 2K pitched planes
   float* B = nullptr;              // [2K][n_events] float
   int n_events = 0;
 };
 
-fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, const double* Xre, const double* Xim,
+fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, Run& r, const double* Xre, const double* Xim,
                             double sign, const double* spec_eff, const double* M, const double* sd,
                             Injection& inj) {
-  const int64_t np = g.npts();
   const int K = g.K, ncol = g.nb == 0 ? 1 : g.nb;
   inj.n_events = (int)inj.step_of_event.size();
   if (inj.n_events == 0) return FD2D_OK;
-  FD2D_TRY(workspace_t(ctx, "f32.P", (size_t)np * 2 * K, &inj.P));
-  k32_make_P<<<(unsigned)((np + 127) / 128), 128, 0, ctx->stream>>>(K, ncol, M, sd, spec_eff, Xre, Xim, sign, inj.P, np);
+  FD2D_TRY(workspace_t(ctx, "f32.P", (size_t)r.ps * 2 * K, &inj.P));
+  dim3 pg((r.G.P + 31) / 32, (g.nz + 7) / 8);
+  k32_make_P<<<pg, r.pblock, 0, ctx->stream>>>(K, ncol, M, sd, spec_eff, Xre, Xim, sign, g.nx, g.nz, r.G.P,
+                                               r.ps, inj.P);
   FD2D_TRY(after_launch(ctx, "k32_make_P"));
   // B[k][j] = Re c(row_j, k); B[K+k][j] = -Im c(row_j, k)   (c = ifft_coeff, dw)
   std::vector<float> B((size_t)2 * K * inj.n_events);
@@ -448,33 +579,32 @@ fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, const double* Xre,
     }
   }
   FD2D_TRY(upload(ctx, "f32.injB", B, &inj.B));
-  // resident chunk of injection planes (bounded to ~4 GiB)
-  const size_t cap = (size_t)4 << 30;
-  inj.chunk = (int)std::max<int64_t>(1, std::min<int64_t>(inj.n_events, (int64_t)(cap / (np * 4))));
-  FD2D_TRY(workspace_t(ctx, "f32.inj", (size_t)np * inj.chunk, &inj.planes));
+  const size_t cap = (size_t)4 << 30;  // resident injection planes <= 4 GiB
+  inj.chunk = (int)std::max<int64_t>(1, std::min<int64_t>(inj.n_events, (int64_t)(cap / (r.ps * 4))));
+  FD2D_TRY(workspace_t(ctx, "f32.inj", (size_t)r.ps * inj.chunk, &inj.planes));
   inj.first = 0;
   inj.count = 0;
-  return FD2D_OK;
+  return set_inj_map(ctx, r, inj.planes, inj.chunk);
 }
 
-// Plane of event j (evaluates the next chunk of planes when j is not resident).
-fd2d_status injection_plane(fd2d_ctx* ctx, const Geometry& g, Injection& inj, int j, const float** out) {
+// Plane index of event j in the resident chunk (evaluates the next chunk when needed).
+fd2d_status injection_plane(fd2d_ctx* ctx, const Run& r, const Geometry& g, Injection& inj, int j, int* plane) {
   if (j < inj.first || j >= inj.first + inj.count) {
     inj.first = j;
     inj.count = std::min(inj.chunk, inj.n_events - j);
     ContractArgs c;
     c.A = inj.P;
-    c.lda = g.npts();
+    c.lda = r.ps;
     c.Kd = 2 * g.K;
     c.B = inj.B + j;
     c.ldb = inj.n_events;
-    c.M = (int)g.npts();
+    c.M = (int)r.ps;
     c.N = inj.count;
     c.out32 = inj.planes;
-    c.ldo = g.npts();
+    c.ldo = r.ps;
     FD2D_TRY(contract(ctx, ctx->stream, c));
   }
-  *out = inj.planes + (size_t)(j - inj.first) * g.npts();
+  *plane = j - inj.first;
   return FD2D_OK;
 }
 
@@ -492,13 +622,15 @@ struct Dft {
   int n_events = 0;
 };
 
-fd2d_status dft_init(fd2d_ctx* ctx, const Geometry& g, int n_events, Dft& d) {
+fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
   d.n_events = n_events;
   if (n_events == 0) return FD2D_OK;
-  const int64_t np = g.npts();
   const size_t cap = (size_t)2 << 30;  // snapshot chunk <= 2 GiB
-  d.T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)n_events, (int64_t)1024, (int64_t)(cap / (np * 4))}));
-  return workspace_t(ctx, "f32.dft_snaps", (size_t)np * d.T, &d.snaps);
+  d.T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)n_events, (int64_t)1024, (int64_t)(cap / (r.ps * 4))}));
+  FD2D_TRY(workspace_t(ctx, "f32.dft_snaps", (size_t)r.ps * d.T, &d.snaps));
+  // the pitch padding of the snapshot planes is never written by the stencil
+  FD2D_CUDA(ctx, cudaMemsetAsync(d.snaps, 0, (size_t)r.ps * d.T * 4, ctx->stream));
+  return FD2D_OK;
 }
 
 // rows[e] = (re, im) coefficient pairs for event e, laid out [e][2K] as float.
@@ -512,23 +644,27 @@ fd2d_status dft_add_target(fd2d_ctx* ctx, const char* name, const std::vector<fl
   return FD2D_OK;
 }
 
-float* dft_slot(const Geometry& g, Dft& d) { return d.snaps + (size_t)d.filled * g.npts(); }
+float* dft_slot(const Run& r, Dft& d) { return d.snaps + (size_t)d.filled * r.ps; }
 
-fd2d_status dft_flush(fd2d_ctx* ctx, const Geometry& g, Dft& d) {
+fd2d_status dft_flush(fd2d_ctx* ctx, const Run& r, const Geometry& g, Dft& d) {
   if (d.filled == 0) return FD2D_OK;
   for (auto& t : d.targets) {
     ContractArgs c;
     c.A = d.snaps;
-    c.lda = g.npts();
+    c.lda = r.ps;
     c.Kd = d.filled;
     c.B = t.B + (size_t)d.done * 2 * g.K;
     c.ldb = 2 * g.K;
-    c.M = (int)g.npts();
+    c.M = (int)r.ps;
     c.N = 2 * g.K;
     c.acc0 = t.re;
     c.acc1 = t.im;
     c.nsplit = g.K;
     c.ldacc = g.npts();
+    c.remap_pitch = r.G.P;
+    c.remap_nx = g.nx;
+    c.remap_nz = g.nz;
+    c.overwrite = d.done == 0;  // the first chunk defines the spectra
     FD2D_TRY(contract(ctx, ctx->stream, c));
   }
   d.done += d.filled;
@@ -536,10 +672,47 @@ fd2d_status dft_flush(fd2d_ctx* ctx, const Geometry& g, Dft& d) {
   return FD2D_OK;
 }
 
-fd2d_status dft_push(fd2d_ctx* ctx, const Geometry& g, Dft& d) {
+fd2d_status dft_push(fd2d_ctx* ctx, const Run& r, const Geometry& g, Dft& d) {
   ++d.filled;
-  if (d.filled == d.T || d.done + d.filled == d.n_events) return dft_flush(ctx, g, d);
+  if (d.filled == d.T || d.done + d.filled == d.n_events) return dft_flush(ctx, r, g, d);
   return FD2D_OK;
+}
+
+// Everything of a Run the captured loop depends on.
+void sig_run(Sig& sg, const Run& r) {
+  sg.add(r.G);
+  sg.add(r.b); sg.add(r.taper); sg.add(r.dtmu);
+  for (int q = 0; q < 2; ++q) { sg.add(r.v[q]); sg.add(r.sxy[q]); sg.add(r.szy[q]); sg.add(r.u[q]); }
+  sg.bytes(r.maps, sizeof(r.maps));
+  sg.add(r.sgrid.x); sg.add(r.sgrid.y); sg.add(r.pgrid.x); sg.add(r.pgrid.y);
+  sg.add(r.R); sg.add(r.rec_xy); sg.add(r.src_xy); sg.add(r.np); sg.add(r.ps);
+}
+
+void sig_args(Sig& sg, const Geometry& g, const SolveArgs& a) {
+  sg.add(g.nx); sg.add(g.nz); sg.add(g.nt); sg.add(g.fs); sg.add(g.fw); sg.add(g.K); sg.add(g.nb);
+  sg.add(a.mode); sg.add(a.src_idx.size()); sg.add(a.rec_idx.size());
+  sg.add(a.G_out); sg.add(a.G_in); sg.add(a.n_G_in); sg.add(a.G_re); sg.add(a.G_im);
+  sg.add(a.dmu); sg.add(a.C_in); sg.add(a.n_C_in); sg.add(a.C_out); sg.add(a.u_fwd); sg.add(a.n_u_fwd);
+  sg.add(a.stf_re); sg.add(a.stf_dims[0]); sg.add(a.stf_dims[1]); sg.add(a.stf_dims[2]);
+  sg.add(a.Kout); sg.add(a.sf_re); sg.add(a.sf_im); sg.add(a.seis);
+}
+
+void sig_dft(Sig& sg, const Dft& d) {
+  sg.add(d.T); sg.add(d.n_events); sg.add(d.snaps); sg.add(d.targets.size());
+  for (const auto& t : d.targets) { sg.add(t.B); sg.add(t.re); sg.add(t.im); }
+}
+
+void sig_inj(Sig& sg, const Injection& j) {
+  sg.add(j.n_events); sg.add(j.chunk); sg.add(j.planes); sg.add(j.P); sg.add(j.B);
+  sg.add_vec(j.step_of_event);
+}
+
+fd2d_status f32_copy_pitched(fd2d_ctx* ctx, const Run& r, const double* a, double scale, const char* name,
+                             float** out) {
+  FD2D_TRY(workspace_t(ctx, name, (size_t)r.ps, out));
+  dim3 pg((r.G.P + 31) / 32, (r.G.nz + 7) / 8);
+  k32_pitched<<<pg, r.pblock, 0, ctx->stream>>>(a, scale, r.G.nx, r.G.nz, r.G.P, *out);
+  return after_launch(ctx, "k32_pitched");
 }
 
 }  // namespace
@@ -557,7 +730,7 @@ fd2d_status fp32_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) 
   for (int n = 1; n <= nt; ++n)
     if ((n + nt - 1) % g.fs == 0) ev.push_back(n);
   Dft d;
-  FD2D_TRY(dft_init(ctx, g, (int)ev.size(), d));
+  FD2D_TRY(dft_init(ctx, r, (int)ev.size(), d));
   if (!ev.empty()) {
     std::vector<float> rows((size_t)ev.size() * 2 * K);
     for (size_t e = 0; e < ev.size(); ++e)
@@ -572,38 +745,36 @@ fd2d_status fp32_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) 
   FD2D_CUDA(ctx, cudaMemsetAsync(a.G_re, 0, (size_t)np * K * 8, ctx->stream));
   FD2D_CUDA(ctx, cudaMemsetAsync(a.G_im, 0, (size_t)np * K * 8, ctx->stream));
   float* dtdmu = nullptr;
-  float* Gs = nullptr;
   const bool born = a.dmu != nullptr;
-  if (born) {
-    FD2D_TRY(workspace_t(ctx, "f32.dtdmu", np, &dtdmu));
-    k32_scale_f<<<(unsigned)((np + 255) / 256), 256, 0, ctx->stream>>>(a.dmu, g.dt, dtdmu, np);
-    FD2D_TRY(after_launch(ctx, "k32_scale_f"));
-  }
-  (void)Gs;
+  if (born) FD2D_TRY(f32_copy_pitched(ctx, r, a.dmu, g.dt, "f32.dtdmu", &dtdmu));
   const int nr = (int)a.rec_idx.size();
-  int i_fw_out = 0, i_fw_in = 0, par = 0;
-  for (int n = 1; n <= nt; ++n) {
-    Step32 s{};
-    s.par = par;
-    if (a.mode != 0 && (n + nt - 1) % g.fw == 0) s.snap_pre = a.G_out + (size_t)np * (i_fw_out++);
-    if (born) {
-      FD2D_DISPATCH_R(r.R, k32_born_pre, r.G, r.F.sxy[par], r.F.szy[par], dtdmu, a.G_in + (size_t)np * (i_fw_in++));
-      FD2D_TRY(after_launch(ctx, "k32_born_pre"));
-    } else {
-      s.src_pt = r.src_pt;
-      s.nsrc = (int)a.src_idx.size();
-      s.amp_const = 1.0e9f;
+  Sig sg;
+  sig_run(sg, r); sig_args(sg, g, a); sig_dft(sg, d); sg.add(dtdmu);
+  return run_captured(ctx, "fp32_forward1", sg.h, [&]() -> fd2d_status {
+    int i_fw_out = 0, i_fw_in = 0, par = 0;
+    for (int n = 1; n <= nt; ++n) {
+      Step32 s{};
+      s.inj_plane = -1;
+      if (a.mode != 0 && (n + nt - 1) % g.fw == 0) s.snap_pre = a.G_out + (size_t)np * (i_fw_out++);
+      if (born) {
+        FD2D_DISPATCH_R(r.R, k32_born_pre, r.G, r.sxy[par], r.szy[par], dtdmu, a.G_in + (size_t)np * (i_fw_in++));
+        FD2D_TRY(after_launch(ctx, "k32_born_pre"));
+      } else {
+        s.src_xy = r.src_xy;
+        s.nsrc = (int)a.src_idx.size();
+        s.amp_const = 1.0e9f;  // stf = 1.0e9*ones(1,nt), code/run_forward1_green.m:64
+      }
+      const bool is_dft = (n + nt - 1) % g.fs == 0;
+      if (is_dft) s.snap_dft = dft_slot(r, d);
+      s.rec_xy = r.rec_xy;
+      s.nrec = nr;
+      s.seis_col = a.seis + (size_t)nr * (n - 1);
+      FD2D_TRY(launch_step(ctx, r, par, s));
+      if (is_dft) FD2D_TRY(dft_push(ctx, r, g, d));
+      par ^= 1;
     }
-    const bool is_dft = (n + nt - 1) % g.fs == 0;
-    if (is_dft) s.snap_dft = dft_slot(g, d);
-    s.rec_pt = r.rec_pt;
-    s.nrec = nr;
-    s.seis_col = a.seis + (size_t)nr * (n - 1);
-    FD2D_TRY(launch_step(ctx, r, s));
-    if (is_dft) FD2D_TRY(dft_push(ctx, g, d));
-    par ^= 1;
-  }
-  return FD2D_OK;
+    return FD2D_OK;
+  });
 }
 
 fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
@@ -620,38 +791,38 @@ fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& 
       inj.step_of_event.push_back(n);
       inj.row_of_event.push_back(n / g.fs - 1);
     }
-  FD2D_TRY(build_injection(ctx, g, a.Gin_re, a.Gin_im, 1.0, spec, M, a.source_dist, inj));
+  FD2D_TRY(build_injection(ctx, g, r, a.Gin_re, a.Gin_im, 1.0, spec, M, a.source_dist, inj));
   float* dmu32 = nullptr;
   const bool born = a.dmu != nullptr;
-  if (born) {
-    FD2D_TRY(workspace_t(ctx, "f32.dmu", np, &dmu32));
-    k32_f_from_d<<<(unsigned)((np + 255) / 256), 256, 0, ctx->stream>>>(a.dmu, dmu32, np);
-    FD2D_TRY(after_launch(ctx, "k32_f_from_d"));
-  }
+  if (born) FD2D_TRY(f32_copy_pitched(ctx, r, a.dmu, 1.0, "f32.dmu", &dmu32));
   const int nr = (int)a.rec_idx.size();
-  int i_fw_out = 0, par = 0, ev = 0;
-  for (int n = 1; n <= ntc; ++n) {
-    Step32 s{};
-    s.par = par;
-    s.has_u = 1;
-    if (a.mode != 0 && n % g.fw == 0) {
-      s.snap_pre = a.C_out + (size_t)np * (i_fw_out++);
-      s.snap_pre_u = 1;
+  Sig sg;
+  sig_run(sg, r); sig_args(sg, g, a); sig_inj(sg, inj); sg.add(dmu32);
+  return run_captured(ctx, "fp32_correlation", sg.h, [&]() -> fd2d_status {
+    int i_fw_out = 0, par = 0, ev = 0;
+    for (int n = 1; n <= ntc; ++n) {
+      Step32 s{};
+      s.inj_plane = -1;
+      s.has_u = 1;
+      if (a.mode != 0 && n % g.fw == 0) {
+        s.snap_pre = a.C_out + (size_t)np * (i_fw_out++);
+        s.snap_pre_u = 1;
+      }
+      if (n % g.fs == 0) FD2D_TRY(injection_plane(ctx, r, g, inj, ev++, &s.inj_plane));
+      s.rec_xy = r.rec_xy;
+      s.nrec = nr;
+      s.seis_col = a.seis + (size_t)nr * (n - 1);
+      s.rec_u = 1;  // u does not depend on this step's Born stress correction
+      FD2D_TRY(launch_step(ctx, r, par, s));
+      par ^= 1;
+      if (born && n != ntc) {
+        FD2D_DISPATCH_R(r.R, k32_born_post, r.G, r.sxy[par], r.szy[par], dmu32,
+                        a.C_in + (size_t)np * (n - 1), a.C_in + (size_t)np * n);
+        FD2D_TRY(after_launch(ctx, "k32_born_post"));
+      }
     }
-    if (n % g.fs == 0) FD2D_TRY(injection_plane(ctx, g, inj, ev++, &s.inj));
-    s.rec_pt = r.rec_pt;
-    s.nrec = nr;
-    s.seis_col = a.seis + (size_t)nr * (n - 1);
-    s.rec_u = 1;  // u does not depend on this step's Born stress correction
-    FD2D_TRY(launch_step(ctx, r, s));
-    par ^= 1;
-    if (born && n != ntc) {
-      FD2D_DISPATCH_R(r.R, k32_born_post, r.G, r.F.sxy[par], r.F.szy[par], dmu32,
-                      a.C_in + (size_t)np * (n - 1), a.C_in + (size_t)np * n);
-      FD2D_TRY(after_launch(ctx, "k32_born_post"));
-    }
-  }
-  return FD2D_OK;
+    return FD2D_OK;
+  });
 }
 
 fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
@@ -698,7 +869,7 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
       FD2D_CUDA(ctx, cudaMemsetAsync(z, 0, (size_t)np * K * 8, ctx->stream));
       sim = z;
     }
-    FD2D_TRY(build_injection(ctx, g, a.stf_re, sim, -1.0, spec, M, a.source_dist, inj));
+    FD2D_TRY(build_injection(ctx, g, r, a.stf_re, sim, -1.0, spec, M, a.source_dist, inj));
   }
   // DFT of u at the fs steps: stf_fft with the rows the reference uses, and the
   // natural-row spectrum U that forms the source kernel.
@@ -711,7 +882,7 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
   FD2D_CUDA(ctx, cudaMemsetAsync(a.sf_im, 0, (size_t)np * K * 8, ctx->stream));
   FD2D_CUDA(ctx, cudaMemsetAsync(a.Kout, 0, (size_t)np * 8 * (ncol + 1), ctx->stream));
   Dft d;
-  FD2D_TRY(dft_init(ctx, g, (int)ev.size(), d));
+  FD2D_TRY(dft_init(ctx, r, (int)ev.size(), d));
   double *Ure = nullptr, *Uim = nullptr;
   auto rows_for = [&](const std::vector<int>& rows_of_event) {
     std::vector<float> rows(ev.size() * 2 * K);
@@ -742,50 +913,52 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
     }
   }
   float* dmu32 = nullptr;
-  if (born) {
-    FD2D_TRY(workspace_t(ctx, "f32.dmu", np, &dmu32));
-    k32_f_from_d<<<(unsigned)((np + 255) / 256), 256, 0, ctx->stream>>>(a.dmu, dmu32, np);
-    FD2D_TRY(after_launch(ctx, "k32_f_from_d"));
-  }
+  if (born) FD2D_TRY(f32_copy_pitched(ctx, r, a.dmu, 1.0, "f32.dmu", &dmu32));
   double* Kmu = a.Kout + (size_t)np * ncol;
   const int nr = (int)a.rec_idx.size();
-  int i_fw_out = 0, i_fw_in = 0, par = 0, j_inj = 0;
-  for (int n = 1; n <= nt_loop; ++n) {
-    Step32 s{};
-    s.par = par;
-    s.has_u = 1;
-    if (save_u && n % g.fw == 0) {
-      s.snap_pre = a.C_out + (size_t)np * (i_fw_out++);
-      s.snap_pre_u = 1;
+  Sig sg;
+  sig_run(sg, r); sig_args(sg, g, a); sig_dft(sg, d); sig_inj(sg, inj);
+  sg.add(dmu32); sg.add(Ure); sg.add(Uim); sg.add(nt_loop);
+  FD2D_TRY(run_captured(ctx, "fp32_adjoint", sg.h, [&]() -> fd2d_status {
+    int i_fw_out = 0, i_fw_in = 0, par = 0, j_inj = 0;
+    for (int n = 1; n <= nt_loop; ++n) {
+      Step32 s{};
+      s.inj_plane = -1;
+      s.has_u = 1;
+      if (save_u && n % g.fw == 0) {
+        s.snap_pre = a.C_out + (size_t)np * (i_fw_out++);
+        s.snap_pre_u = 1;
+      }
+      if (stf2d) {
+        s.src_xy = r.src_xy;
+        s.nsrc = (int)a.src_idx.size();
+        s.amp = a.stf_re + (size_t)d0 * (n - 1);
+      } else if (inj.n_events && j_inj < inj.n_events && inj.step_of_event[j_inj] == n) {
+        FD2D_TRY(injection_plane(ctx, r, g, inj, j_inj++, &s.inj_plane));
+      }
+      const bool is_dft = d.n_events && n % g.fs == 0;
+      if (is_dft) s.snap_dft = dft_slot(r, d);
+      s.rec_xy = r.rec_xy;
+      s.nrec = nr;
+      s.seis_col = a.seis + (size_t)nr * (n - 1);
+      s.rec_u = 1;
+      FD2D_TRY(launch_step(ctx, r, par, s));
+      par ^= 1;
+      if (born && n != ntc) {
+        FD2D_DISPATCH_R(r.R, k32_born_post, r.G, r.sxy[par], r.szy[par], dmu32,
+                        a.C_in + (size_t)np * (n - 1), a.C_in + (size_t)np * n);
+        FD2D_TRY(after_launch(ctx, "k32_born_post"));
+      }
+      if (have_fwd && a.n_u_fwd >= i_fw_in + 1 && n % g.fw == 0) {
+        const float* uf = a.u_fwd + (size_t)np * (a.n_u_fwd - 1 - i_fw_in);
+        FD2D_DISPATCH_R(r.R, k32_kmu, r.G, r.u[par], uf, Kmu, (float)g.fw);
+        FD2D_TRY(after_launch(ctx, "k32_kmu"));
+        ++i_fw_in;
+      }
+      if (is_dft) FD2D_TRY(dft_push(ctx, r, g, d));
     }
-    if (stf2d) {
-      s.src_pt = r.src_pt;
-      s.nsrc = (int)a.src_idx.size();
-      s.amp = a.stf_re + (size_t)d0 * (n - 1);
-    } else if (!inj.step_of_event.empty() && j_inj < inj.n_events && inj.step_of_event[j_inj] == n) {
-      FD2D_TRY(injection_plane(ctx, g, inj, j_inj++, &s.inj));
-    }
-    const bool is_dft = d.n_events && n % g.fs == 0;
-    if (is_dft) s.snap_dft = dft_slot(g, d);
-    s.rec_pt = r.rec_pt;
-    s.nrec = nr;
-    s.seis_col = a.seis + (size_t)nr * (n - 1);
-    s.rec_u = 1;
-    FD2D_TRY(launch_step(ctx, r, s));
-    par ^= 1;
-    if (born && n != ntc) {
-      FD2D_DISPATCH_R(r.R, k32_born_post, r.G, r.F.sxy[par], r.F.szy[par], dmu32,
-                      a.C_in + (size_t)np * (n - 1), a.C_in + (size_t)np * n);
-      FD2D_TRY(after_launch(ctx, "k32_born_post"));
-    }
-    if (have_fwd && a.n_u_fwd >= i_fw_in + 1 && n % g.fw == 0) {
-      const float* uf = a.u_fwd + (size_t)np * (a.n_u_fwd - 1 - i_fw_in);
-      FD2D_DISPATCH_R(r.R, k32_kmu, r.G, r.F.u[par], uf, Kmu, (float)g.fw);
-      FD2D_TRY(after_launch(ctx, "k32_kmu"));
-      ++i_fw_in;
-    }
-    if (is_dft) FD2D_TRY(dft_push(ctx, g, d));
-  }
+    return FD2D_OK;
+  }));
   if (Gvalid) {
     k32_source_kernel<<<(unsigned)((np + 127) / 128), 128, 0, ctx->stream>>>(
         K, ncol, M, spec, a.Gin_re, a.Gin_im, Ure, Uim, g.dw / g.dt, a.Kout, np);

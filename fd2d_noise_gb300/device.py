@@ -43,7 +43,12 @@ class DeviceSession:
         self.device = device
         self.ctx = _lib.Context(device, _prec(precision))
         self.ctx.set_memspace(_lib.MEM_DEVICE)
-        self.ctx.set_stream(torch.cuda.current_stream(device).cuda_stream)
+        # time loops are captured as CUDA graphs, which the legacy default
+        # stream does not allow: work on torch's current stream unless that is
+        # the default one, else on a stream of our own.
+        cur = torch.cuda.current_stream(device)
+        self.stream = cur if cur.cuda_stream != 0 else torch.cuda.Stream(device)
+        self.ctx.set_stream(self.stream.cuda_stream)
         self.c = cfg.to_c()
 
     def set_precision(self, precision: str):

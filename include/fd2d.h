@@ -218,6 +218,15 @@ fd2d_status fd2d_noise_adjoint(fd2d_ctx* ctx, const fd2d_config* cfg,
                                float* u_out,
                                double* seismograms);
 
+/* ---- building block ----------------------------------------------------------
+ * R[n*ldr + m] = sum_{k<Kd} A[k*lda + m] * B[k*ldb + n]  for m < M, n < N:
+ * the split-TF32 tensor-core contraction behind the on-the-fly DFT
+ * (code/run_forward1_green.m:176-183) and the correlation-source injection
+ * (code/run_forward2_correlation.m:195-216).  Device pointers, FP32, queued on
+ * the context's stream.  No reference counterpart as a separate function. */
+fd2d_status fd2d_contract_f32(fd2d_ctx* ctx, const float* A, int64_t lda, const float* B, int64_t ldb,
+                              int32_t M, int32_t N, int32_t Kd, float* R, int64_t ldr);
+
 #ifdef __cplusplus
 }
 #endif
