@@ -90,7 +90,7 @@ struct fd2d_ctx {
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
-  struct TimerRec { int a, b, cls; int64_t units; };
+  struct TimerRec { int a, b, cls; int64_t units, count; };
   std::vector<TimerRec> recs;
   double t_ms[FD2D_TIMER_COUNT] = {0, 0, 0};
   int64_t t_cnt[FD2D_TIMER_COUNT] = {0, 0, 0};
@@ -122,7 +122,8 @@ void free_workspace(fd2d_ctx* ctx);
 
 // Brackets the next launch(es) with timing events when instrumentation is on.
 int timer_begin(fd2d_ctx* ctx, cudaStream_t stream);
-void timer_end(fd2d_ctx* ctx, cudaStream_t stream, int begin, int cls, int64_t units);
+// `count` launches of class `cls` doing `units` work ran between begin and end.
+void timer_end(fd2d_ctx* ctx, cudaStream_t stream, int begin, int cls, int64_t units, int64_t count = 1);
 
 // Checks the last launch and counts it.
 fd2d_status after_launch(fd2d_ctx* ctx, const char* what);

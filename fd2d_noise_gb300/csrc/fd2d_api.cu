@@ -102,17 +102,17 @@ int timer_begin(fd2d_ctx* ctx, cudaStream_t stream) {
   return i;
 }
 
-void timer_end(fd2d_ctx* ctx, cudaStream_t stream, int begin, int cls, int64_t units) {
+void timer_end(fd2d_ctx* ctx, cudaStream_t stream, int begin, int cls, int64_t units, int64_t count) {
   if (!ctx->timing || begin < 0) return;
   if (ctx->capturing) {
     int i = capture_event(ctx, stream);
-    if (i >= 0) ctx->cap_recs.push_back({begin, i, cls, units});
+    if (i >= 0) ctx->cap_recs.push_back({begin, i, cls, units, count});
     return;
   }
   int i = next_event(ctx);
   if (i < 0) return;
   cudaEventRecord(ctx->ev_pool[i], stream);
-  ctx->recs.push_back({begin, i, cls, units});
+  ctx->recs.push_back({begin, i, cls, units, count});
 }
 
 static fd2d_ctx::GraphEntry* find_graph(fd2d_ctx* ctx, const char* name) {
@@ -137,7 +137,7 @@ static fd2d_status launch_graph(fd2d_ctx* ctx, fd2d_ctx::GraphEntry& g) {
       float t = 0.f;
       if (cudaEventElapsedTime(&t, g.ev[r.a], g.ev[r.b]) == cudaSuccess) {
         ctx->t_ms[r.cls] += t;
-        ctx->t_cnt[r.cls] += 1;
+        ctx->t_cnt[r.cls] += r.count;
         ctx->t_units[r.cls] += r.units;
       }
     }
@@ -409,7 +409,7 @@ fd2d_status fd2d_ctx_timing(fd2d_ctx* ctx, double* ms, int64_t* launches, int64_
     float t = 0.f;
     if (cudaEventElapsedTime(&t, ctx->ev_pool[r.a], ctx->ev_pool[r.b]) == cudaSuccess) {
       ctx->t_ms[r.cls] += t;
-      ctx->t_cnt[r.cls] += 1;
+      ctx->t_cnt[r.cls] += r.count;
       ctx->t_units[r.cls] += r.units;
     }
   }
