@@ -34,7 +34,7 @@ def test_colon_end_and_linear_indexing():
 def test_precedence_and_min_find():
     src = ("function [r, k] = f(x, p)\nr = -2^2 + 3*2 - 1;\n"
            "k = min( find( min(abs(x-p)) == abs(x-p) ) );\n")
-    r, k = run(src, "f", np.array([[0.0, 1.0, 2.0, 3.0]]), 1.5)
+    r, k = run(src, "f", np.array([[0.0, 1.0, 2.0, 3.0]]), 1.5, nargout=2)
     assert r[0, 0] == 1.0 and k[0, 0] == 2.0  # tie at 1 and 2 goes to the lower index
 
 
