@@ -31,6 +31,7 @@ EXPORTED = [
     "fd2d_ctx_kernel_launches", "fd2d_last_error", "fd2d_query_sizes",
     "fd2d_forward1_green", "fd2d_forward2_correlation", "fd2d_noise_adjoint",
     "fd2d_ctx_set_timing", "fd2d_ctx_timing", "fd2d_contract_f32",
+    "fd2d_forward1_seismograms_noalloc",
 ]
 TIMER_STEP_V, TIMER_STEP_VU, TIMER_CONTRACT, TIMER_COUNT = 0, 1, 2, 3
 
@@ -74,6 +75,7 @@ def load(path: str = LIB_PATH):
         L.fd2d_last_error.restype = ctypes.c_char_p
         L.fd2d_query_sizes.argtypes = [_cfgp, _i32, ctypes.POINTER(FD2DSizes)]
         L.fd2d_contract_f32.argtypes = [_vp, _vp, _i64, _vp, _i64, _i32, _i32, _i32, _vp, _i64]
+        L.fd2d_forward1_seismograms_noalloc.argtypes = [_cfgp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp]
         L.fd2d_ctx_set_timing.argtypes = [_vp, _i32]
         L.fd2d_ctx_timing.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i64),
                                       ctypes.POINTER(_i64)]

@@ -974,3 +974,156 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
 }
 
 }  // namespace fd2d
+
+// ---------------------------------------------------------------------------------
+// Allocation-free entry point (include/fd2d.h: fd2d_forward1_seismograms_noalloc).
+// For callers that must not allocate GPU memory: all working memory of the
+// Green-function time loop lives in the statically sized device array below.
+// ---------------------------------------------------------------------------------
+#include <mutex>
+
+namespace fd2d {
+namespace {
+
+// The scratch array.  In host code this name is only a host-side stand-in for
+// the device symbol -- never an address to hand to a kernel; its device
+// address is looked up with cudaGetSymbolAddress once per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[FD2D_NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void* g_noalloc_dev_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device (looked up on the
+// first call for that device, with the device current).
+fd2d_status noalloc_scratch(int dev, unsigned char** out) {
+  if (dev < 0 || dev >= kMaxDevices) return set_error(nullptr, FD2D_ERR_ARG, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_dev_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return set_error(nullptr, FD2D_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    }
+    g_noalloc_dev_ptr[dev] = p;
+  }
+  *out = static_cast<unsigned char*>(g_noalloc_dev_ptr[dev]);
+  return FD2D_OK;
+}
+
+// dt/rho and dt*mu into pitched planes (taper comes from the host).
+__global__ void k32_prep_coeffs(const double* mu, const double* rho, double dt, int nx, int nz, int P, float* b,
+                                float* dtmu) {
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+  if (i >= P || j >= nz) return;
+  const int64_t q = i + (int64_t)P * j;
+  if (i >= nx) {
+    b[q] = dtmu[q] = 0.f;
+    return;
+  }
+  const int64_t p = i + (int64_t)nx * j;
+  b[q] = (float)(dt / rho[p]);
+  dtmu[q] = (float)(dt * mu[p]);
+}
+
+}  // namespace
+}  // namespace fd2d
+
+extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg, const double* mu,
+                                                         const double* rho, const double* src, int32_t ns,
+                                                         const double* rec, int32_t nr, double* seismograms,
+                                                         void* stream_ptr) {
+  using namespace fd2d;
+  Geometry g;
+  std::string err;
+  fd2d_status st = make_geometry(cfg, g, err);
+  if (st != FD2D_OK) return set_error(nullptr, st, err);
+  if (!mu || !rho) return set_error(nullptr, FD2D_ERR_ARG, "mu and rho are required");
+  if (ns < 0 || nr < 0 || (ns && !src) || (nr && !rec) || (nr && !seismograms))
+    return set_error(nullptr, FD2D_ERR_ARG, "bad source / receiver arguments");
+  const int nx = g.nx, nz = g.nz, P = (nx + 31) / 32 * 32;
+  const int64_t ps = ((int64_t)P * nz + 127) / 128 * 128;
+  const size_t plane = (size_t)ps * 4;
+  const size_t head = 256 + (((size_t)(ns + nr) * 8 + 255) / 256) * 256;
+  const size_t need = head + 9 * plane;
+  if (need > FD2D_NOALLOC_SCRATCH_BYTES)
+    return set_error(nullptr, FD2D_ERR_SHAPE,
+                     "grid needs " + std::to_string(need) + " bytes of scratch; the allocation-free entry point has " +
+                         std::to_string((size_t)FD2D_NOALLOC_SCRATCH_BYTES));
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) return set_error(nullptr, FD2D_ERR_NO_DEVICE, cudaGetErrorString(ce));
+  unsigned char* base = nullptr;
+  FD2D_TRY(noalloc_scratch(dev, &base));
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+  // carve the scratch: error flag | sources, receivers | 9 planes
+  int* d_err = reinterpret_cast<int*>(base);
+  int2* src_xy = reinterpret_cast<int2*>(base + 256);
+  int2* rec_xy = src_xy + ns;
+  float* planes = reinterpret_cast<float*>(base + head);
+  Run r;
+  r.np = g.npts();
+  r.ps = ps;
+  r.R = g.r;
+  r.G.nx = nx; r.G.nz = nz; r.G.P = P;
+  for (int m = 0; m < 4; ++m) r.G.c[m] = (float)g.c[m];
+  r.G.inv_dx = (float)(1.0 / g.dx);
+  r.G.inv_dz = (float)(1.0 / g.dz);
+  r.G.dt = (float)g.dt;
+  r.G.err = d_err;
+  r.b = planes;
+  r.taper = planes + ps;
+  r.dtmu = planes + 2 * ps;
+  for (int q = 0; q < 2; ++q) {
+    r.v[q] = planes + (3 + q) * ps;
+    r.sxy[q] = planes + (5 + q) * ps;
+    r.szy[q] = planes + (7 + q) * ps;
+    r.u[q] = nullptr;
+  }
+  r.sgrid = dim3((nx + TX - 1) / TX, (nz + TZ - 1) / TZ);
+  r.pgrid = dim3((P + 31) / 32, (nz + 7) / 8);
+  // The array keeps the previous call's contents: clear what must start at zero.
+  FD2D_CUDA(nullptr, cudaMemsetAsync(d_err, 0, sizeof(int), stream));
+  FD2D_CUDA(nullptr, cudaMemsetAsync(r.v[0], 0, 6 * plane, stream));  // v, sxy, szy of both buffers
+  // host-side inputs: taper (pitched FP32), source / receiver nodes
+  std::vector<float> taper((size_t)ps, 0.f);
+  for (int j = 0; j < nz; ++j)
+    for (int i = 0; i < nx; ++i) taper[i + (size_t)P * j] = (float)g.absbound[i + (size_t)nx * j];
+  std::vector<int2> xy;
+  for (int k = 0; k < ns; ++k) xy.push_back(make_int2(nearest_node(g.x, src[k]), nearest_node(g.z, src[ns + k])));
+  for (int k = 0; k < nr; ++k) xy.push_back(make_int2(nearest_node(g.x, rec[k]), nearest_node(g.z, rec[nr + k])));
+  FD2D_CUDA(nullptr, cudaMemcpyAsync(r.taper, taper.data(), plane, cudaMemcpyHostToDevice, stream));
+  if (!xy.empty())
+    FD2D_CUDA(nullptr, cudaMemcpyAsync(src_xy, xy.data(), xy.size() * sizeof(int2), cudaMemcpyHostToDevice, stream));
+  k32_prep_coeffs<<<r.pgrid, r.pblock, 0, stream>>>(mu, rho, g.dt, nx, nz, P, r.b, r.dtmu);
+  FD2D_CUDA(nullptr, cudaGetLastError());
+  FD2D_TRY(step_attributes(nullptr));
+  FD2D_TRY(make_maps(nullptr, r));
+  for (int n = 1, par = 0; n <= g.nt; ++n, par ^= 1) {
+    Step32 s{};
+    s.inj_plane = -1;
+    s.src_xy = src_xy;
+    s.nsrc = ns;
+    s.amp_const = 1.0e9f;  // stf = 1.0e9*ones(1,nt), code/run_forward1_green.m:64
+    s.rec_xy = rec_xy;
+    s.nrec = nr;
+    s.seis_col = seismograms + (size_t)nr * (n - 1);
+    s.vo = r.v[1 - par];
+    s.sxyo = r.sxy[1 - par];
+    s.szyo = r.szy[1 - par];
+    s.uo = nullptr;
+    switch (r.R) {
+      case 1: k32_step<1><<<r.sgrid, NT, Tile<1>::BYTES, stream>>>(r.G, r.maps[par], s); break;
+      case 2: k32_step<2><<<r.sgrid, NT, Tile<2>::BYTES, stream>>>(r.G, r.maps[par], s); break;
+      case 3: k32_step<3><<<r.sgrid, NT, Tile<3>::BYTES, stream>>>(r.G, r.maps[par], s); break;
+      default: k32_step<4><<<r.sgrid, NT, Tile<4>::BYTES, stream>>>(r.G, r.maps[par], s); break;
+    }
+    FD2D_CUDA(nullptr, cudaGetLastError());
+  }
+  int herr = 0;
+  FD2D_CUDA(nullptr, cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  FD2D_CUDA(nullptr, cudaStreamSynchronize(stream));
+  if (herr) return set_error(nullptr, FD2D_ERR_TIMEOUT, "a bounded device-side wait gave up");
+  return FD2D_OK;
+}

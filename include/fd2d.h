@@ -227,6 +227,28 @@ fd2d_status fd2d_noise_adjoint(fd2d_ctx* ctx, const fd2d_config* cfg,
 fd2d_status fd2d_contract_f32(fd2d_ctx* ctx, const float* A, int64_t lda, const float* B, int64_t ldb,
                               int32_t M, int32_t N, int32_t Kd, float* R, int64_t ldr);
 
+/* ---- allocation-free Green-function seismograms --------------------------------
+ * No counterpart in the reference: an extra entry point for callers that must
+ * not allocate GPU memory -- hosts that own a fixed device-memory budget, or run
+ * inside a runtime whose allocator they do not control, so that any cudaMalloc
+ * could fail or stall mid-run.  It runs the FP32 Green-function time loop of
+ * fd2d_forward1_green (mode 0, point force 1e9 at `src`) and returns only the
+ * velocity seismograms; no spectra, no snapshots, no context.
+ *   mu, rho, seismograms  DEVICE pointers (nx*nz, nx*nz, nr*nt doubles)
+ *   src, rec              HOST pointers (ns-by-2, nr-by-2 positions [m])
+ *   stream                cudaStream_t to queue the work on (NULL: default stream)
+ * All working memory is one statically sized device array compiled into the
+ * library (FD2D_NOALLOC_SCRATCH_BYTES per GPU, held until the process exits):
+ * 9 FP32 planes of ((nx rounded up to 32) * nz) floats plus 8 bytes per source
+ * and receiver must fit, else FD2D_ERR_SHAPE.  The first call on a device looks
+ * up that array's device address (make that first call before any stream
+ * capture).  Every call reuses the same array, so calls whose work overlaps on
+ * the GPU (other streams, other host threads) race: serialise them. */
+#define FD2D_NOALLOC_SCRATCH_BYTES (16u << 20)
+fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg, const double* mu, const double* rho,
+                                              const double* src, int32_t ns, const double* rec, int32_t nr,
+                                              double* seismograms, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
