@@ -209,11 +209,12 @@ def main():
     refs = [to_device(w.ref_stations[i:i + 1], np.float64, dev) for i in range(n_ref)]
     G_re, G_im, _, seis_g = sess.green_outputs(nr)
     seis_c = [sess.zeros(nr * cfg.ntc, torch.float64) for _ in range(n_ref)]
+    batch = [dict(cfg=cfg, mu=mu, rho=rho, spectrum=spec, source_dist=sd, src=refs[i], rec=rec, nr=nr,
+                  out=seis_c[i]) for i in range(n_ref)]
 
     def step(s: DeviceSession, outs):
-        for i in range(n_ref):
-            s.forward1_green(mu, rho, refs[i], 1, rec, nr, G_re, G_im, seis_g)
-            s.forward2_correlation(mu, rho, G_re, G_im, spec, 1, sd, 1, rec, nr, outs[i])
+        # one call = the station loop of code/calculate_data.m:189-202
+        s.correlation_batch(batch)
 
     gpt_step = n_ref * w.gpt_per_station()
     torch.cuda.synchronize()
@@ -350,21 +351,21 @@ def e2e(args, w, dev):
     spec, sd = pinned(w.spectrum, np.float64), pinned(w.source_dist, np.float64)
     rec = pinned(w.receivers, np.float64)
     refs = [pinned(w.ref_stations[i:i + 1], np.float64) for i in range(n_ref)]
-    G_re = torch.empty(np_ * K, dtype=torch.float64, pin_memory=True)
-    G_im = torch.empty(np_ * K, dtype=torch.float64, pin_memory=True)
-    seis_g = torch.empty(nr * cfg.nt, dtype=torch.float64, pin_memory=True)
-    seis_c = torch.empty(nr * cfg.ntc, dtype=torch.float64, pin_memory=True)
     c = cfg.to_c()
     L = ctx.L
+    outs = [torch.empty(nr * cfg.ntc, dtype=torch.float64, pin_memory=True) for _ in range(n_ref)]
+    jobs = (_lib.FD2DJob * n_ref)()
+    for i in range(n_ref):
+        jobs[i].cfg = ctypes.pointer(c)
+        jobs[i].mu, jobs[i].rho = mu.data_ptr(), rho.data_ptr()
+        jobs[i].spectrum, jobs[i].n_noise_sources = spec.data_ptr(), 1
+        jobs[i].source_dist, jobs[i].n_dist = sd.data_ptr(), 1
+        jobs[i].src, jobs[i].rec, jobs[i].nr = refs[i].data_ptr(), rec.data_ptr(), nr
+        jobs[i].correlations = outs[i].data_ptr()
 
     def step():
-        for i in range(n_ref):
-            _lib.check(L.fd2d_forward1_green(ctx.h, ctypes.byref(c), p(mu), p(rho), p(refs[i]), 1,
-                                             p(rec), nr, 0, None, None, 0, p(G_re), p(G_im), None,
-                                             p(seis_g)), ctx.h)
-            _lib.check(L.fd2d_forward2_correlation(ctx.h, ctypes.byref(c), p(mu), p(rho), p(G_re),
-                                                   p(G_im), K, p(spec), 1, p(sd), 1, p(rec), nr, 0,
-                                                   None, None, 0, p(seis_c), None), ctx.h)
+        # host buffers in, correlations back to the host: code/calculate_data.m:189-202
+        _lib.check(L.fd2d_correlation_batch(ctx.h, jobs, n_ref), ctx.h)
 
     for _ in range(max(1, min(args.warmup, 2))):
         step()
@@ -373,12 +374,13 @@ def e2e(args, w, dev):
         step()
     dt = time.perf_counter() - t0
     gpt = n_ref * w.gpt_per_station() * args.steps
-    h2d = n_ref * (2 * (2 * np_ * 8) + 16 + 2 * nr * 16 + 2 * np_ * K * 8 + K * 8 + np_ * 8)
-    d2h = n_ref * (2 * np_ * K * 8 + nr * cfg.nt * 8 + nr * cfg.ntc * 8)
+    # per station: mu, rho, spectrum, source distribution and positions in; correlations out
+    h2d = n_ref * (2 * np_ * 8 + K * 8 + np_ * 8 + 16 + nr * 16)
+    d2h = n_ref * (nr * cfg.ntc * 8)
     ctx.close()
     return {"value": gpt / dt / 1e9, "unit": "Gpt-updates/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * dt / args.steps,
-            "path": "fd2d_forward1_green + fd2d_forward2_correlation, host (pinned) buffers"}
+            "path": "fd2d_correlation_batch (Green + correlation per station), host (pinned) buffers"}
 
 
 if __name__ == "__main__":

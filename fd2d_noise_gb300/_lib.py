@@ -31,8 +31,20 @@ EXPORTED = [
     "fd2d_ctx_kernel_launches", "fd2d_last_error", "fd2d_query_sizes",
     "fd2d_forward1_green", "fd2d_forward2_correlation", "fd2d_noise_adjoint",
     "fd2d_ctx_set_timing", "fd2d_ctx_timing", "fd2d_contract_f32",
-    "fd2d_forward1_seismograms_noalloc",
+    "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
 ]
+
+
+class FD2DJob(ctypes.Structure):
+    """ctypes mirror of ``fd2d_job``."""
+
+    _fields_ = [
+        ("cfg", ctypes.POINTER(FD2DConfig)), ("mu", ctypes.c_void_p), ("rho", ctypes.c_void_p),
+        ("spectrum", ctypes.c_void_p), ("n_noise_sources", ctypes.c_int32),
+        ("source_dist", ctypes.c_void_p), ("n_dist", ctypes.c_int32),
+        ("src", ctypes.c_void_p), ("rec", ctypes.c_void_p), ("nr", ctypes.c_int32),
+        ("correlations", ctypes.c_void_p),
+    ]
 TIMER_STEP_V, TIMER_STEP_VU, TIMER_CONTRACT, TIMER_COUNT = 0, 1, 2, 3
 
 _vp = ctypes.c_void_p
@@ -76,6 +88,8 @@ def load(path: str = LIB_PATH):
         L.fd2d_query_sizes.argtypes = [_cfgp, _i32, ctypes.POINTER(FD2DSizes)]
         L.fd2d_contract_f32.argtypes = [_vp, _vp, _i64, _vp, _i64, _i32, _i32, _i32, _vp, _i64]
         L.fd2d_forward1_seismograms_noalloc.argtypes = [_cfgp, _vp, _vp, _vp, _i32, _vp, _i32, _vp, _vp]
+        L.fd2d_correlation_batch.argtypes = [_vp, ctypes.POINTER(FD2DJob), _i32]
+        L.fd2d_ctx_set_memory_budget.argtypes = [_vp, _i64]
         L.fd2d_ctx_set_timing.argtypes = [_vp, _i32]
         L.fd2d_ctx_timing.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_i64),
                                       ctypes.POINTER(_i64)]

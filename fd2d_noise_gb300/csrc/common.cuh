@@ -9,6 +9,8 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <functional>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -45,9 +47,11 @@ fd2d_status set_error(fd2d_ctx* ctx, fd2d_status s, const std::string& msg);
 struct Geometry {
   int nx = 0, nz = 0, nt = 0, ntc = 0, order = 4, r = 2, K = 0, fs = 1, fw = 1, nb = 0;
   double Lx = 0, Lz = 0, dt = 0, dx = 0, dz = 0, dw = 0;
-  std::vector<double> x, z, w, absbound;  // absbound nx*nz column-major
+  std::vector<double> x, z, w;
+  std::shared_ptr<const std::vector<double>> absbound;  // taper, nx*nz column-major (shared: copies are cheap)
   double c[4] = {0, 0, 0, 0};             // staggered coefficients c_1..c_r
   std::vector<double> t_fwd, t_corr;      // time axes (0:dt:(nt-1)dt and -(nt-1)dt:dt:(nt-1)dt)
+  uint64_t key = 0;                       // identity of the configuration (config_hash)
   int64_t npts() const { return (int64_t)nx * nz; }
 };
 
@@ -68,6 +72,7 @@ inline void dft_coeff(double th, double scale, double& re, double& im) {
 struct DevBuf {
   void* ptr = nullptr;
   size_t bytes = 0;
+  uint64_t tag = 0;  // identity of the content last uploaded (upload_tagged)
 };
 
 }  // namespace fd2d
@@ -107,6 +112,12 @@ struct fd2d_ctx {
     int64_t launches = 0;  // kernels inside the graph
   };
   std::vector<std::pair<std::string, GraphEntry>> graphs;
+  // batches: workspace names of job j carry a prefix; side streams and events
+  // fork the jobs' loops into parallel branches of one captured graph
+  std::string ws_prefix;
+  int64_t mem_budget = 0;  // batch device-memory budget (0: 80 % of free memory)
+  std::vector<cudaStream_t> side_streams;
+  std::vector<cudaEvent_t> fork_events;
 };
 
 namespace fd2d {
@@ -168,6 +179,27 @@ fd2d_status stage_in(fd2d_ctx* ctx, const char* name, const void* src, size_t by
 fd2d_status out_buffer(fd2d_ctx* ctx, const char* name, void* user, size_t bytes, void** dev);
 fd2d_status stage_out(fd2d_ctx* ctx, void* user, const void* dev, size_t bytes);
 
+// Like upload(), but the content is only generated and copied when the buffer's
+// tag differs from `tag` (tables that depend only on the configuration).
+fd2d_status workspace_tag(fd2d_ctx* ctx, const char* name, size_t bytes, uint64_t tag, void** out, bool* hit);
+template <typename T, typename F>
+fd2d_status upload_tagged(fd2d_ctx* ctx, const char* name, uint64_t tag, size_t count, F&& fill, T** dev) {
+  bool hit = false;
+  void* p = nullptr;
+  FD2D_TRY(workspace_tag(ctx, name, (count ? count : 1) * sizeof(T) + 256, tag, &p, &hit));
+  *dev = static_cast<T*>(p);
+  if (hit || count == 0) return FD2D_OK;
+  std::vector<T> h(count);
+  fill(h);
+  cudaError_t e = cudaMemcpyAsync(p, h.data(), count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) return set_error(ctx, FD2D_ERR_CUDA, std::string("upload ") + name + ": " + cudaGetErrorString(e));
+  // pageable source: the copy has been staged when cudaMemcpyAsync returns
+  return FD2D_OK;
+}
+
+// Identity of a configuration (all fields and frequencies).
+uint64_t config_hash(const fd2d_config* cfg);
+
 // Uploads a host vector into a named workspace buffer (async on the ctx stream).
 template <typename T>
 fd2d_status upload(fd2d_ctx* ctx, const char* name, const std::vector<T>& v, T** dev) {
@@ -211,7 +243,20 @@ struct SolveArgs {
   double* seis = nullptr;
 };
 
+// A prepared time loop: `loop` only launches work on ctx->stream (capturable).
+struct LoopPlan {
+  std::string name;
+  uint64_t key = 0;
+  std::function<fd2d_status()> loop;
+};
+
+// Runs the loops of several prepared solves as parallel branches of one cached
+// CUDA graph (fork/join over side streams).
+fd2d_status run_parallel(fd2d_ctx* ctx, const char* name, uint64_t key, std::vector<LoopPlan>& plans);
+
 // Precision-specific drivers (solver_fp64.cu / solver_fp32.cu).
+fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, LoopPlan& plan);
+fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, LoopPlan& plan);
 fd2d_status fp64_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
 fd2d_status fp64_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
 fd2d_status fp64_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);

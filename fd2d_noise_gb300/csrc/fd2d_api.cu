@@ -24,7 +24,9 @@ fd2d_status set_error(fd2d_ctx* ctx, fd2d_status s, const std::string& msg) {
   return s;
 }
 
-fd2d_status workspace(fd2d_ctx* ctx, const char* name, size_t bytes, void** out) {
+fd2d_status workspace(fd2d_ctx* ctx, const char* name_in, size_t bytes, void** out) {
+  const std::string key = ctx->ws_prefix + name_in;
+  const char* name = key.c_str();
   for (auto& kv : ctx->bufs) {
     if (kv.first == name) {
       if (kv.second.bytes >= bytes) {
@@ -43,6 +45,7 @@ fd2d_status workspace(fd2d_ctx* ctx, const char* name, size_t bytes, void** out)
                                                 std::to_string(bytes) + " B): " + cudaGetErrorString(e));
       }
       kv.second.bytes = bytes;
+      kv.second.tag = 0;
       *out = kv.second.ptr;
       return FD2D_OK;
     }
@@ -57,6 +60,18 @@ fd2d_status workspace(fd2d_ctx* ctx, const char* name, size_t bytes, void** out)
   b.bytes = bytes;
   ctx->bufs.emplace_back(name, b);
   *out = b.ptr;
+  return FD2D_OK;
+}
+
+fd2d_status workspace_tag(fd2d_ctx* ctx, const char* name, size_t bytes, uint64_t tag, void** out, bool* hit) {
+  FD2D_TRY(workspace(ctx, name, bytes, out));
+  const std::string key = ctx->ws_prefix + name;
+  *hit = false;
+  for (auto& kv : ctx->bufs)
+    if (kv.first == key) {
+      *hit = kv.second.tag == tag && tag != 0;
+      kv.second.tag = tag;
+    }
   return FD2D_OK;
 }
 
@@ -216,6 +231,40 @@ fd2d_status graph_end(fd2d_ctx* ctx, const char* name, uint64_t key, fd2d_status
   return launch_graph(ctx, *g);
 }
 
+fd2d_status run_parallel(fd2d_ctx* ctx, const char* name, uint64_t key, std::vector<LoopPlan>& plans) {
+  Sig sg;
+  sg.add(key);
+  for (const auto& p : plans) sg.add(p.key);
+  // side streams and fork/join events exist before the capture starts
+  while (ctx->side_streams.size() < plans.size()) {
+    cudaStream_t s;
+    FD2D_CUDA(ctx, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    ctx->side_streams.push_back(s);
+  }
+  while (ctx->fork_events.size() < plans.size() + 1) {
+    cudaEvent_t e;
+    FD2D_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->fork_events.push_back(e);
+  }
+  bool replayed = false;
+  FD2D_TRY(graph_begin(ctx, name, sg.h, &replayed));
+  if (replayed) return FD2D_OK;
+  cudaStream_t main = ctx->stream;
+  fd2d_status st = FD2D_OK;
+  cudaEventRecord(ctx->fork_events[0], main);
+  for (size_t j = 0; j < plans.size() && st == FD2D_OK; ++j) {
+    cudaStream_t sj = ctx->side_streams[j];
+    cudaStreamWaitEvent(sj, ctx->fork_events[0], 0);
+    ctx->stream = sj;
+    st = plans[j].loop();
+    ctx->stream = main;
+    cudaEventRecord(ctx->fork_events[j + 1], sj);
+    cudaStreamWaitEvent(main, ctx->fork_events[j + 1], 0);
+  }
+  ctx->stream = main;
+  return graph_end(ctx, name, sg.h, st);
+}
+
 fd2d_status stage_in(fd2d_ctx* ctx, const char* name, const void* src, size_t bytes, const void** dev) {
   if (!src || bytes == 0) {
     *dev = nullptr;
@@ -342,6 +391,8 @@ fd2d_status fd2d_ctx_destroy(fd2d_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   for (auto& kv : ctx->graphs) destroy_graph(kv.second);
   ctx->graphs.clear();
+  for (auto s : ctx->side_streams) cudaStreamDestroy(s);
+  for (auto e : ctx->fork_events) cudaEventDestroy(e);
   free_workspace(ctx);
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->d_err) cudaFree(ctx->d_err);
@@ -701,3 +752,148 @@ fd2d_status fd2d_noise_adjoint(fd2d_ctx* ctx, const fd2d_config* cfg, const doub
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Batches of reference stations (include/fd2d.h: fd2d_correlation_batch)
+// ---------------------------------------------------------------------------------
+namespace fd2d {
+namespace {
+
+struct BatchJob {
+  Geometry g;
+  SolveArgs green, corr;
+  size_t bytes = 0;
+  int nr = 0;
+};
+
+// Device bytes one FP32 job holds (fields, snapshot chunk, spectra, P and
+// injection planes, staged inputs); the FP64 form needs less.
+size_t job_footprint(const Geometry& g, int nr, int n_dist, bool host_inputs) {
+  const size_t P = (size_t)(g.nx + 31) / 32 * 32;
+  const size_t ps = (P * g.nz + 127) / 128 * 128;
+  const size_t np = (size_t)g.npts();
+  const size_t plane = ps * 4;
+  size_t n_dft = 0;
+  for (int n = 1; n <= g.nt; ++n) n_dft += ((n + g.nt - 1) % g.fs == 0);
+  const size_t T = std::min<size_t>({n_dft, 1024, ((size_t)2 << 30) / plane});
+  const size_t n_inj = g.ntc / g.fs;
+  const size_t chunk = std::min<size_t>(n_inj, ((size_t)4 << 30) / plane);
+  size_t b = 11 * plane + T * plane + 16 * np * g.K + 2 * (size_t)g.K * plane + chunk * plane;
+  b += (size_t)nr * (g.nt + g.ntc) * 8 + (size_t)1 << 20;
+  if (host_inputs) b += np * 8 * (2 + n_dist) + (size_t)nr * g.ntc * 8;
+  return b;
+}
+
+}  // namespace
+}  // namespace fd2d
+
+extern "C" fd2d_status fd2d_ctx_set_memory_budget(fd2d_ctx* ctx, int64_t bytes) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  if (bytes < 0) return set_error(ctx, FD2D_ERR_ARG, "negative memory budget");
+  ctx->mem_budget = bytes;
+  return FD2D_OK;
+}
+
+extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* jobs, int32_t n_jobs) {
+  FD2D_TRY(check_ctx(ctx));
+  if (n_jobs < 0 || (n_jobs > 0 && !jobs)) return set_error(ctx, FD2D_ERR_ARG, "bad job list");
+  std::vector<BatchJob> B(n_jobs);
+  for (int j = 0; j < n_jobs; ++j) {
+    const fd2d_job& J = jobs[j];
+    std::string err;
+    fd2d_status s = make_geometry(J.cfg, B[j].g, err);
+    if (s != FD2D_OK) return set_error(ctx, s, "job " + std::to_string(j) + ": " + err);
+    const Geometry& g = B[j].g;
+    if (!J.mu || !J.rho || !J.src || (J.nr > 0 && (!J.rec || !J.correlations)) || J.nr < 0)
+      return set_error(ctx, FD2D_ERR_ARG, "job " + std::to_string(j) + ": missing array");
+    if (!J.spectrum || J.n_noise_sources < 1 || (g.nb == 0 && J.n_noise_sources != 1))
+      return set_error(ctx, FD2D_ERR_SHAPE, "job " + std::to_string(j) + ": spectrum");
+    if (!J.source_dist || J.n_dist != (g.nb == 0 ? J.n_noise_sources : g.nb))
+      return set_error(ctx, FD2D_ERR_SHAPE, "job " + std::to_string(j) + ": source_dist planes");
+    B[j].nr = J.nr;
+    B[j].bytes = job_footprint(g, J.nr, J.n_dist, ctx->memspace == FD2D_MEM_HOST);
+  }
+  size_t budget = (size_t)ctx->mem_budget;
+  if (budget == 0) {
+    size_t free_b = 0, total_b = 0;
+    FD2D_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+    budget = free_b / 10 * 8;
+  }
+  int j0 = 0;
+  fd2d_status st = FD2D_OK;
+  while (j0 < n_jobs && st == FD2D_OK) {
+    int j1 = j0 + 1;
+    size_t used = B[j0].bytes;
+    while (j1 < n_jobs && used + B[j1].bytes <= budget) used += B[j1++].bytes;
+    // stage the group's inputs and outputs, each job under its own prefix
+    for (int j = j0; j < j1 && st == FD2D_OK; ++j) {
+      const fd2d_job& J = jobs[j];
+      BatchJob& b = B[j];
+      const Geometry& g = b.g;
+      const size_t np = (size_t)g.npts();
+      ctx->ws_prefix = "b" + std::to_string(j - j0) + ":";
+      std::vector<double> hp;
+      SolveArgs& ga = b.green;
+      SolveArgs& ca = b.corr;
+      const void* p;
+      void* q;
+      if ((st = host_points(ctx, J.src, 1, hp)) != FD2D_OK) break;
+      if ((st = point_indices(ctx, g, hp.data(), 1, "src", ga.src_idx)) != FD2D_OK) break;
+      if ((st = host_points(ctx, J.rec, J.nr, hp)) != FD2D_OK) break;
+      if ((st = point_indices(ctx, g, hp.data(), J.nr, "rec", ga.rec_idx)) != FD2D_OK) break;
+      ca.rec_idx = ga.rec_idx;
+      if ((st = stage_in(ctx, "in.mu", J.mu, np * 8, &p)) != FD2D_OK) break;
+      ga.mu = ca.mu = (const double*)p;
+      if ((st = stage_in(ctx, "in.rho", J.rho, np * 8, &p)) != FD2D_OK) break;
+      ga.rho = ca.rho = (const double*)p;
+      if ((st = stage_in(ctx, "in.spectrum", J.spectrum, (size_t)g.K * J.n_noise_sources * 8, &p)) != FD2D_OK) break;
+      ca.spectrum = (const double*)p;
+      ca.n_src = J.n_noise_sources;
+      if ((st = stage_in(ctx, "in.source_dist", J.source_dist, np * 8 * J.n_dist, &p)) != FD2D_OK) break;
+      ca.source_dist = (const double*)p;
+      ca.n_dist = J.n_dist;
+      if ((st = workspace(ctx, "batch.G_re", np * 8 * g.K, &q)) != FD2D_OK) break;
+      ga.G_re = (double*)q;
+      if ((st = workspace(ctx, "batch.G_im", np * 8 * g.K, &q)) != FD2D_OK) break;
+      ga.G_im = (double*)q;
+      ca.Gin_re = ga.G_re;
+      ca.Gin_im = ga.G_im;
+      ca.n_G = g.K;
+      if ((st = workspace(ctx, "batch.seis_green", (size_t)std::max(J.nr, 1) * g.nt * 8, &q)) != FD2D_OK) break;
+      ga.seis = (double*)q;
+      if ((st = out_buffer(ctx, "out.corr", J.correlations, (size_t)J.nr * g.ntc * 8, &q)) != FD2D_OK) break;
+      if (!q && (st = workspace(ctx, "batch.corr", 8, &q)) != FD2D_OK) break;
+      ca.seis = (double*)q;
+    }
+    if (st != FD2D_OK) break;
+    if (ctx->precision == FD2D_PREC_FP64) {
+      for (int j = j0; j < j1 && st == FD2D_OK; ++j) {
+        ctx->ws_prefix = "b" + std::to_string(j - j0) + ":";
+        st = fp64_forward1(ctx, B[j].g, B[j].green);
+        if (st == FD2D_OK) st = fp64_correlation(ctx, B[j].g, B[j].corr);
+      }
+    } else {
+      std::vector<LoopPlan> plans(j1 - j0);
+      for (int j = j0; j < j1 && st == FD2D_OK; ++j) {
+        ctx->ws_prefix = "b" + std::to_string(j - j0) + ":";
+        st = fp32_forward1_plan(ctx, B[j].g, B[j].green, plans[j - j0]);
+      }
+      ctx->ws_prefix.clear();
+      if (st == FD2D_OK) st = run_parallel(ctx, "batch_green", 0x1u, plans);
+      for (int j = j0; j < j1 && st == FD2D_OK; ++j) {
+        ctx->ws_prefix = "b" + std::to_string(j - j0) + ":";
+        st = fp32_correlation_plan(ctx, B[j].g, B[j].corr, plans[j - j0]);
+      }
+      ctx->ws_prefix.clear();
+      if (st == FD2D_OK) st = run_parallel(ctx, "batch_corr", 0x2u, plans);
+    }
+    for (int j = j0; j < j1 && st == FD2D_OK; ++j)
+      st = stage_out(ctx, jobs[j].correlations, B[j].corr.seis, (size_t)jobs[j].nr * B[j].g.ntc * 8);
+    if (st == FD2D_OK && j1 < n_jobs && ctx->memspace == FD2D_MEM_DEVICE)
+      st = FD2D_OK;  // device outputs are already in place
+    j0 = j1;
+  }
+  ctx->ws_prefix.clear();
+  if (st != FD2D_OK) return st;
+  return finish(ctx);
+}

@@ -10,6 +10,7 @@
 #include "common.cuh"
 
 #include <algorithm>
+#include <mutex>
 
 namespace fd2d {
 
@@ -71,8 +72,7 @@ static void stagger_weights(int r, double* c) {
   }
 }
 
-fd2d_status make_geometry(const fd2d_config* cfg, Geometry& g, std::string& err) {
-  if (!cfg) { err = "cfg is NULL"; return FD2D_ERR_ARG; }
+static fd2d_status build_geometry(const fd2d_config* cfg, Geometry& g, std::string& err) {
   if (cfg->nx < 2 || cfg->nz < 2 || cfg->nt < 1 || cfg->freq_samp < 1 || cfg->fw_nth < 1 ||
       !(cfg->dt > 0) || !(cfg->Lx > 0) || !(cfg->Lz > 0)) {
     err = "configuration needs nx, nz >= 2, nt, freq_samp, fw_nth >= 1 and dt, Lx, Lz > 0";
@@ -118,7 +118,7 @@ fd2d_status make_geometry(const fd2d_config* cfg, Geometry& g, std::string& err)
   // Cerjan taper, product over the enabled sides; exp(-(X-w)^2/(2w)^2) inside.
   const double wd = cfg->absorb_width;
   const double den = (2 * wd) * (2 * wd);
-  g.absbound.assign((size_t)g.nx * g.nz, 1.0);
+  auto ab = std::make_shared<std::vector<double>>((size_t)g.nx * g.nz, 1.0);
   for (int j = 0; j < g.nz; ++j) {
     const double Z = g.z[j];
     for (int i = 0; i < g.nx; ++i) {
@@ -140,11 +140,43 @@ fd2d_status make_geometry(const fd2d_config* cfg, Geometry& g, std::string& err)
         const double e = g.Lz - wd, d = Z - e;
         a *= (Z < e ? 1.0 : 0.0) + std::exp(-(d * d) / den) * (Z >= e ? 1.0 : 0.0);
       }
-      g.absbound[i + (size_t)g.nx * j] = a;
+      (*ab)[i + (size_t)g.nx * j] = a;
     }
   }
+  g.absbound = ab;
   stagger_weights(g.r, g.c);
   return FD2D_OK;
+}
+
+uint64_t config_hash(const fd2d_config* c) {
+  Sig s;
+  s.add(c->Lx); s.add(c->Lz); s.add(c->nx); s.add(c->nz); s.add(c->dt); s.add(c->nt); s.add(c->order);
+  s.add(c->n_basis_fct); s.add(c->fw_nth); s.add(c->n_sample); s.add(c->freq_samp); s.add(c->absorb_width);
+  s.add(c->absorb_left); s.add(c->absorb_right); s.add(c->absorb_top); s.add(c->absorb_bottom);
+  if (c->f_sample && c->n_sample > 0) s.bytes(c->f_sample, sizeof(double) * c->n_sample);
+  return s.h | 1;
+}
+
+// Geometries of recently used configurations (grid, taper, time axes).
+static std::mutex g_geo_mu;
+static std::vector<std::pair<uint64_t, Geometry>> g_geo_cache;
+
+fd2d_status make_geometry(const fd2d_config* cfg, Geometry& g, std::string& err) {
+  if (!cfg) { err = "cfg is NULL"; return FD2D_ERR_ARG; }
+  const uint64_t key = (cfg->f_sample || cfg->n_sample < 1) ? config_hash(cfg) : 0;
+  if (key) {
+    std::lock_guard<std::mutex> lk(g_geo_mu);
+    for (auto& kv : g_geo_cache)
+      if (kv.first == key) { g = kv.second; return FD2D_OK; }
+  }
+  fd2d_status s = build_geometry(cfg, g, err);
+  g.key = key;
+  if (s == FD2D_OK && key) {
+    std::lock_guard<std::mutex> lk(g_geo_mu);
+    if (g_geo_cache.size() >= 16) g_geo_cache.erase(g_geo_cache.begin());
+    g_geo_cache.emplace_back(key, g);
+  }
+  return s;
 }
 
 fd2d_status make_interpol_matrix(int K, int nb, std::vector<double>& M, std::string& err) {

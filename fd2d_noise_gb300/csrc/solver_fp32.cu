@@ -490,7 +490,8 @@ fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, bool 
   FD2D_TRY(workspace_t(ctx, "f32.taper", ps, &r.taper));
   FD2D_TRY(workspace_t(ctx, "f32.dtmu", ps, &r.dtmu));
   double* ab;
-  FD2D_TRY(upload(ctx, "f32.absbound64", g.absbound, &ab));
+  FD2D_TRY(upload_tagged<double>(ctx, "f32.absbound64", g.key, g.absbound->size(),
+                                  [&](std::vector<double>& h) { h = *g.absbound; }, &ab));
   dim3 pg((P + 31) / 32, (nz + 7) / 8);
   k32_prep<<<pg, r.pblock, 0, ctx->stream>>>(a.mu, a.rho, ab, g.dt, nx, nz, P, r.b, r.taper, r.dtmu);
   FD2D_TRY(after_launch(ctx, "k32_prep"));
@@ -529,18 +530,30 @@ fd2d_status interp_dev(fd2d_ctx* ctx, const Geometry& g, double** M) {
   std::string err;
   fd2d_status s = make_interpol_matrix(g.K, g.nb, h, err);
   if (s != FD2D_OK) return set_error(ctx, s, err);
-  return upload(ctx, "f32.interp", h, M);
+  return upload_tagged<double>(ctx, "f32.interp", g.key, h.size(), [&](std::vector<double>& o) { o = h; }, M);
+}
+
+// e[k] = sum_s spectrum(k, s), summed in source order.
+__global__ void k32_spectrum_eff(const double* spec, int K, int n_src, double* e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  double acc = 0.0;
+  for (int s = 0; s < n_src; ++s) acc += spec[k + (int64_t)K * s];
+  e[k] = acc;
 }
 
 // Effective spectrum: sum over noise sources (they share one distribution).
 fd2d_status spectrum_eff(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, double** out) {
-  std::vector<double> h((size_t)g.K * std::max(a.n_src, 1));
-  FD2D_CUDA(ctx, cudaMemcpyAsync(h.data(), a.spectrum, h.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
-  FD2D_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  std::vector<double> e(g.K, 0.0);
-  for (int s = 0; s < a.n_src; ++s)
-    for (int k = 0; k < g.K; ++k) e[k] += h[k + (size_t)g.K * s];
-  return upload(ctx, "f32.spec_eff", e, out);
+  FD2D_TRY(workspace_t(ctx, "f32.spec_eff", (size_t)g.K, out));
+  k32_spectrum_eff<<<(g.K + 127) / 128, 128, 0, ctx->stream>>>(a.spectrum, g.K, a.n_src, *out);
+  return after_launch(ctx, "k32_spectrum_eff");
+}
+
+// Tag of a coefficient table: configuration, table kind and the rows it holds.
+uint64_t table_tag(const Geometry& g, int kind, const std::vector<int>& rows) {
+  Sig s;
+  s.add(g.key); s.add(kind); s.add_vec(rows);
+  return g.key ? (s.h | 1) : 0;
 }
 
 // Injection planes for the listed coefficient rows (ifft rows, one per event).
@@ -566,17 +579,19 @@ fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, Run& r, const doub
                                                r.ps, inj.P);
   FD2D_TRY(after_launch(ctx, "k32_make_P"));
   // B[k][j] = Re c(row_j, k); B[K+k][j] = -Im c(row_j, k)   (c = ifft_coeff, dw)
-  std::vector<float> B((size_t)2 * K * inj.n_events);
-  for (int j = 0; j < inj.n_events; ++j) {
-    const int n = (inj.row_of_event[j] + 1) * g.fs;  // step whose time this row holds
-    for (int k = 0; k < K; ++k) {
-      double re, im;
-      dft_coeff(g.w[k] * g.t_corr[n - 1], g.dw, re, im);
-      B[(size_t)k * inj.n_events + j] = (float)re;
-      B[(size_t)(K + k) * inj.n_events + j] = (float)(-im);
+  auto fill = [&](std::vector<float>& B) {
+    for (int j = 0; j < inj.n_events; ++j) {
+      const int n = (inj.row_of_event[j] + 1) * g.fs;  // step whose time this row holds
+      for (int k = 0; k < K; ++k) {
+        double re, im;
+        dft_coeff(g.w[k] * g.t_corr[n - 1], g.dw, re, im);
+        B[(size_t)k * inj.n_events + j] = (float)re;
+        B[(size_t)(K + k) * inj.n_events + j] = (float)(-im);
+      }
     }
-  }
-  FD2D_TRY(upload(ctx, "f32.injB", B, &inj.B));
+  };
+  FD2D_TRY(upload_tagged<float>(ctx, "f32.injB", table_tag(g, 2, inj.row_of_event),
+                                (size_t)2 * K * inj.n_events, fill, &inj.B));
   const size_t cap = (size_t)4 << 30;  // resident injection planes <= 4 GiB
   inj.chunk = (int)std::max<int64_t>(1, std::min<int64_t>(inj.n_events, (int64_t)(cap / (r.ps * 4))));
   FD2D_TRY(workspace_t(ctx, "f32.inj", (size_t)r.ps * inj.chunk, &inj.planes));
@@ -631,11 +646,13 @@ fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
   return FD2D_OK;
 }
 
-// rows[e] = (re, im) coefficient pairs for event e, laid out [e][2K] as float.
-fd2d_status dft_add_target(fd2d_ctx* ctx, const char* name, const std::vector<float>& rows, double* re,
+// rows[e] = (re, im) coefficient pairs for event e, laid out [e][2K] as float;
+// `fill` generates them when the buffer does not already hold table `tag`.
+template <typename F>
+fd2d_status dft_add_target(fd2d_ctx* ctx, const char* name, uint64_t tag, size_t count, F&& fill, double* re,
                            double* im, Dft& d) {
   Dft::Target t;
-  FD2D_TRY(upload(ctx, name, rows, &t.B));
+  FD2D_TRY(upload_tagged<float>(ctx, name, tag, count, fill, &t.B));
   t.re = re;
   t.im = im;
   d.targets.push_back(t);
@@ -716,7 +733,10 @@ fd2d_status f32_copy_pitched(fd2d_ctx* ctx, const Run& r, const double* a, doubl
 }  // namespace
 
 // ---------------------------------------------------------------------------------
-fd2d_status fp32_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
+// forward1 / correlation are split into an eager prepare step (buffers, uploads,
+// P planes) and a capturable time loop, so that a batch can run the loops of
+// many solves as parallel branches of one CUDA graph.
+fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, LoopPlan& plan) {
   Run r;
   FD2D_TRY(init_run(ctx, g, a, false, r));
   const int nt = g.nt, K = g.K;
@@ -730,25 +750,32 @@ fd2d_status fp32_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) 
   Dft d;
   FD2D_TRY(dft_init(ctx, r, (int)ev.size(), d));
   if (!ev.empty()) {
-    std::vector<float> rows((size_t)ev.size() * 2 * K);
-    for (size_t e = 0; e < ev.size(); ++e)
-      for (int k = 0; k < K; ++k) {
-        double re, im;
-        dft_coeff(-(g.w[k] * g.t_fwd[ev[e] - 1]), g.dt, re, im);
-        rows[e * 2 * K + k] = (float)re;
-        rows[e * 2 * K + K + k] = (float)(-im);
-      }
-    FD2D_TRY(dft_add_target(ctx, "f32.dftB0", rows, a.G_re, a.G_im, d));
+    auto fill = [&](std::vector<float>& rows) {
+      for (size_t e = 0; e < ev.size(); ++e)
+        for (int k = 0; k < K; ++k) {
+          double re, im;
+          dft_coeff(-(g.w[k] * g.t_fwd[ev[e] - 1]), g.dt, re, im);
+          rows[e * 2 * K + k] = (float)re;
+          rows[e * 2 * K + K + k] = (float)(-im);
+        }
+    };
+    FD2D_TRY(dft_add_target(ctx, "f32.dftB0", table_tag(g, 0, ev), ev.size() * 2 * K, fill, a.G_re, a.G_im, d));
+  } else {
+    // no DFT step: the spectra are zero (otherwise the first flush overwrites them)
+    FD2D_CUDA(ctx, cudaMemsetAsync(a.G_re, 0, (size_t)np * K * 8, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(a.G_im, 0, (size_t)np * K * 8, ctx->stream));
   }
-  FD2D_CUDA(ctx, cudaMemsetAsync(a.G_re, 0, (size_t)np * K * 8, ctx->stream));
-  FD2D_CUDA(ctx, cudaMemsetAsync(a.G_im, 0, (size_t)np * K * 8, ctx->stream));
   float* dtdmu = nullptr;
   const bool born = a.dmu != nullptr;
   if (born) FD2D_TRY(f32_copy_pitched(ctx, r, a.dmu, g.dt, "f32.dtdmu", &dtdmu));
-  const int nr = (int)a.rec_idx.size();
   Sig sg;
   sig_run(sg, r); sig_args(sg, g, a); sig_dft(sg, d); sg.add(dtdmu);
-  return run_captured(ctx, "fp32_forward1", sg.h, [&]() -> fd2d_status {
+  plan.name = "fp32_forward1";
+  plan.key = sg.h;
+  plan.loop = [ctx, g, a, r, d, dtdmu, born]() -> fd2d_status {
+    Dft dd = d;  // the loop's own chunk bookkeeping
+    const int nt = g.nt, nr = (int)a.rec_idx.size();
+    const int64_t np = r.np;
     int i_fw_out = 0, i_fw_in = 0, par = 0;
     const int tl = timer_begin(ctx, ctx->stream);  // whole loop; contractions are timed inside it
     for (int n = 1; n <= nt; ++n) {
@@ -764,24 +791,24 @@ fd2d_status fp32_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) 
         s.amp_const = 1.0e9f;  // stf = 1.0e9*ones(1,nt), code/run_forward1_green.m:64
       }
       const bool is_dft = (n + nt - 1) % g.fs == 0;
-      if (is_dft) s.snap_dft = dft_slot(r, d);
+      if (is_dft) s.snap_dft = dft_slot(r, dd);
       s.rec_xy = r.rec_xy;
       s.nrec = nr;
       s.seis_col = a.seis + (size_t)nr * (n - 1);
       FD2D_TRY(launch_step(ctx, r, par, s));
-      if (is_dft) FD2D_TRY(dft_push(ctx, r, g, d));
+      if (is_dft) FD2D_TRY(dft_push(ctx, r, g, dd));
       par ^= 1;
     }
     timer_end(ctx, ctx->stream, tl, FD2D_TIMER_STEP_V, np * nt, nt);
     return FD2D_OK;
-  });
+  };
+  return FD2D_OK;
 }
 
-fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
+fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, LoopPlan& plan) {
   Run r;
   FD2D_TRY(init_run(ctx, g, a, true, r));
   const int ntc = g.ntc;
-  const int64_t np = r.np;
   double *M, *spec;
   FD2D_TRY(interp_dev(ctx, g, &M));
   FD2D_TRY(spectrum_eff(ctx, g, a, &spec));
@@ -795,10 +822,14 @@ fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& 
   float* dmu32 = nullptr;
   const bool born = a.dmu != nullptr;
   if (born) FD2D_TRY(f32_copy_pitched(ctx, r, a.dmu, 1.0, "f32.dmu", &dmu32));
-  const int nr = (int)a.rec_idx.size();
   Sig sg;
   sig_run(sg, r); sig_args(sg, g, a); sig_inj(sg, inj); sg.add(dmu32);
-  return run_captured(ctx, "fp32_correlation", sg.h, [&]() -> fd2d_status {
+  plan.name = "fp32_correlation";
+  plan.key = sg.h;
+  plan.loop = [ctx, g, a, r, inj, dmu32, born]() -> fd2d_status {
+    Injection ij = inj;  // the loop's own chunk bookkeeping
+    const int ntc = g.ntc, nr = (int)a.rec_idx.size();
+    const int64_t np = r.np;
     int i_fw_out = 0, par = 0, ev = 0;
     const int tl = timer_begin(ctx, ctx->stream);
     for (int n = 1; n <= ntc; ++n) {
@@ -809,7 +840,7 @@ fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& 
         s.snap_pre = a.C_out + (size_t)np * (i_fw_out++);
         s.snap_pre_u = 1;
       }
-      if (n % g.fs == 0) FD2D_TRY(injection_plane(ctx, r, g, inj, ev++, &s.inj_plane));
+      if (n % g.fs == 0) FD2D_TRY(injection_plane(ctx, r, g, ij, ev++, &s.inj_plane));
       s.rec_xy = r.rec_xy;
       s.nrec = nr;
       s.seis_col = a.seis + (size_t)nr * (n - 1);
@@ -824,7 +855,20 @@ fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& 
     }
     timer_end(ctx, ctx->stream, tl, FD2D_TIMER_STEP_VU, np * ntc, ntc);
     return FD2D_OK;
-  });
+  };
+  return FD2D_OK;
+}
+
+fd2d_status fp32_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
+  LoopPlan p;
+  FD2D_TRY(fp32_forward1_plan(ctx, g, a, p));
+  return run_captured(ctx, p.name.c_str(), p.key, p.loop);
+}
+
+fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
+  LoopPlan p;
+  FD2D_TRY(fp32_correlation_plan(ctx, g, a, p));
+  return run_captured(ctx, p.name.c_str(), p.key, p.loop);
 }
 
 fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
@@ -887,23 +931,25 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
   FD2D_TRY(dft_init(ctx, r, (int)ev.size(), d));
   double *Ure = nullptr, *Uim = nullptr;
   auto rows_for = [&](const std::vector<int>& rows_of_event) {
-    std::vector<float> rows(ev.size() * 2 * K);
-    for (size_t e = 0; e < ev.size(); ++e) {
-      const int n = (rows_of_event[e] + 1) * g.fs;
-      for (int k = 0; k < K; ++k) {
-        double re, im;
-        dft_coeff(-(g.w[k] * g.t_corr[n - 1]), g.dt, re, im);
-        rows[e * 2 * K + k] = (float)re;
-        rows[e * 2 * K + K + k] = (float)im;
+    return [&g, &ev, &rows_of_event, K](std::vector<float>& rows) {
+      for (size_t e = 0; e < ev.size(); ++e) {
+        const int n = (rows_of_event[e] + 1) * g.fs;
+        for (int k = 0; k < K; ++k) {
+          double re, im;
+          dft_coeff(-(g.w[k] * g.t_corr[n - 1]), g.dt, re, im);
+          rows[e * 2 * K + k] = (float)re;
+          rows[e * 2 * K + K + k] = (float)im;
+        }
       }
-    }
-    return rows;
+    };
   };
+  const size_t nrows = ev.size() * 2 * K;
   if (!ev.empty()) {
     std::vector<int> nat(ev.size());
     for (size_t e = 0; e < ev.size(); ++e) nat[e] = ev[e] / g.fs - 1;
     if (dft_u) {
-      FD2D_TRY(dft_add_target(ctx, "f32.dftB0", rows_for(dft_row), a.sf_re, a.sf_im, d));
+      FD2D_TRY(dft_add_target(ctx, "f32.dftB0", table_tag(g, 1, dft_row), nrows, rows_for(dft_row), a.sf_re,
+                              a.sf_im, d));
       if (natural) { Ure = a.sf_re; Uim = a.sf_im; }
     }
     if (Gvalid && !Ure) {
@@ -911,7 +957,7 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
       FD2D_TRY(workspace_t(ctx, "f32.Uim", (size_t)np * K, &Uim));
       FD2D_CUDA(ctx, cudaMemsetAsync(Ure, 0, (size_t)np * K * 8, ctx->stream));
       FD2D_CUDA(ctx, cudaMemsetAsync(Uim, 0, (size_t)np * K * 8, ctx->stream));
-      FD2D_TRY(dft_add_target(ctx, "f32.dftB1", rows_for(nat), Ure, Uim, d));
+      FD2D_TRY(dft_add_target(ctx, "f32.dftB1", table_tag(g, 1, nat), nrows, rows_for(nat), Ure, Uim, d));
     }
   }
   float* dmu32 = nullptr;
@@ -1089,7 +1135,7 @@ extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg,
   // host-side inputs: taper (pitched FP32), source / receiver nodes
   std::vector<float> taper((size_t)ps, 0.f);
   for (int j = 0; j < nz; ++j)
-    for (int i = 0; i < nx; ++i) taper[i + (size_t)P * j] = (float)g.absbound[i + (size_t)nx * j];
+    for (int i = 0; i < nx; ++i) taper[i + (size_t)P * j] = (float)(*g.absbound)[i + (size_t)nx * j];
   std::vector<int2> xy;
   for (int k = 0; k < ns; ++k) xy.push_back(make_int2(nearest_node(g.x, src[k]), nearest_node(g.z, src[ns + k])));
   for (int k = 0; k < nr; ++k) xy.push_back(make_int2(nearest_node(g.x, rec[k]), nearest_node(g.z, rec[nr + k])));

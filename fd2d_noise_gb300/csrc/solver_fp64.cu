@@ -312,7 +312,7 @@ fd2d_status init_base(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, bool
   FD2D_TRY(after_launch(ctx, "k64_inv"));
   P.inv_rho = inv_rho;
   double* ab;
-  FD2D_TRY(upload(ctx, "f64.absbound", g.absbound, &ab));
+  FD2D_TRY(upload(ctx, "f64.absbound", *g.absbound, &ab));
   P.absbound = ab;
   P.mu = a.mu;
   P.dmu = a.dmu;

@@ -94,6 +94,22 @@ class DeviceSession:
             _p(dmu), _p(u_in), int(n_u_in), _p(K), _p(sf_re), _p(sf_im), _p(u_out), _p(seis))
         _lib.check(st, self.ctx.h)
 
+    def correlation_batch(self, jobs):
+        """Runs fd2d_correlation_batch.  ``jobs``: list of dicts with keys cfg (Config),
+        mu, rho, spectrum, n_src, source_dist, n_dist, src, rec, nr, out (tensors)."""
+        arr = (_lib.FD2DJob * len(jobs))()
+        keep = []
+        for j, d in enumerate(jobs):
+            c = d["cfg"].to_c()
+            keep.append(c)
+            arr[j].cfg = ctypes.pointer(c)
+            arr[j].mu, arr[j].rho = d["mu"].data_ptr(), d["rho"].data_ptr()
+            arr[j].spectrum, arr[j].n_noise_sources = d["spectrum"].data_ptr(), int(d.get("n_src", 1))
+            arr[j].source_dist, arr[j].n_dist = d["source_dist"].data_ptr(), int(d.get("n_dist", 1))
+            arr[j].src, arr[j].rec, arr[j].nr = d["src"].data_ptr(), d["rec"].data_ptr(), int(d["nr"])
+            arr[j].correlations = d["out"].data_ptr()
+        _lib.check(self.ctx.L.fd2d_correlation_batch(self.ctx.h, arr, len(jobs)), self.ctx.h)
+
     def kernel_planes(self) -> int:
         return n_kernel_planes(self.cfg)
 

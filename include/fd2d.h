@@ -218,6 +218,33 @@ fd2d_status fd2d_noise_adjoint(fd2d_ctx* ctx, const fd2d_config* cfg,
                                float* u_out,
                                double* seismograms);
 
+/* ---- batches -------------------------------------------------------------------
+ * One job is one reference station of the parfor loop of
+ * code/calculate_data.m:189-202: the Green function (run_forward1_green,
+ * mode 0) followed by the correlation wavefield (run_forward2_correlation,
+ * mode 0); the job returns the correlations.  Jobs may have different
+ * configurations (grid sizes, nt) and models.  Arrays follow the context's
+ * memspace.  In FP32 the jobs advance concurrently -- their time loops are
+ * parallel branches of one CUDA graph -- in groups whose device buffers fit in
+ * the memory budget (default: 80 % of the free device memory at the call).
+ * In FP64 (the plain form) the jobs run one after another. */
+typedef struct fd2d_job {
+  const fd2d_config* cfg;
+  const double* mu;
+  const double* rho;
+  const double* spectrum;     /* n_sample-by-n_noise_sources */
+  int32_t n_noise_sources;
+  const double* source_dist;  /* nx*nz*n_dist */
+  int32_t n_dist;
+  const double* src;          /* 1-by-2 reference station [m] */
+  const double* rec;          /* nr-by-2 receivers [m] */
+  int32_t nr;
+  double* correlations;       /* out: nr*(2*nt-1) */
+} fd2d_job;
+fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* jobs, int32_t n_jobs);
+/* Device-memory budget of a batch in bytes (0 = 80 % of the free memory). */
+fd2d_status fd2d_ctx_set_memory_budget(fd2d_ctx* ctx, int64_t bytes);
+
 /* ---- building block ----------------------------------------------------------
  * R[n*ldr + m] = sum_{k<Kd} A[k*lda + m] * B[k*ldb + n]  for m < M, n < N:
  * the split-TF32 tensor-core contraction behind the on-the-fly DFT

@@ -1,0 +1,63 @@
+"""Batched reference stations (fd2d_correlation_batch) against single solves.
+
+Each job is one station of code/calculate_data.m:189-202 (Green function, then
+correlation).  The batch runs the jobs' time loops concurrently; its
+correlations must equal those of the one-at-a-time entry points, for jobs of
+different grid sizes and lengths, in both precisions and memory-budget
+groupings.
+"""
+import numpy as np
+import pytest
+
+from tests.problems import media, noise_source, rel_l2, small_cfg, stations
+
+pytestmark = pytest.mark.gpu
+
+
+def _jobs():
+    out = []
+    for seed, kw in enumerate([dict(nx=40, nz=36, nt=60, order=4), dict(nx=52, nz=44, nt=48, order=8),
+                               dict(nx=40, nz=36, nt=60, order=4)]):
+        cfg = small_cfg(K=20, fs=5, fw=1, **kw)
+        mu, rho = media(cfg, seed=seed)
+        spec, sd = noise_source(cfg, seed=seed)
+        src = stations(cfg, 1, seed=10 + seed)
+        rec = stations(cfg, 5, seed=20 + seed)
+        out.append(dict(cfg=cfg, mu=mu, rho=rho, spec=spec, sd=sd, src=src, rec=rec))
+    return out
+
+
+def _single(job, prec):
+    from fd2d_noise_gb300 import solvers
+    G, _, _ = solvers.run_forward1_green(job["mu"], job["rho"], job["src"], job["rec"], 0, cfg=job["cfg"],
+                                         precision=prec)
+    c, _ = solvers.run_forward2_correlation(job["mu"], job["rho"], G, job["spec"], job["sd"], job["rec"], 0,
+                                            cfg=job["cfg"], precision=prec)
+    return c
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("budget", [0, 1])
+def test_batch_matches_single_solves(fd2d_lib, prec, budget):
+    import torch
+    from fd2d_noise_gb300 import _lib
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+    jobs = _jobs()
+    sess = DeviceSession(jobs[0]["cfg"], 0, prec)
+    if budget:
+        _lib.check(sess.ctx.L.fd2d_ctx_set_memory_budget(sess.ctx.h, 1), sess.ctx.h)  # one job per group
+    dj = []
+    for j in jobs:
+        c = j["cfg"]
+        dj.append(dict(cfg=c, mu=to_device(j["mu"], np.float64), rho=to_device(j["rho"], np.float64),
+                       spectrum=to_device(j["spec"], np.float64), source_dist=to_device(j["sd"], np.float64),
+                       src=to_device(j["src"], np.float64), rec=to_device(j["rec"], np.float64),
+                       nr=j["rec"].shape[0],
+                       out=torch.zeros(j["rec"].shape[0] * c.ntc, dtype=torch.float64, device="cuda")))
+    for rep in range(2):  # the second call replays the cached graphs
+        sess.correlation_batch(dj)
+        sess.ctx.synchronize()
+        for j, d in zip(jobs, dj):
+            got = d["out"].cpu().numpy().reshape(j["rec"].shape[0], j["cfg"].ntc, order="F")
+            ref = _single(j, prec)
+            assert rel_l2(got, ref) < (1e-12 if prec == "fp64" else 1e-6), rep
