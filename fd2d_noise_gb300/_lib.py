@@ -32,7 +32,10 @@ EXPORTED = [
     "fd2d_forward1_green", "fd2d_forward2_correlation", "fd2d_noise_adjoint",
     "fd2d_ctx_set_timing", "fd2d_ctx_timing", "fd2d_contract_f32",
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
+    "fd2d_make_adjoint_sources",
 ]
+MEAS_WAVEFORM_DIFFERENCE = 0
+MEAS_LOG_AMPLITUDE_RATIO = 1
 
 
 class FD2DJob(ctypes.Structure):

@@ -138,6 +138,11 @@ void timer_end(fd2d_ctx* ctx, cudaStream_t stream, int begin, int cls, int64_t u
 
 // Checks the last launch and counts it.
 fd2d_status after_launch(fd2d_ctx* ctx, const char* what);
+// Start of an entry point: ctx non-NULL, its device current, last error cleared.
+fd2d_status check_ctx(fd2d_ctx* ctx);
+// End of an entry point: host memspace waits for the stream and reports a
+// device-side wait that gave up.
+fd2d_status finish_call(fd2d_ctx* ctx);
 
 // Signature of everything a captured time loop depends on (FNV-1a).
 struct Sig {
@@ -255,8 +260,10 @@ struct LoopPlan {
 fd2d_status run_parallel(fd2d_ctx* ctx, const char* name, uint64_t key, std::vector<LoopPlan>& plans);
 
 // Precision-specific drivers (solver_fp64.cu / solver_fp32.cu).
-fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, LoopPlan& plan);
-fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, LoopPlan& plan);
+// Plans of S lanes a[0..S-1] advanced by one launch per step (S > 1: mode 0, no
+// Born term, spectra and seismograms of lane l at constant strides from lane 0's).
+fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S, LoopPlan& plan);
+fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S, LoopPlan& plan);
 fd2d_status fp64_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
 fd2d_status fp64_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
 fd2d_status fp64_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);

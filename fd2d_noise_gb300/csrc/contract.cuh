@@ -35,6 +35,10 @@ struct ContractArgs {
   // and the FP64 planes are MATLAB-layout nx-by-nz: m -> i + remap_nx*j, and
   // points outside the grid are dropped.
   int remap_pitch = 0, remap_nx = 0, remap_nz = 0;
+  // Lanes: when lane_m > 0 the points are lane_m-long runs of independent
+  // solves, m = l*lane_m + (pitched point), and lane l's FP64 planes start
+  // l*acc_lane elements after acc0 / acc1.
+  int64_t lane_m = 0, acc_lane = 0;
   // FP32 store: out32[n*ldo + m]
   float* out32 = nullptr;
   int64_t ldo = 0;

@@ -216,9 +216,15 @@ __global__ __launch_bounds__(NTHREADS, 1) void k_contract_tc(ContractArgs a, int
     int64_t q = m;
     bool valid = ok && m < a.M;
     if (valid && a.remap_pitch) {
-      const int ii = m % a.remap_pitch, jj = m / a.remap_pitch;
+      int64_t mm = m, lane_off = 0;
+      if (a.lane_m) {
+        const int64_t l = mm / a.lane_m;
+        mm -= l * a.lane_m;
+        lane_off = l * a.acc_lane;
+      }
+      const int ii = (int)(mm % a.remap_pitch), jj = (int)(mm / a.remap_pitch);
       valid = ii < a.remap_nx && jj < a.remap_nz;
-      q = ii + (int64_t)a.remap_nx * jj;
+      q = lane_off + ii + (int64_t)a.remap_nx * jj;
     }
     for (int c0 = 0; c0 < bn; c0 += 32) {
       float v[32];

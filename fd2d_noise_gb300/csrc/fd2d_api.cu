@@ -299,7 +299,7 @@ fd2d_status stage_out(fd2d_ctx* ctx, void* user, const void* dev, size_t bytes) 
   return FD2D_OK;
 }
 
-static fd2d_status finish(fd2d_ctx* ctx) {
+fd2d_status finish_call(fd2d_ctx* ctx) {
   if (ctx->memspace == FD2D_MEM_HOST) FD2D_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   int herr = 0;
   if (ctx->memspace == FD2D_MEM_HOST && ctx->d_err) {
@@ -338,7 +338,7 @@ static fd2d_status host_points(fd2d_ctx* ctx, const double* p, int n, std::vecto
   return FD2D_OK;
 }
 
-static fd2d_status check_ctx(fd2d_ctx* ctx) {
+fd2d_status check_ctx(fd2d_ctx* ctx) {
   if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return set_error(ctx, FD2D_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
@@ -562,7 +562,7 @@ fd2d_status fd2d_forward1_green(fd2d_ctx* ctx, const fd2d_config* cfg, const dou
   FD2D_TRY(stage_out(ctx, G_fft_im, a.G_im, np * 8 * g.K));
   if (a.G_out) FD2D_TRY(stage_out(ctx, G_out, a.G_out, np * 4 * nfw));
   FD2D_TRY(stage_out(ctx, seismograms, a.seis, (size_t)nr * g.nt * 8));
-  return finish(ctx);
+  return finish_call(ctx);
 }
 
 fd2d_status fd2d_forward2_correlation(fd2d_ctx* ctx, const fd2d_config* cfg, const double* mu,
@@ -626,7 +626,7 @@ fd2d_status fd2d_forward2_correlation(fd2d_ctx* ctx, const fd2d_config* cfg, con
   if (s != FD2D_OK) return s;
   if (a.C_out) FD2D_TRY(stage_out(ctx, C_out, a.C_out, np * 4 * nfw));
   FD2D_TRY(stage_out(ctx, seismograms, a.seis, (size_t)nr * g.ntc * 8));
-  return finish(ctx);
+  return finish_call(ctx);
 }
 
 fd2d_status fd2d_noise_adjoint(fd2d_ctx* ctx, const fd2d_config* cfg, const double* mu,
@@ -748,7 +748,7 @@ fd2d_status fd2d_noise_adjoint(fd2d_ctx* ctx, const fd2d_config* cfg, const doub
   FD2D_TRY(stage_out(ctx, stf_fft_im, a.sf_im, np * 8 * g.K));
   if (a.C_out) FD2D_TRY(stage_out(ctx, u_out, a.C_out, np * 4 * nfw));
   FD2D_TRY(stage_out(ctx, seismograms, a.seis, (size_t)nr * g.ntc * 8));
-  return finish(ctx);
+  return finish_call(ctx);
 }
 
 }  // extern "C"
@@ -764,6 +764,8 @@ struct BatchJob {
   SolveArgs green, corr;
   size_t bytes = 0;
   int nr = 0;
+  int lane_group = -1, lane = 0;  // jobs of one geometry and receiver count share launches
+  double* corr_lane = nullptr;    // the lane's correlations inside the group buffer
 };
 
 // Device bytes one FP32 job holds (fields, snapshot chunk, spectra, P and
@@ -825,6 +827,42 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
     int j1 = j0 + 1;
     size_t used = B[j0].bytes;
     while (j1 < n_jobs && used + B[j1].bytes <= budget) used += B[j1++].bytes;
+    // lane groups: jobs of one geometry (configuration) and receiver count
+    // advance together, one launch per time step for the whole group
+    std::vector<std::vector<int>> lanes;
+    if (ctx->precision == FD2D_PREC_FP32) {
+      for (int j = j0; j < j1; ++j) {
+        int gi = -1;
+        for (size_t q = 0; q < lanes.size() && gi < 0; ++q) {
+          const BatchJob& h = B[lanes[q][0]];
+          if (h.g.key && h.g.key == B[j].g.key && h.nr == B[j].nr) gi = (int)q;
+        }
+        if (gi < 0) {
+          gi = (int)lanes.size();
+          lanes.emplace_back();
+        }
+        B[j].lane_group = gi;
+        B[j].lane = (int)lanes[gi].size();
+        lanes[gi].push_back(j);
+      }
+    }
+    // group buffers: spectra, Green seismograms and correlations of all lanes,
+    // lane after lane
+    std::vector<double*> grp_gre(lanes.size()), grp_gim(lanes.size()), grp_sg(lanes.size()), grp_c(lanes.size());
+    for (size_t q = 0; q < lanes.size() && st == FD2D_OK; ++q) {
+      const Geometry& g = B[lanes[q][0]].g;
+      const size_t S = lanes[q].size(), np = (size_t)g.npts(), nr = (size_t)std::max(B[lanes[q][0]].nr, 1);
+      ctx->ws_prefix = "L" + std::to_string(q) + ":";
+      void* w;
+      if ((st = workspace(ctx, "batch.G_re", S * np * 8 * g.K, &w)) != FD2D_OK) break;
+      grp_gre[q] = (double*)w;
+      if ((st = workspace(ctx, "batch.G_im", S * np * 8 * g.K, &w)) != FD2D_OK) break;
+      grp_gim[q] = (double*)w;
+      if ((st = workspace(ctx, "batch.seis_green", S * nr * g.nt * 8, &w)) != FD2D_OK) break;
+      grp_sg[q] = (double*)w;
+      if ((st = workspace(ctx, "batch.corr", S * nr * g.ntc * 8, &w)) != FD2D_OK) break;
+      grp_c[q] = (double*)w;
+    }
     // stage the group's inputs and outputs, each job under its own prefix
     for (int j = j0; j < j1 && st == FD2D_OK; ++j) {
       const fd2d_job& J = jobs[j];
@@ -852,18 +890,27 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
       if ((st = stage_in(ctx, "in.source_dist", J.source_dist, np * 8 * J.n_dist, &p)) != FD2D_OK) break;
       ca.source_dist = (const double*)p;
       ca.n_dist = J.n_dist;
-      if ((st = workspace(ctx, "batch.G_re", np * 8 * g.K, &q)) != FD2D_OK) break;
-      ga.G_re = (double*)q;
-      if ((st = workspace(ctx, "batch.G_im", np * 8 * g.K, &q)) != FD2D_OK) break;
-      ga.G_im = (double*)q;
+      ca.n_G = g.K;
+      if (b.lane_group >= 0) {
+        const int q = b.lane_group;
+        const size_t nr = (size_t)std::max(J.nr, 1);
+        ga.G_re = grp_gre[q] + (size_t)b.lane * np * g.K;
+        ga.G_im = grp_gim[q] + (size_t)b.lane * np * g.K;
+        ga.seis = grp_sg[q] + (size_t)b.lane * nr * g.nt;
+        ca.seis = b.corr_lane = grp_c[q] + (size_t)b.lane * nr * g.ntc;
+      } else {
+        if ((st = workspace(ctx, "batch.G_re", np * 8 * g.K, &q)) != FD2D_OK) break;
+        ga.G_re = (double*)q;
+        if ((st = workspace(ctx, "batch.G_im", np * 8 * g.K, &q)) != FD2D_OK) break;
+        ga.G_im = (double*)q;
+        if ((st = workspace(ctx, "batch.seis_green", (size_t)std::max(J.nr, 1) * g.nt * 8, &q)) != FD2D_OK) break;
+        ga.seis = (double*)q;
+        if ((st = out_buffer(ctx, "out.corr", J.correlations, (size_t)J.nr * g.ntc * 8, &q)) != FD2D_OK) break;
+        if (!q && (st = workspace(ctx, "batch.corr", 8, &q)) != FD2D_OK) break;
+        ca.seis = (double*)q;
+      }
       ca.Gin_re = ga.G_re;
       ca.Gin_im = ga.G_im;
-      ca.n_G = g.K;
-      if ((st = workspace(ctx, "batch.seis_green", (size_t)std::max(J.nr, 1) * g.nt * 8, &q)) != FD2D_OK) break;
-      ga.seis = (double*)q;
-      if ((st = out_buffer(ctx, "out.corr", J.correlations, (size_t)J.nr * g.ntc * 8, &q)) != FD2D_OK) break;
-      if (!q && (st = workspace(ctx, "batch.corr", 8, &q)) != FD2D_OK) break;
-      ca.seis = (double*)q;
     }
     if (st != FD2D_OK) break;
     if (ctx->precision == FD2D_PREC_FP64) {
@@ -873,27 +920,44 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
         if (st == FD2D_OK) st = fp64_correlation(ctx, B[j].g, B[j].corr);
       }
     } else {
-      std::vector<LoopPlan> plans(j1 - j0);
-      for (int j = j0; j < j1 && st == FD2D_OK; ++j) {
-        ctx->ws_prefix = "b" + std::to_string(j - j0) + ":";
-        st = fp32_forward1_plan(ctx, B[j].g, B[j].green, plans[j - j0]);
+      // one plan per lane group; the groups' loops run as parallel graph branches
+      std::vector<LoopPlan> plans(lanes.size());
+      std::vector<SolveArgs> la;
+      for (size_t q = 0; q < lanes.size() && st == FD2D_OK; ++q) {
+        ctx->ws_prefix = "L" + std::to_string(q) + ":";
+        la.clear();
+        for (int j : lanes[q]) la.push_back(B[j].green);
+        st = fp32_forward1_plan(ctx, B[lanes[q][0]].g, la.data(), (int)la.size(), plans[q]);
       }
       ctx->ws_prefix.clear();
       if (st == FD2D_OK) st = run_parallel(ctx, "batch_green", 0x1u, plans);
-      for (int j = j0; j < j1 && st == FD2D_OK; ++j) {
-        ctx->ws_prefix = "b" + std::to_string(j - j0) + ":";
-        st = fp32_correlation_plan(ctx, B[j].g, B[j].corr, plans[j - j0]);
+      for (size_t q = 0; q < lanes.size() && st == FD2D_OK; ++q) {
+        ctx->ws_prefix = "L" + std::to_string(q) + ":";
+        la.clear();
+        for (int j : lanes[q]) la.push_back(B[j].corr);
+        st = fp32_correlation_plan(ctx, B[lanes[q][0]].g, la.data(), (int)la.size(), plans[q]);
       }
       ctx->ws_prefix.clear();
       if (st == FD2D_OK) st = run_parallel(ctx, "batch_corr", 0x2u, plans);
     }
-    for (int j = j0; j < j1 && st == FD2D_OK; ++j)
-      st = stage_out(ctx, jobs[j].correlations, B[j].corr.seis, (size_t)jobs[j].nr * B[j].g.ntc * 8);
+    for (int j = j0; j < j1 && st == FD2D_OK; ++j) {
+      const size_t bytes = (size_t)jobs[j].nr * B[j].g.ntc * 8;
+      if (B[j].corr_lane) {
+        if (bytes && jobs[j].correlations)
+        {
+          const cudaError_t e =
+              cudaMemcpyAsync(jobs[j].correlations, B[j].corr_lane, bytes, cudaMemcpyDefault, ctx->stream);
+          if (e != cudaSuccess) st = set_error(ctx, FD2D_ERR_CUDA, std::string("copy correlations: ") + cudaGetErrorString(e));
+        }
+      } else {
+        st = stage_out(ctx, jobs[j].correlations, B[j].corr.seis, bytes);
+      }
+    }
     if (st == FD2D_OK && j1 < n_jobs && ctx->memspace == FD2D_MEM_DEVICE)
       st = FD2D_OK;  // device outputs are already in place
     j0 = j1;
   }
   ctx->ws_prefix.clear();
   if (st != FD2D_OK) return st;
-  return finish(ctx);
+  return finish_call(ctx);
 }

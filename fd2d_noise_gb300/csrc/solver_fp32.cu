@@ -42,6 +42,8 @@ constexpr int MAX_BOX_SRC = 64;
 
 struct Grid32 {
   int nx, nz, P;  // P: row pitch of internal arrays (floats)
+  int S;          // lanes: solves of this grid advanced by one launch (blockIdx.z)
+  int64_t ps;     // plane stride of the pitched arrays; lane l's plane starts at l*ps
   float c[4];
   float inv_dx, inv_dz, dt;
   int* err;       // device error flag (bounded waits)
@@ -73,20 +75,23 @@ struct alignas(64) StepMaps {
   CUtensorMap sxy, szy, v, u, b, taper, dtmu, inj;
 };
 
+// Per-step arguments.  Arrays marked "per lane" hold lane l's part at the
+// stated offset (lanes are the solves of one launch, blockIdx.z).
 struct Step32 {
-  float *vo, *sxyo, *szyo, *uo;  // fields written this step (buffer 1 - par)
+  float *vo, *sxyo, *szyo, *uo;  // fields written this step (buffer 1 - par); per lane + l*ps
   int has_u;
-  int inj_plane;                 // plane of the injection map, or -1
-  const int2* src_xy;
+  int inj_plane;                 // plane of the injection map (lane l reads plane inj_plane*S + l), or -1
+  const int2* src_xy;            // per lane + l*nsrc
   int nsrc;
-  const double* amp;             // per-source amplitude of this step, or nullptr -> amp_const
+  const double* amp;             // per-source amplitude of this step (per lane + l*nsrc), or nullptr -> amp_const
   float amp_const;
-  float* snap_pre;               // single(old field) in MATLAB layout, or nullptr
+  float* snap_pre;               // single(old field) in MATLAB layout, or nullptr (one lane only)
   int snap_pre_u;
-  float* snap_dft;               // new field (v or u) into the DFT snapshot plane (pitched)
-  const int2* rec_xy;
+  float* snap_dft;               // new field (v or u) into the DFT snapshot plane (pitched); per lane + l*ps
+  const int2* rec_xy;            // per lane + l*nrec
   int nrec;
-  double* seis_col;              // seismograms(:, n)
+  double* seis_col;              // seismograms(:, n); per lane + l*seis_lane
+  int64_t seis_lane;
   int rec_u;
 };
 
@@ -105,6 +110,10 @@ __global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__
   const int nx = G.nx, nz = G.nz, P = G.P;
   const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
   const int bx0 = x0 - R + 1, bz0 = z0 - R + 1;
+  const int lane = blockIdx.z;
+  const int64_t lo = (int64_t)lane * G.ps;
+  const int2* src_xy = S.src_xy + (int64_t)lane * S.nsrc;
+  const double* amp = S.amp ? S.amp + (int64_t)lane * S.nsrc : nullptr;
 
   if (tid == 0) {
     s_nsrc = 0;
@@ -114,21 +123,21 @@ __global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__
     if (S.has_u) bytes += 4u * TZ * TX;
     if (S.inj_plane >= 0) bytes += 4u * T::BH * T::BWa;
     mbar_expect_tx(&bar, bytes);
-    tma_load_2d(sm + T::O_SXY, &M.sxy, x0 - 8, bz0, &bar);
-    tma_load_2d(sm + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, &bar);
-    tma_load_2d(sm + T::O_V, &M.v, x0 - 4, bz0, &bar);
-    tma_load_2d(sm + T::O_B, &M.b, x0 - 4, bz0, &bar);
-    tma_load_2d(sm + T::O_T, &M.taper, x0 - 4, bz0, &bar);
-    tma_load_2d(sm + T::O_MU, &M.dtmu, x0, z0, &bar);
-    if (S.has_u) tma_load_2d(sm + T::O_U, &M.u, x0, z0, &bar);
-    if (S.inj_plane >= 0) tma_load_3d(sm + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane, &bar);
+    tma_load_3d(sm + T::O_SXY, &M.sxy, x0 - 8, bz0, lane, &bar);
+    tma_load_3d(sm + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, lane, &bar);
+    tma_load_3d(sm + T::O_V, &M.v, x0 - 4, bz0, lane, &bar);
+    tma_load_3d(sm + T::O_B, &M.b, x0 - 4, bz0, lane, &bar);
+    tma_load_3d(sm + T::O_T, &M.taper, x0 - 4, bz0, lane, &bar);
+    tma_load_3d(sm + T::O_MU, &M.dtmu, x0, z0, lane, &bar);
+    if (S.has_u) tma_load_3d(sm + T::O_U, &M.u, x0, z0, lane, &bar);
+    if (S.inj_plane >= 0) tma_load_3d(sm + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, &bar);
   }
   // point sources of the box (global loads overlap the TMA traffic)
   int2 my_src = make_int2(-1 << 30, -1 << 30);
   float my_amp = 0.f;
   if (tid < S.nsrc) {
-    my_src = S.src_xy[tid];
-    my_amp = S.amp ? (float)S.amp[tid] : S.amp_const;
+    my_src = src_xy[tid];
+    my_amp = amp ? (float)amp[tid] : S.amp_const;
   }
   __syncthreads();  // barrier initialised, s_nsrc cleared
   {
@@ -142,12 +151,12 @@ __global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__
     }
   }
   for (int k = tid + NT; k < S.nsrc; k += NT) {  // more sources than threads: rare
-    const int2 q = S.src_xy[k];
+    const int2 q = src_xy[k];
     if (q.x >= bx0 && q.x < bx0 + T::BWc && q.y >= bz0 && q.y < bz0 + T::BH) {
       const int slot = atomicAdd(&s_nsrc, 1);
       if (slot < MAX_BOX_SRC) {
         s_src[slot] = (q.y - bz0) * T::BWc + (q.x - bx0);
-        s_amp[slot] = S.amp ? (float)S.amp[k] : S.amp_const;
+        s_amp[slot] = amp ? (float)amp[k] : S.amp_const;
       }
     }
   }
@@ -197,8 +206,8 @@ __global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__
           if (s_src[q] == e) ds += s_amp[q];
       } else {
         for (int q = 0; q < S.nsrc; ++q) {
-          const int2 w = S.src_xy[q];
-          if (w.x == gx && w.y == gz) ds += S.amp ? (float)S.amp[q] : S.amp_const;
+          const int2 w = src_xy[q];
+          if (w.x == gx && w.y == gz) ds += amp ? (float)amp[q] : S.amp_const;
         }
       }
     }
@@ -220,7 +229,7 @@ __global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__
     const int e = tz * TX + tx;
     const int i = x0 + tx, j = z0 + tz;
     if (i >= nx || j >= nz) continue;
-    const int p = i + P * j;
+    const int64_t p = lo + i + P * j;
     const int rr = tz + R - 1, cc = tx + R - 1;
     const float* vrow = s_vn + rr * T::BWc + cc;
     const float vn = vrow[0];
@@ -256,11 +265,13 @@ __global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__
   }
   if (S.nrec) {
     __syncthreads();
+    const int2* rec_xy = S.rec_xy + (int64_t)lane * S.nrec;
+    double* seis = S.seis_col + lane * S.seis_lane;
     for (int k = tid; k < S.nrec; k += NT) {
-      const int2 q = S.rec_xy[k];
+      const int2 q = rec_xy[k];
       if (q.x >= x0 && q.x < x0 + TX && q.y >= z0 && q.y < z0 + TZ) {
-        const int p = q.x + P * q.y;
-        S.seis_col[k] = (double)(S.rec_u ? S.uo[p] : S.vo[p]);
+        const int64_t p = lo + q.x + P * q.y;
+        seis[k] = (double)(S.rec_u ? S.uo[p] : S.vo[p]);
       }
     }
   }
@@ -405,6 +416,8 @@ struct Run {
   int2* src_xy = nullptr;
   int64_t np = 0;   // nx*nz
   int64_t ps = 0;   // pitched plane size P*nz rounded up to 128
+  int S = 1;        // lanes; every internal array holds S planes (lane l at l*ps)
+  int64_t lanes_ps() const { return (int64_t)S * ps; }
 };
 
 template <int R>
@@ -451,18 +464,22 @@ fd2d_status make_maps(fd2d_ctx* ctx, Run& r) {
   const int BH = TZ + 2 * R - 1, SZH = TZ + 4 * R - 2, BWa = TX + 8, SXWa = TX + 16;
   for (int q = 0; q < 2; ++q) {
     StepMaps& m = r.maps[q];
-    FD2D_TRY(make_tmap_f32(ctx, &m.sxy, r.sxy[q], nx, nz, P, SXWa, BH));
-    FD2D_TRY(make_tmap_f32(ctx, &m.szy, r.szy[q], nx, nz, P, BWa, SZH));
-    FD2D_TRY(make_tmap_f32(ctx, &m.v, r.v[q], nx, nz, P, BWa, BH));
-    FD2D_TRY(make_tmap_f32(ctx, &m.u, r.u[q] ? r.u[q] : r.v[q], nx, nz, P, TX, TZ));
-    FD2D_TRY(make_tmap_f32(ctx, &m.b, r.b, nx, nz, P, BWa, BH));
-    FD2D_TRY(make_tmap_f32(ctx, &m.taper, r.taper, nx, nz, P, BWa, BH));
-    FD2D_TRY(make_tmap_f32(ctx, &m.dtmu, r.dtmu, nx, nz, P, TX, TZ));
+    // lanes are the third dimension (plane stride ps)
+    const int S = r.S;
+    const int64_t ps = r.ps;
+    FD2D_TRY(make_tmap_f32(ctx, &m.sxy, r.sxy[q], nx, nz, P, SXWa, BH, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.szy, r.szy[q], nx, nz, P, BWa, SZH, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.v, r.v[q], nx, nz, P, BWa, BH, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.u, r.u[q] ? r.u[q] : r.v[q], nx, nz, P, TX, TZ, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.b, r.b, nx, nz, P, BWa, BH, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.taper, r.taper, nx, nz, P, BWa, BH, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.dtmu, r.dtmu, nx, nz, P, TX, TZ, S, ps));
     FD2D_TRY(make_tmap_f32(ctx, &m.inj, r.b, nx, nz, P, BWa, BH));  // replaced when planes exist
   }
   return FD2D_OK;
 }
 
+// Injection planes are [event][lane] planes of stride ps: lane l of event j is plane j*S + l.
 fd2d_status set_inj_map(fd2d_ctx* ctx, Run& r, const float* planes, int n_planes) {
   const int BH = TZ + 2 * r.R - 1, BWa = TX + 8;
   for (int q = 0; q < 2; ++q)
@@ -470,54 +487,67 @@ fd2d_status set_inj_map(fd2d_ctx* ctx, Run& r, const float* planes, int n_planes
   return FD2D_OK;
 }
 
-fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, bool with_u, Run& r) {
+// Buffers, coefficient planes and tensor maps of S lanes a[0..S-1] (solves of
+// one geometry with the same numbers of sources and receivers).
+fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S, bool with_u, Run& r) {
   const int nx = g.nx, nz = g.nz;
   const int P = (nx + 31) / 32 * 32;
+  for (int l = 1; l < S; ++l)
+    if (a[l].src_idx.size() != a[0].src_idx.size() || a[l].rec_idx.size() != a[0].rec_idx.size())
+      return set_error(ctx, FD2D_ERR_SHAPE, "lanes of one launch need equal source and receiver counts");
+  r.S = S;
   r.np = g.npts();
   r.ps = ((int64_t)P * nz + 127) / 128 * 128;
   r.R = g.r;
   r.G.nx = nx;
   r.G.nz = nz;
   r.G.P = P;
+  r.G.S = S;
+  r.G.ps = r.ps;
   for (int m = 0; m < 4; ++m) r.G.c[m] = (float)g.c[m];
   r.G.inv_dx = (float)(1.0 / g.dx);
   r.G.inv_dz = (float)(1.0 / g.dz);
   r.G.dt = (float)g.dt;
   r.G.err = ctx->d_err;
   r.pblock = dim3(32, 8);
-  const size_t ps = (size_t)r.ps;
-  FD2D_TRY(workspace_t(ctx, "f32.b", ps, &r.b));
-  FD2D_TRY(workspace_t(ctx, "f32.taper", ps, &r.taper));
-  FD2D_TRY(workspace_t(ctx, "f32.dtmu", ps, &r.dtmu));
+  const size_t ps = (size_t)r.ps, sps = (size_t)r.lanes_ps();
+  FD2D_TRY(workspace_t(ctx, "f32.b", sps, &r.b));
+  FD2D_TRY(workspace_t(ctx, "f32.taper", sps, &r.taper));
+  FD2D_TRY(workspace_t(ctx, "f32.dtmu", sps, &r.dtmu));
   double* ab;
   FD2D_TRY(upload_tagged<double>(ctx, "f32.absbound64", g.key, g.absbound->size(),
                                   [&](std::vector<double>& h) { h = *g.absbound; }, &ab));
   dim3 pg((P + 31) / 32, (nz + 7) / 8);
-  k32_prep<<<pg, r.pblock, 0, ctx->stream>>>(a.mu, a.rho, ab, g.dt, nx, nz, P, r.b, r.taper, r.dtmu);
-  FD2D_TRY(after_launch(ctx, "k32_prep"));
+  for (int l = 0; l < S; ++l) {
+    k32_prep<<<pg, r.pblock, 0, ctx->stream>>>(a[l].mu, a[l].rho, ab, g.dt, nx, nz, P, r.b + l * ps,
+                                               r.taper + l * ps, r.dtmu + l * ps);
+    FD2D_TRY(after_launch(ctx, "k32_prep"));
+  }
   static const char* names[2][4] = {{"f32.v0", "f32.sxy0", "f32.szy0", "f32.u0"},
                                     {"f32.v1", "f32.sxy1", "f32.szy1", "f32.u1"}};
   for (int q = 0; q < 2; ++q) {
-    FD2D_TRY(workspace_t(ctx, names[q][0], ps, &r.v[q]));
-    FD2D_TRY(workspace_t(ctx, names[q][1], ps, &r.sxy[q]));
-    FD2D_TRY(workspace_t(ctx, names[q][2], ps, &r.szy[q]));
-    FD2D_CUDA(ctx, cudaMemsetAsync(r.v[q], 0, ps * 4, ctx->stream));
-    FD2D_CUDA(ctx, cudaMemsetAsync(r.sxy[q], 0, ps * 4, ctx->stream));
-    FD2D_CUDA(ctx, cudaMemsetAsync(r.szy[q], 0, ps * 4, ctx->stream));
+    FD2D_TRY(workspace_t(ctx, names[q][0], sps, &r.v[q]));
+    FD2D_TRY(workspace_t(ctx, names[q][1], sps, &r.sxy[q]));
+    FD2D_TRY(workspace_t(ctx, names[q][2], sps, &r.szy[q]));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.v[q], 0, sps * 4, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.sxy[q], 0, sps * 4, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.szy[q], 0, sps * 4, ctx->stream));
     if (with_u) {
-      FD2D_TRY(workspace_t(ctx, names[q][3], ps, &r.u[q]));
-      FD2D_CUDA(ctx, cudaMemsetAsync(r.u[q], 0, ps * 4, ctx->stream));
+      FD2D_TRY(workspace_t(ctx, names[q][3], sps, &r.u[q]));
+      FD2D_CUDA(ctx, cudaMemsetAsync(r.u[q], 0, sps * 4, ctx->stream));
     }
   }
-  auto xy = [&](const std::vector<int>& idx) {
+  // node lists of all lanes, lane after lane
+  auto xy = [&](bool rec) {
     std::vector<int2> out;
-    for (int p : idx) out.push_back(make_int2(p % nx, p / nx));
+    for (int l = 0; l < S; ++l)
+      for (int p : rec ? a[l].rec_idx : a[l].src_idx) out.push_back(make_int2(p % nx, p / nx));
     if (out.empty()) out.push_back(make_int2(-1 << 30, -1 << 30));
     return out;
   };
-  FD2D_TRY(upload(ctx, "f32.rec", xy(a.rec_idx), &r.rec_xy));
-  FD2D_TRY(upload(ctx, "f32.src", xy(a.src_idx), &r.src_xy));
-  r.sgrid = dim3((nx + TX - 1) / TX, (nz + TZ - 1) / TZ);
+  FD2D_TRY(upload(ctx, "f32.rec", xy(true), &r.rec_xy));
+  FD2D_TRY(upload(ctx, "f32.src", xy(false), &r.src_xy));
+  r.sgrid = dim3((nx + TX - 1) / TX, (nz + TZ - 1) / TZ, S);
   r.pgrid = dim3((nx + 31) / 32, (nz + 7) / 8);
   FD2D_TRY(step_attributes(ctx));
   FD2D_TRY(contract_prepare(ctx));
@@ -542,11 +572,15 @@ __global__ void k32_spectrum_eff(const double* spec, int K, int n_src, double* e
   e[k] = acc;
 }
 
-// Effective spectrum: sum over noise sources (they share one distribution).
-fd2d_status spectrum_eff(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, double** out) {
-  FD2D_TRY(workspace_t(ctx, "f32.spec_eff", (size_t)g.K, out));
-  k32_spectrum_eff<<<(g.K + 127) / 128, 128, 0, ctx->stream>>>(a.spectrum, g.K, a.n_src, *out);
-  return after_launch(ctx, "k32_spectrum_eff");
+// Effective spectrum: sum over noise sources (they share one distribution);
+// lane l's K values at out + l*K.
+fd2d_status spectrum_eff(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S, double** out) {
+  FD2D_TRY(workspace_t(ctx, "f32.spec_eff", (size_t)g.K * S, out));
+  for (int l = 0; l < S; ++l) {
+    k32_spectrum_eff<<<(g.K + 127) / 128, 128, 0, ctx->stream>>>(a[l].spectrum, g.K, a[l].n_src, *out + l * g.K);
+    FD2D_TRY(after_launch(ctx, "k32_spectrum_eff"));
+  }
+  return FD2D_OK;
 }
 
 // Tag of a coefficient table: configuration, table kind and the rows it holds.
@@ -562,22 +596,27 @@ struct Injection {
   std::vector<int> row_of_event;   // coefficient row used by event j
   float* planes = nullptr;         // [chunk][ps]
   int chunk = 0, first = 0, count = 0;  // events [first, first+count) resident
-  float* P = nullptr;              // 2K pitched planes
+  float* P = nullptr;              // 2K planes of S lanes: [k][lane][ps]
   float* B = nullptr;              // [2K][n_events] float
   int n_events = 0;
 };
 
-fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, Run& r, const double* Xre, const double* Xim,
-                            double sign, const double* spec_eff, const double* M, const double* sd,
-                            Injection& inj) {
+// Per lane l: X = (Xre[l], Xim[l]) spectra, source distribution sd[l], and
+// effective spectrum spec_eff + l*K.
+fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, Run& r, const double* const* Xre,
+                            const double* const* Xim, double sign, const double* spec_eff, const double* M,
+                            const double* const* sd, Injection& inj) {
   const int K = g.K, ncol = g.nb == 0 ? 1 : g.nb;
   inj.n_events = (int)inj.step_of_event.size();
   if (inj.n_events == 0) return FD2D_OK;
-  FD2D_TRY(workspace_t(ctx, "f32.P", (size_t)r.ps * 2 * K, &inj.P));
+  const int64_t sps = r.lanes_ps();
+  FD2D_TRY(workspace_t(ctx, "f32.P", (size_t)sps * 2 * K, &inj.P));
   dim3 pg((r.G.P + 31) / 32, (g.nz + 7) / 8);
-  k32_make_P<<<pg, r.pblock, 0, ctx->stream>>>(K, ncol, M, sd, spec_eff, Xre, Xim, sign, g.nx, g.nz, r.G.P,
-                                               r.ps, inj.P);
-  FD2D_TRY(after_launch(ctx, "k32_make_P"));
+  for (int l = 0; l < r.S; ++l) {
+    k32_make_P<<<pg, r.pblock, 0, ctx->stream>>>(K, ncol, M, sd[l], spec_eff + l * K, Xre[l], Xim[l], sign, g.nx,
+                                                 g.nz, r.G.P, sps, inj.P + l * r.ps);
+    FD2D_TRY(after_launch(ctx, "k32_make_P"));
+  }
   // B[k][j] = Re c(row_j, k); B[K+k][j] = -Im c(row_j, k)   (c = ifft_coeff, dw)
   auto fill = [&](std::vector<float>& B) {
     for (int j = 0; j < inj.n_events; ++j) {
@@ -593,11 +632,11 @@ fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, Run& r, const doub
   FD2D_TRY(upload_tagged<float>(ctx, "f32.injB", table_tag(g, 2, inj.row_of_event),
                                 (size_t)2 * K * inj.n_events, fill, &inj.B));
   const size_t cap = (size_t)4 << 30;  // resident injection planes <= 4 GiB
-  inj.chunk = (int)std::max<int64_t>(1, std::min<int64_t>(inj.n_events, (int64_t)(cap / (r.ps * 4))));
-  FD2D_TRY(workspace_t(ctx, "f32.inj", (size_t)r.ps * inj.chunk, &inj.planes));
+  inj.chunk = (int)std::max<int64_t>(1, std::min<int64_t>(inj.n_events, (int64_t)(cap / (sps * 4))));
+  FD2D_TRY(workspace_t(ctx, "f32.inj", (size_t)sps * inj.chunk, &inj.planes));
   inj.first = 0;
   inj.count = 0;
-  return set_inj_map(ctx, r, inj.planes, inj.chunk);
+  return set_inj_map(ctx, r, inj.planes, inj.chunk * r.S);
 }
 
 // Plane index of event j in the resident chunk (evaluates the next chunk when needed).
@@ -607,14 +646,14 @@ fd2d_status injection_plane(fd2d_ctx* ctx, const Run& r, const Geometry& g, Inje
     inj.count = std::min(inj.chunk, inj.n_events - j);
     ContractArgs c;
     c.A = inj.P;
-    c.lda = r.ps;
+    c.lda = r.lanes_ps();
     c.Kd = 2 * g.K;
     c.B = inj.B + j;
     c.ldb = inj.n_events;
-    c.M = (int)r.ps;
+    c.M = (int)r.lanes_ps();
     c.N = inj.count;
     c.out32 = inj.planes;
-    c.ldo = r.ps;
+    c.ldo = r.lanes_ps();
     FD2D_TRY(contract(ctx, ctx->stream, c));
   }
   *plane = j - inj.first;
@@ -629,7 +668,8 @@ struct Dft {
   float* snaps = nullptr;
   struct Target {
     float* B = nullptr;  // [n_events][2K] rows
-    double *re = nullptr, *im = nullptr;
+    double *re = nullptr, *im = nullptr;  // lane 0's spectra; lane l's start l*lane_stride later
+    int64_t lane_stride = 0;
   };
   std::vector<Target> targets;
   int n_events = 0;
@@ -639,10 +679,11 @@ fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
   d.n_events = n_events;
   if (n_events == 0) return FD2D_OK;
   const size_t cap = (size_t)2 << 30;  // snapshot chunk <= 2 GiB
-  d.T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)n_events, (int64_t)1024, (int64_t)(cap / (r.ps * 4))}));
-  FD2D_TRY(workspace_t(ctx, "f32.dft_snaps", (size_t)r.ps * d.T, &d.snaps));
+  const int64_t sps = r.lanes_ps();
+  d.T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)n_events, (int64_t)1024, (int64_t)(cap / (sps * 4))}));
+  FD2D_TRY(workspace_t(ctx, "f32.dft_snaps", (size_t)sps * d.T, &d.snaps));
   // the pitch padding of the snapshot planes is never written by the stencil
-  FD2D_CUDA(ctx, cudaMemsetAsync(d.snaps, 0, (size_t)r.ps * d.T * 4, ctx->stream));
+  FD2D_CUDA(ctx, cudaMemsetAsync(d.snaps, 0, (size_t)sps * d.T * 4, ctx->stream));
   return FD2D_OK;
 }
 
@@ -650,27 +691,32 @@ fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
 // `fill` generates them when the buffer does not already hold table `tag`.
 template <typename F>
 fd2d_status dft_add_target(fd2d_ctx* ctx, const char* name, uint64_t tag, size_t count, F&& fill, double* re,
-                           double* im, Dft& d) {
+                           double* im, int64_t lane_stride, Dft& d) {
   Dft::Target t;
   FD2D_TRY(upload_tagged<float>(ctx, name, tag, count, fill, &t.B));
   t.re = re;
   t.im = im;
+  t.lane_stride = lane_stride;
   d.targets.push_back(t);
   return FD2D_OK;
 }
 
-float* dft_slot(const Run& r, Dft& d) { return d.snaps + (size_t)d.filled * r.ps; }
+float* dft_slot(const Run& r, Dft& d) { return d.snaps + (size_t)d.filled * r.lanes_ps(); }
 
 fd2d_status dft_flush(fd2d_ctx* ctx, const Run& r, const Geometry& g, Dft& d) {
   if (d.filled == 0) return FD2D_OK;
   for (auto& t : d.targets) {
     ContractArgs c;
     c.A = d.snaps;
-    c.lda = r.ps;
+    c.lda = r.lanes_ps();
     c.Kd = d.filled;
     c.B = t.B + (size_t)d.done * 2 * g.K;
     c.ldb = 2 * g.K;
-    c.M = (int)r.ps;
+    c.M = (int)r.lanes_ps();
+    if (r.S > 1) {
+      c.lane_m = r.ps;
+      c.acc_lane = t.lane_stride;
+    }
     c.N = 2 * g.K;
     c.acc0 = t.re;
     c.acc1 = t.im;
@@ -736,9 +782,38 @@ fd2d_status f32_copy_pitched(fd2d_ctx* ctx, const Run& r, const double* a, doubl
 // forward1 / correlation are split into an eager prepare step (buffers, uploads,
 // P planes) and a capturable time loop, so that a batch can run the loops of
 // many solves as parallel branches of one CUDA graph.
-fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, LoopPlan& plan) {
+// Lanes a[0..S-1]: solves of one geometry advanced together (S > 1: mode 0,
+// no Born term, outputs at constant strides from lane 0's).
+template <typename T>
+static fd2d_status lane_stride_of(fd2d_ctx* ctx, int S, T* const* p, int64_t* out) {
+  *out = 0;
+  if (S < 2) return FD2D_OK;
+  *out = p[1] - p[0];
+  for (int l = 2; l < S; ++l)
+    if (p[l] - p[l - 1] != *out) return set_error(ctx, FD2D_ERR_ARG, "lane outputs are not equally spaced");
+  return FD2D_OK;
+}
+
+static fd2d_status check_lanes(fd2d_ctx* ctx, const SolveArgs* a, int S) {
+  if (S < 1) return set_error(ctx, FD2D_ERR_ARG, "no lanes");
+  for (int l = 0; l < S && S > 1; ++l)
+    if (a[l].mode != 0 || a[l].dmu)
+      return set_error(ctx, FD2D_ERR_UNSUPPORTED, "lanes advance mode-0 solves without Born terms only");
+  return FD2D_OK;
+}
+
+fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* al, int S, LoopPlan& plan) {
+  FD2D_TRY(check_lanes(ctx, al, S));
+  const SolveArgs& a = al[0];
+  std::vector<double*> gre(S), gim(S), seis(S);
+  for (int l = 0; l < S; ++l) { gre[l] = al[l].G_re; gim[l] = al[l].G_im; seis[l] = al[l].seis; }
+  int64_t g_lane = 0, gi_lane = 0, seis_lane = 0;
+  FD2D_TRY(lane_stride_of(ctx, S, gre.data(), &g_lane));
+  FD2D_TRY(lane_stride_of(ctx, S, gim.data(), &gi_lane));
+  FD2D_TRY(lane_stride_of(ctx, S, seis.data(), &seis_lane));
+  if (g_lane != gi_lane) return set_error(ctx, FD2D_ERR_ARG, "lane spectra strides differ");
   Run r;
-  FD2D_TRY(init_run(ctx, g, a, false, r));
+  FD2D_TRY(init_run(ctx, g, al, S, false, r));
   const int nt = g.nt, K = g.K;
   const int64_t np = r.np;
   // DFT events: steps n with mod(n+nt-1, freq_samp) == 0; coefficient of step n is
@@ -759,20 +834,23 @@ fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs
           rows[e * 2 * K + K + k] = (float)(-im);
         }
     };
-    FD2D_TRY(dft_add_target(ctx, "f32.dftB0", table_tag(g, 0, ev), ev.size() * 2 * K, fill, a.G_re, a.G_im, d));
+    FD2D_TRY(dft_add_target(ctx, "f32.dftB0", table_tag(g, 0, ev), ev.size() * 2 * K, fill, a.G_re, a.G_im,
+                            g_lane, d));
   } else {
     // no DFT step: the spectra are zero (otherwise the first flush overwrites them)
-    FD2D_CUDA(ctx, cudaMemsetAsync(a.G_re, 0, (size_t)np * K * 8, ctx->stream));
-    FD2D_CUDA(ctx, cudaMemsetAsync(a.G_im, 0, (size_t)np * K * 8, ctx->stream));
+    for (int l = 0; l < S; ++l) {
+      FD2D_CUDA(ctx, cudaMemsetAsync(al[l].G_re, 0, (size_t)np * K * 8, ctx->stream));
+      FD2D_CUDA(ctx, cudaMemsetAsync(al[l].G_im, 0, (size_t)np * K * 8, ctx->stream));
+    }
   }
   float* dtdmu = nullptr;
   const bool born = a.dmu != nullptr;
   if (born) FD2D_TRY(f32_copy_pitched(ctx, r, a.dmu, g.dt, "f32.dtdmu", &dtdmu));
   Sig sg;
-  sig_run(sg, r); sig_args(sg, g, a); sig_dft(sg, d); sg.add(dtdmu);
+  sig_run(sg, r); sig_args(sg, g, a); sig_dft(sg, d); sg.add(dtdmu); sg.add(S); sg.add(seis_lane);
   plan.name = "fp32_forward1";
   plan.key = sg.h;
-  plan.loop = [ctx, g, a, r, d, dtdmu, born]() -> fd2d_status {
+  plan.loop = [ctx, g, a, r, d, dtdmu, born, seis_lane]() -> fd2d_status {
     Dft dd = d;  // the loop's own chunk bookkeeping
     const int nt = g.nt, nr = (int)a.rec_idx.size();
     const int64_t np = r.np;
@@ -795,38 +873,51 @@ fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs
       s.rec_xy = r.rec_xy;
       s.nrec = nr;
       s.seis_col = a.seis + (size_t)nr * (n - 1);
+      s.seis_lane = seis_lane;
       FD2D_TRY(launch_step(ctx, r, par, s));
       if (is_dft) FD2D_TRY(dft_push(ctx, r, g, dd));
       par ^= 1;
     }
-    timer_end(ctx, ctx->stream, tl, FD2D_TIMER_STEP_V, np * nt, nt);
+    timer_end(ctx, ctx->stream, tl, FD2D_TIMER_STEP_V, np * nt * r.S, nt);
     return FD2D_OK;
   };
   return FD2D_OK;
 }
 
-fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a, LoopPlan& plan) {
+fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* al, int S, LoopPlan& plan) {
+  FD2D_TRY(check_lanes(ctx, al, S));
+  const SolveArgs& a = al[0];
+  std::vector<double*> seis(S);
+  std::vector<const double*> xre(S), xim(S), sd(S);
+  for (int l = 0; l < S; ++l) {
+    seis[l] = al[l].seis;
+    xre[l] = al[l].Gin_re;
+    xim[l] = al[l].Gin_im;
+    sd[l] = al[l].source_dist;
+  }
+  int64_t seis_lane = 0;
+  FD2D_TRY(lane_stride_of(ctx, S, seis.data(), &seis_lane));
   Run r;
-  FD2D_TRY(init_run(ctx, g, a, true, r));
+  FD2D_TRY(init_run(ctx, g, al, S, true, r));
   const int ntc = g.ntc;
   double *M, *spec;
   FD2D_TRY(interp_dev(ctx, g, &M));
-  FD2D_TRY(spectrum_eff(ctx, g, a, &spec));
+  FD2D_TRY(spectrum_eff(ctx, g, al, S, &spec));
   Injection inj;
   for (int n = 1; n <= ntc; ++n)
     if (n % g.fs == 0) {
       inj.step_of_event.push_back(n);
       inj.row_of_event.push_back(n / g.fs - 1);
     }
-  FD2D_TRY(build_injection(ctx, g, r, a.Gin_re, a.Gin_im, 1.0, spec, M, a.source_dist, inj));
+  FD2D_TRY(build_injection(ctx, g, r, xre.data(), xim.data(), 1.0, spec, M, sd.data(), inj));
   float* dmu32 = nullptr;
   const bool born = a.dmu != nullptr;
   if (born) FD2D_TRY(f32_copy_pitched(ctx, r, a.dmu, 1.0, "f32.dmu", &dmu32));
   Sig sg;
-  sig_run(sg, r); sig_args(sg, g, a); sig_inj(sg, inj); sg.add(dmu32);
+  sig_run(sg, r); sig_args(sg, g, a); sig_inj(sg, inj); sg.add(dmu32); sg.add(S); sg.add(seis_lane);
   plan.name = "fp32_correlation";
   plan.key = sg.h;
-  plan.loop = [ctx, g, a, r, inj, dmu32, born]() -> fd2d_status {
+  plan.loop = [ctx, g, a, r, inj, dmu32, born, seis_lane]() -> fd2d_status {
     Injection ij = inj;  // the loop's own chunk bookkeeping
     const int ntc = g.ntc, nr = (int)a.rec_idx.size();
     const int64_t np = r.np;
@@ -844,6 +935,7 @@ fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveA
       s.rec_xy = r.rec_xy;
       s.nrec = nr;
       s.seis_col = a.seis + (size_t)nr * (n - 1);
+      s.seis_lane = seis_lane;
       s.rec_u = 1;  // u does not depend on this step's Born stress correction
       FD2D_TRY(launch_step(ctx, r, par, s));
       par ^= 1;
@@ -853,7 +945,7 @@ fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveA
         FD2D_TRY(after_launch(ctx, "k32_born_post"));
       }
     }
-    timer_end(ctx, ctx->stream, tl, FD2D_TIMER_STEP_VU, np * ntc, ntc);
+    timer_end(ctx, ctx->stream, tl, FD2D_TIMER_STEP_VU, np * ntc * r.S, ntc);
     return FD2D_OK;
   };
   return FD2D_OK;
@@ -861,19 +953,19 @@ fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveA
 
 fd2d_status fp32_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
   LoopPlan p;
-  FD2D_TRY(fp32_forward1_plan(ctx, g, a, p));
+  FD2D_TRY(fp32_forward1_plan(ctx, g, &a, 1, p));
   return run_captured(ctx, p.name.c_str(), p.key, p.loop);
 }
 
 fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
   LoopPlan p;
-  FD2D_TRY(fp32_correlation_plan(ctx, g, a, p));
+  FD2D_TRY(fp32_correlation_plan(ctx, g, &a, 1, p));
   return run_captured(ctx, p.name.c_str(), p.key, p.loop);
 }
 
 fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
   Run r;
-  FD2D_TRY(init_run(ctx, g, a, true, r));
+  FD2D_TRY(init_run(ctx, g, &a, 1, true, r));
   const int ntc = g.ntc, K = g.K, mode = a.mode;
   const int64_t np = r.np;
   const int ncol = g.nb == 0 ? 1 : g.nb;
@@ -903,7 +995,7 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
   }
   double *M, *spec = nullptr;
   FD2D_TRY(interp_dev(ctx, g, &M));
-  if (a.spectrum) FD2D_TRY(spectrum_eff(ctx, g, a, &spec));
+  if (a.spectrum) FD2D_TRY(spectrum_eff(ctx, g, &a, 1, &spec));
   Injection inj;
   if (stf3d && a.source_dist) {
     inj.step_of_event = inj_step;
@@ -915,7 +1007,7 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
       FD2D_CUDA(ctx, cudaMemsetAsync(z, 0, (size_t)np * K * 8, ctx->stream));
       sim = z;
     }
-    FD2D_TRY(build_injection(ctx, g, r, a.stf_re, sim, -1.0, spec, M, a.source_dist, inj));
+    FD2D_TRY(build_injection(ctx, g, r, &a.stf_re, &sim, -1.0, spec, M, &a.source_dist, inj));
   }
   // DFT of u at the fs steps: stf_fft with the rows the reference uses, and the
   // natural-row spectrum U that forms the source kernel.
@@ -949,7 +1041,7 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
     for (size_t e = 0; e < ev.size(); ++e) nat[e] = ev[e] / g.fs - 1;
     if (dft_u) {
       FD2D_TRY(dft_add_target(ctx, "f32.dftB0", table_tag(g, 1, dft_row), nrows, rows_for(dft_row), a.sf_re,
-                              a.sf_im, d));
+                              a.sf_im, 0, d));
       if (natural) { Ure = a.sf_re; Uim = a.sf_im; }
     }
     if (Gvalid && !Ure) {
@@ -957,7 +1049,7 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
       FD2D_TRY(workspace_t(ctx, "f32.Uim", (size_t)np * K, &Uim));
       FD2D_CUDA(ctx, cudaMemsetAsync(Ure, 0, (size_t)np * K * 8, ctx->stream));
       FD2D_CUDA(ctx, cudaMemsetAsync(Uim, 0, (size_t)np * K * 8, ctx->stream));
-      FD2D_TRY(dft_add_target(ctx, "f32.dftB1", table_tag(g, 1, nat), nrows, rows_for(nat), Ure, Uim, d));
+      FD2D_TRY(dft_add_target(ctx, "f32.dftB1", table_tag(g, 1, nat), nrows, rows_for(nat), Ure, Uim, 0, d));
     }
   }
   float* dmu32 = nullptr;
@@ -1113,6 +1205,7 @@ extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg,
   r.ps = ps;
   r.R = g.r;
   r.G.nx = nx; r.G.nz = nz; r.G.P = P;
+  r.G.S = 1; r.G.ps = ps;
   for (int m = 0; m < 4; ++m) r.G.c[m] = (float)g.c[m];
   r.G.inv_dx = (float)(1.0 / g.dx);
   r.G.inv_dz = (float)(1.0 / g.dz);

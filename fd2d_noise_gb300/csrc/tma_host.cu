@@ -27,7 +27,7 @@ fd2d_status make_tmap_f32(fd2d_ctx* ctx, CUtensorMap* map, const float* base, in
   }
   if ((reinterpret_cast<uintptr_t>(base) & 15) || (pitch_elems * 4) % 16 || bw % 4 || bw > 256 || bh > 256)
     return set_error(ctx, FD2D_ERR_ARG, "tensor map needs 16-byte aligned base, pitch and box width");
-  const cuuint32_t rank = d > 1 ? 3 : 2;
+  const cuuint32_t rank = (d > 1 || plane_elems > 0) ? 3 : 2;
   cuuint64_t dims[3] = {(cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)d};
   cuuint64_t strides[2] = {(cuuint64_t)pitch_elems * 4, (cuuint64_t)plane_elems * 4};
   cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};

@@ -224,9 +224,12 @@ fd2d_status fd2d_noise_adjoint(fd2d_ctx* ctx, const fd2d_config* cfg,
  * mode 0) followed by the correlation wavefield (run_forward2_correlation,
  * mode 0); the job returns the correlations.  Jobs may have different
  * configurations (grid sizes, nt) and models.  Arrays follow the context's
- * memspace.  In FP32 the jobs advance concurrently -- their time loops are
- * parallel branches of one CUDA graph -- in groups whose device buffers fit in
- * the memory budget (default: 80 % of the free device memory at the call).
+ * memspace.  In FP32 the jobs advance concurrently, in groups whose device
+ * buffers fit in the memory budget (default: 80 % of the free device memory at
+ * the call): jobs of one configuration and receiver count are lanes of the same
+ * launches (one stencil launch per time step for all of them, one DFT and one
+ * injection contraction over all their grid points), and jobs of different
+ * configurations run as parallel branches of one CUDA graph.
  * In FP64 (the plain form) the jobs run one after another. */
 typedef struct fd2d_job {
   const fd2d_config* cfg;
@@ -244,6 +247,26 @@ typedef struct fd2d_job {
 fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* jobs, int32_t n_jobs);
 /* Device-memory budget of a batch in bytes (0 = 80 % of the free memory). */
 fd2d_status fd2d_ctx_set_memory_budget(fd2d_ctx* ctx, int64_t bytes);
+
+/* ---- measurements ---------------------------------------------------------------
+ * [misfit_n, adstf] = make_adjoint_sources(u, u_0, du, t, veldis, measurement,
+ *                                          src, rec, deriv_order)
+ * tools/measurement/make_adjoint_sources.m:31-175 with log_amp_ratio.m:23-93
+ * (fixed 100-200 s Hann window on the causal branch and its mirror, :87-103)
+ * and waveform_difference.m:23-48 (cos-taper window over the whole axis), FP64.
+ *   measurement   FD2D_MEAS_*
+ *   deriv_order   1 ('1st': misfit and adjoint source) or 2 ('2nd': the
+ *                 Hessian adjoint source along du; misfit_n is set to 0)
+ *   velocity      0 'dis', 1 'vel' (u, u_0 differentiated; adstf corrected)
+ *   u, u_0, du    n_rec-by-nt (du only for deriv_order 2)
+ *   t             nt time samples, HOST pointer (dt = |t(2) - t(1)|)
+ *   misfit        out, n_rec (may be NULL)        adstf  out, n_rec-by-nt
+ * The source/receiver positions of the MATLAB signature only feed commented-out
+ * window choices there and are not arguments.  nt <= 20480. */
+enum { FD2D_MEAS_WAVEFORM_DIFFERENCE = 0, FD2D_MEAS_LOG_AMPLITUDE_RATIO = 1 };
+fd2d_status fd2d_make_adjoint_sources(fd2d_ctx* ctx, int32_t measurement, int32_t deriv_order, int32_t velocity,
+                                      const double* u, const double* u_0, const double* du, int32_t n_rec,
+                                      int32_t nt, const double* t, double* misfit, double* adstf);
 
 /* ---- building block ----------------------------------------------------------
  * R[n*ldr + m] = sum_{k<Kd} A[k*lda + m] * B[k*ldb + n]  for m < M, n < N:

@@ -91,6 +91,23 @@ def tokenize(src: str) -> List[Tok]:
             out.append(Tok("str", "".join(s), line))
             i = j + 1
             continue
+        if c == '"':  # double-quoted string literal ("" escapes a quote)
+            j = i + 1
+            s = []
+            while True:
+                if j >= n:
+                    raise MatlabError("unterminated string")
+                if src[j] == '"':
+                    if j + 1 < n and src[j + 1] == '"':
+                        s.append('"')
+                        j += 2
+                        continue
+                    break
+                s.append(src[j])
+                j += 1
+            out.append(Tok("str", "".join(s), line))
+            i = j + 1
+            continue
         m = TOKEN_RE.match(src, i)
         if not m:
             raise MatlabError(f"line {line}: cannot tokenize {src[i:i+20]!r}")
@@ -751,6 +768,61 @@ def b_find(x, k=None):
     return idx.reshape(-1, 1)
 
 
+def b_find_n(x, k=None, direction=None):
+    if direction is None or str(direction) == "first":
+        return b_find(x, k)
+    a = A(x)
+    idx = np.nonzero(a.reshape(-1, order="F") != 0)[0] + 1.0
+    idx = idx[-int(scalar(k)):] if k is not None else idx
+    if a.shape[0] == 1 and a.ndim == 2:
+        return idx.reshape(1, -1)
+    return idx.reshape(-1, 1)
+
+
+def b_max(x, *rest):
+    """max of a vector: [value, first index of the maximum]."""
+    if rest:
+        raise MatlabError("max with more than one argument")
+    v = A(x).reshape(-1, order="F")
+    i = int(np.argmax(v))
+    return [A(v[i]), A(float(i + 1))]
+
+
+def b_sum(x):
+    a = A(x)
+    if a.ndim == 2 and (a.shape[0] == 1 or a.shape[1] == 1):
+        acc = a.dtype.type(0) if a.dtype != bool else 0.0
+        for v in a.reshape(-1, order="F"):
+            acc = acc + v
+        return A(acc)
+    return np.asfortranarray(A(np.sum(a, axis=0, keepdims=True)))
+
+
+def b_diff(x):
+    a = A(x)
+    if a.ndim == 2 and a.shape[0] == 1:
+        return np.asfortranarray(a[:, 1:] - a[:, :-1])
+    return np.asfortranarray(a[1:] - a[:-1])
+
+
+def b_trapz(y):
+    """trapz(Y) of a vector: trapezoidal rule with unit spacing."""
+    v = A(y).reshape(-1, order="F")
+    acc = 0.0
+    for i in range(v.size - 1):
+        acc = acc + (v[i] + v[i + 1]) / 2.0
+    return A(acc)
+
+
+def b_hann(n):
+    """Symmetric Hann window (column): 0.5*(1 - cos(2*pi*k/(N-1))), k = 0..N-1."""
+    N = int(scalar(n))
+    if N == 1:
+        return A(1.0)
+    k = np.arange(N, dtype=np.float64)
+    return np.asfortranarray((0.5 * (1.0 - np.cos(2.0 * np.pi * k / (N - 1)))).reshape(-1, 1))
+
+
 def b_min(x, *rest):
     if rest:
         raise MatlabError("min with more than one argument")
@@ -791,7 +863,7 @@ def b_length(x):
 
 BUILTINS: Dict[str, Callable] = {
     "zeros": b_zeros, "ones": b_ones, "size": b_size, "length": lambda x: b_length(x),
-    "reshape": b_reshape, "find": b_find, "min": b_min, "mod": b_mod, "squeeze": b_squeeze,
+    "reshape": b_reshape, "min": b_min, "mod": b_mod, "squeeze": b_squeeze,
     "meshgrid": b_meshgrid,
     "abs": lambda x: np.asfortranarray(np.abs(A(x))),
     "exp": lambda x: np.asfortranarray(np.exp(to_float(A(x)))),
@@ -806,6 +878,14 @@ BUILTINS: Dict[str, Callable] = {
     "all": lambda x: A(bool(np.all(A(x) != 0))),
     "numel": lambda x: A(float(A(x).size)),
     "pi": lambda: A(np.pi),
+    "eps": lambda: A(np.finfo(np.float64).eps),
+    "log": lambda x: np.asfortranarray(np.log(to_float(A(x)))),
+    "cos": lambda x: np.asfortranarray(np.cos(to_float(A(x)))),
+    "fliplr": lambda x: np.asfortranarray(A(x)[:, ::-1]),
+    "strcmp": lambda a, b: A(isinstance(a, str) and isinstance(b, str) and a == b),
+    "fprintf": lambda *a: [],
+    "error": lambda *a: (_ for _ in ()).throw(MatlabError(str(a[0]) if a else "error")),
+    "find": b_find_n, "max": b_max, "sum": b_sum, "diff": b_diff, "trapz": b_trapz, "hann": b_hann,
     "floor_": None,
 }
 del BUILTINS["floor_"]
