@@ -285,6 +285,7 @@ def main():
                          % (2 * np_ * K * 8 / 1e9, (cfg.ntc // cfg.freq_samp) * np_ * 4 / 1e9)},
         "roofline": roof, "gpu_launches": launches, "clocks": clk,
     }
+    result["config"]["launch_groups"] = sess.ctx.last_batch()  # lanes per launch group
 
     if rank == 0 and not args.no_fp64:
         # plain FP64 GPU form, one station, and the FP32 error against it

@@ -32,7 +32,7 @@ EXPORTED = [
     "fd2d_forward1_green", "fd2d_forward2_correlation", "fd2d_noise_adjoint",
     "fd2d_ctx_set_timing", "fd2d_ctx_timing", "fd2d_contract_f32",
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
-    "fd2d_make_adjoint_sources",
+    "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch",
 ]
 MEAS_WAVEFORM_DIFFERENCE = 0
 MEAS_LOG_AMPLITUDE_RATIO = 1
@@ -86,6 +86,8 @@ def load(path: str = LIB_PATH):
         L.fd2d_ctx_synchronize.argtypes = [_vp]
         L.fd2d_ctx_kernel_launches.argtypes = [_vp]
         L.fd2d_ctx_kernel_launches.restype = _i64
+        L.fd2d_ctx_last_batch.argtypes = [_vp, ctypes.POINTER(ctypes.c_int32), _i32]
+        L.fd2d_ctx_last_batch.restype = _i32
         L.fd2d_last_error.argtypes = [_vp]
         L.fd2d_last_error.restype = ctypes.c_char_p
         L.fd2d_query_sizes.argtypes = [_cfgp, _i32, ctypes.POINTER(FD2DSizes)]
@@ -105,7 +107,8 @@ def load(path: str = LIB_PATH):
             _vp, _cfgp, _vp, _vp, _vp, _i32, _vp, _vp, ctypes.POINTER(_i64), _vp, _i32, _vp, _i32,
             _vp, _i32, _vp, _i32, _vp, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp]
         for name in EXPORTED:
-            if name not in ("fd2d_abi_version", "fd2d_ctx_kernel_launches", "fd2d_last_error"):
+            if name not in ("fd2d_abi_version", "fd2d_ctx_kernel_launches", "fd2d_last_error",
+                            "fd2d_ctx_last_batch"):
                 getattr(L, name).restype = _i32
         _lib = L
         return L
@@ -160,6 +163,13 @@ class Context:
     @property
     def kernel_launches(self) -> int:
         return int(self.L.fd2d_ctx_kernel_launches(self.h))
+
+    def last_batch(self):
+        """Lane counts of the launch groups of the last batch."""
+        cap = 4096
+        buf = (ctypes.c_int32 * cap)()
+        n = int(self.L.fd2d_ctx_last_batch(self.h, buf, cap))
+        return [int(buf[i]) for i in range(min(n, cap))]
 
     def set_timing(self, enable: bool):
         check(self.L.fd2d_ctx_set_timing(self.h, 1 if enable else 0), self.h)

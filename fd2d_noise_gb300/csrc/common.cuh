@@ -116,6 +116,7 @@ struct fd2d_ctx {
   // fork the jobs' loops into parallel branches of one captured graph
   std::string ws_prefix;
   int64_t mem_budget = 0;  // batch device-memory budget (0: 80 % of free memory)
+  std::vector<int32_t> last_lanes;  // lanes of each launch group of the last batch
   std::vector<cudaStream_t> side_streams;
   std::vector<cudaEvent_t> fork_events;
 };

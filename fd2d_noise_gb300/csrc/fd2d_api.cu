@@ -781,13 +781,20 @@ size_t job_footprint(const Geometry& g, int nr, int n_dist, bool host_inputs) {
   const size_t n_inj = g.ntc / g.fs;
   const size_t chunk = std::min<size_t>(n_inj, ((size_t)4 << 30) / plane);
   size_t b = 11 * plane + T * plane + 16 * np * g.K + 2 * (size_t)g.K * plane + chunk * plane;
-  b += (size_t)nr * (g.nt + g.ntc) * 8 + (size_t)1 << 20;
+  b += (size_t)nr * (g.nt + g.ntc) * 8 + ((size_t)1 << 20);
   if (host_inputs) b += np * 8 * (2 + n_dist) + (size_t)nr * g.ntc * 8;
   return b;
 }
 
 }  // namespace
 }  // namespace fd2d
+
+extern "C" int32_t fd2d_ctx_last_batch(const fd2d_ctx* ctx, int32_t* lanes, int32_t cap) {
+  if (!ctx) return 0;
+  const int32_t n = (int32_t)ctx->last_lanes.size();
+  for (int32_t i = 0; i < n && i < cap && lanes; ++i) lanes[i] = ctx->last_lanes[i];
+  return n;
+}
 
 extern "C" fd2d_status fd2d_ctx_set_memory_budget(fd2d_ctx* ctx, int64_t bytes) {
   if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
@@ -823,6 +830,7 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
   }
   int j0 = 0;
   fd2d_status st = FD2D_OK;
+  ctx->last_lanes.clear();
   while (j0 < n_jobs && st == FD2D_OK) {
     int j1 = j0 + 1;
     size_t used = B[j0].bytes;
@@ -846,6 +854,9 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
         lanes[gi].push_back(j);
       }
     }
+    if (lanes.empty())
+      for (int j = j0; j < j1; ++j) ctx->last_lanes.push_back(1);
+    for (const auto& l : lanes) ctx->last_lanes.push_back((int32_t)l.size());
     // group buffers: spectra, Green seismograms and correlations of all lanes,
     // lane after lane
     std::vector<double*> grp_gre(lanes.size()), grp_gim(lanes.size()), grp_sg(lanes.size()), grp_c(lanes.size());

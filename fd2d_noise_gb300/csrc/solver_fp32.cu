@@ -366,9 +366,10 @@ __global__ void k32_pitched(const double* a, double s, int nx, int nz, int P, fl
 
 // P planes of the field source: P_k = spec(k) * (sum_b M(k,b) sd_b) * (Xre_k + i*sign*Xim_k)
 // as 2K pitched float planes [Re P_0..Re P_{K-1}, Im P_0..Im P_{K-1}], plane stride ps.
-__global__ void k32_make_P(int K, int ncol, const double* M, const double* sd, const double* spec,
-                           const double* Xre, const double* Xim, double sign, int nx, int nz, int P,
-                           int64_t ps, float* Pl) {
+__global__ void k32_make_P(int K, int ncol, const double* __restrict__ M, const double* __restrict__ sd,
+                           const double* __restrict__ spec, const double* __restrict__ Xre,
+                           const double* __restrict__ Xim, double sign, int nx, int nz, int P, int64_t ps,
+                           float* __restrict__ Pl) {
   const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
   if (i >= P || j >= nz) return;
   const int64_t q = i + (int64_t)P * j;
@@ -379,12 +380,26 @@ __global__ void k32_make_P(int K, int ncol, const double* M, const double* sd, c
   const int64_t np = (int64_t)nx * nz, p = i + (int64_t)nx * j;
   double sdv[8];
   for (int b = 0; b < ncol && b < 8; ++b) sdv[b] = sd[p + np * b];
-  for (int k = 0; k < K; ++k) {
-    double dist = 0.0;
-    for (int b = 0; b < ncol; ++b) dist += M[k + (int64_t)K * b] * (b < 8 ? sdv[b] : sd[p + np * b]);
-    const double Rk = spec[k] * dist;
-    Pl[q + ps * k] = (float)(Rk * Xre[p + np * k]);
-    Pl[q + ps * (K + k)] = (float)(Rk * sign * (Xim ? Xim[p + np * k] : 0.0));
+  // groups of 4 frequencies: all 8 spectrum loads are issued before any store
+  constexpr int G = 4;
+  for (int k0 = 0; k0 < K; k0 += G) {
+    double xr[G], xi[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int k = k0 + g;
+      xr[g] = k < K ? Xre[p + np * k] : 0.0;
+      xi[g] = (k < K && Xim) ? Xim[p + np * k] : 0.0;
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int k = k0 + g;
+      if (k >= K) break;
+      double dist = 0.0;
+      for (int b = 0; b < ncol; ++b) dist += M[k + (int64_t)K * b] * (b < 8 ? sdv[b] : sd[p + np * b]);
+      const double Rk = spec[k] * dist;
+      Pl[q + ps * k] = (float)(Rk * xr[g]);
+      Pl[q + ps * (K + k)] = (float)(Rk * sign * xi[g]);
+    }
   }
 }
 

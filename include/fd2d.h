@@ -247,6 +247,10 @@ typedef struct fd2d_job {
 fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* jobs, int32_t n_jobs);
 /* Device-memory budget of a batch in bytes (0 = 80 % of the free memory). */
 fd2d_status fd2d_ctx_set_memory_budget(fd2d_ctx* ctx, int64_t bytes);
+/* Launch groups of the last batch on ctx: writes up to `cap` lane counts (jobs
+ * advanced by one launch per step, in execution order) and returns the number
+ * of groups. */
+int32_t fd2d_ctx_last_batch(const fd2d_ctx* ctx, int32_t* lanes, int32_t cap);
 
 /* ---- measurements ---------------------------------------------------------------
  * [misfit_n, adstf] = make_adjoint_sources(u, u_0, du, t, veldis, measurement,

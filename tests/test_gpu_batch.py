@@ -59,6 +59,11 @@ def test_batch_matches_single_solves(fd2d_lib, prec, budget):
     for rep in range(2):  # the second call replays the cached graphs
         sess.correlation_batch(dj)
         sess.ctx.synchronize()
+        groups = sess.ctx.last_batch()
+        if prec == "fp32" and not budget:
+            assert sorted(groups) == [1, 3], groups  # jobs 0, 2, 3 are lanes of one launch
+        else:
+            assert sum(groups) == len(jobs) and max(groups) == 1, groups
         for j, d in zip(jobs, dj):
             got = d["out"].cpu().numpy().reshape(j["rec"].shape[0], j["cfg"].ntc, order="F")
             ref = _single(j, prec)
