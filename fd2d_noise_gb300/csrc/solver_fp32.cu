@@ -37,7 +37,7 @@
 namespace fd2d {
 namespace {
 
-constexpr int TX = 32, TZ = 16, NT = 256;
+constexpr int TX = 32, TZ = 16, NT = 128;
 constexpr int MAX_BOX_SRC = 64;
 
 struct Grid32 {
@@ -67,7 +67,7 @@ struct Tile {
   static constexpr int O_MU = O_I + al(BH * BWa);
   static constexpr int O_U = O_MU + al(TZ * TX);
   static constexpr int O_VN = O_U + al(TZ * TX);
-  static constexpr int TOTAL = O_VN + al(BH * BWc);
+  static constexpr int TOTAL = O_VN + al(BH * BWa);  // new v on the 40-wide box (x from x0-4)
   static constexpr int BYTES = TOTAL * 4 + 128;  // + alignment slack
 };
 
@@ -123,16 +123,25 @@ __global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__
     if (S.has_u) bytes += 4u * TZ * TX;
     if (S.inj_plane >= 0) bytes += 4u * T::BH * T::BWa;
     mbar_expect_tx(&bar, bytes);
-    tma_load_3d(sm + T::O_SXY, &M.sxy, x0 - 8, bz0, lane, &bar);
-    tma_load_3d(sm + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, lane, &bar);
-    tma_load_3d(sm + T::O_V, &M.v, x0 - 4, bz0, lane, &bar);
+    // coefficient planes are not written by the time loop: their loads may
+    // overlap the end of the previous step (programmatic dependent launch)
     tma_load_3d(sm + T::O_B, &M.b, x0 - 4, bz0, lane, &bar);
     tma_load_3d(sm + T::O_T, &M.taper, x0 - 4, bz0, lane, &bar);
     tma_load_3d(sm + T::O_MU, &M.dtmu, x0, z0, lane, &bar);
+  }
+  // Everything below reads what the previous launch wrote, or writes what it
+  // read (ping-pong buffers): wait for it to complete.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (tid == 0) {
+    tma_load_3d(sm + T::O_SXY, &M.sxy, x0 - 8, bz0, lane, &bar);
+    tma_load_3d(sm + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, lane, &bar);
+    tma_load_3d(sm + T::O_V, &M.v, x0 - 4, bz0, lane, &bar);
     if (S.has_u) tma_load_3d(sm + T::O_U, &M.u, x0, z0, lane, &bar);
     if (S.inj_plane >= 0) tma_load_3d(sm + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, &bar);
   }
-  // point sources of the box (global loads overlap the TMA traffic)
+  // point sources of the box (global loads overlap the TMA traffic); the box
+  // of new v is 40 columns wide from x0-4 (4-aligned for vector loads)
+  const int vx0 = x0 - 4;
   int2 my_src = make_int2(-1 << 30, -1 << 30);
   float my_amp = 0.f;
   if (tid < S.nsrc) {
@@ -142,20 +151,20 @@ __global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__
   __syncthreads();  // barrier initialised, s_nsrc cleared
   {
     const int gx = my_src.x, gz = my_src.y;
-    if (gx >= bx0 && gx < bx0 + T::BWc && gz >= bz0 && gz < bz0 + T::BH) {
+    if (gx >= vx0 && gx < vx0 + T::BWa && gz >= bz0 && gz < bz0 + T::BH) {
       const int slot = atomicAdd(&s_nsrc, 1);
       if (slot < MAX_BOX_SRC) {
-        s_src[slot] = (gz - bz0) * T::BWc + (gx - bx0);
+        s_src[slot] = (gz - bz0) * T::BWa + (gx - vx0);
         s_amp[slot] = my_amp;
       }
     }
   }
   for (int k = tid + NT; k < S.nsrc; k += NT) {  // more sources than threads: rare
     const int2 q = src_xy[k];
-    if (q.x >= bx0 && q.x < bx0 + T::BWc && q.y >= bz0 && q.y < bz0 + T::BH) {
+    if (q.x >= vx0 && q.x < vx0 + T::BWa && q.y >= bz0 && q.y < bz0 + T::BH) {
       const int slot = atomicAdd(&s_nsrc, 1);
       if (slot < MAX_BOX_SRC) {
-        s_src[slot] = (q.y - bz0) * T::BWc + (q.x - bx0);
+        s_src[slot] = (q.y - bz0) * T::BWa + (q.x - vx0);
         s_amp[slot] = amp ? (float)amp[k] : S.amp_const;
       }
     }
@@ -176,93 +185,180 @@ __global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__
   const float* s_u = sm + T::O_U;
   float* s_vn = sm + T::O_VN;
   const bool inj = S.inj_plane >= 0;
+  constexpr int W = T::BWa;  // 40: row stride of the box regions
 
-  // ---- new v on the tile plus its halo ring -----------------------------------------
-  // Threads own a column (tx) and march over rows; the 2R-1 right-fringe
-  // columns of the box are a second, short pass.
-  constexpr int NR = NT / TX, FW = T::BWc - TX;
-  const int tx0 = tid % TX, ty0 = tid / TX;
-  auto vnew = [&](int rr, int cc) {
-    const int e = rr * T::BWc + cc;
-    const int gx = bx0 + cc, gz = bz0 + rr;
-    float ds = 0.f;
-    if (gx >= R && gx <= nx - R - 1) {
-      const float* row = s_sxy + rr * T::SXWa + cc + 8 - R;  // row[m] = sxy(gx+m-1), row[1-m] = sxy(gx-m)
-      float acc = 0.f;
+  // ---- new v on the box: each thread a 4-wide, 2-tall block ------------------------
+  // DS = div_s(sxy, szy) (+ sources) (+ injection); v = (v + DS*dt/rho)*taper.
+  // Sums are formed in the same order as the scalar form (m = 1..R).
+  {
+    constexpr int NQ = W / 4, NRB = (T::BH + 1) / 2;
+    if (tid < NQ * NRB) {
+      const int q = tid % NQ, r0 = 2 * (tid / NQ);
+      const int c0 = 4 * q;  // box column of element 0; global x = vx0 + c0 + e
+      float xs[2][12];       // sxy columns c0 .. c0+11 (x from x0-8 = box column - 4)
+      float zs[2 * R + 1][4];
 #pragma unroll
-      for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (row[m] - row[1 - m]);
-      ds = acc * G.inv_dx;
-    }
-    if (gz >= R && gz <= nz - R - 1) {
-      const float* col = s_szy + (rr + R) * T::BWa + cc + 5 - R;  // col[(m-1)W] = szy(gz+m-1)
-      float acc = 0.f;
+      for (int k = 0; k < 2; ++k) {
+        const int rr = min(r0 + k, T::BH - 1);
+        const float4* rowp = reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + c0);
 #pragma unroll
-      for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (col[(m - 1) * T::BWa] - col[-m * T::BWa]);
-      ds += acc * G.inv_dz;
-    }
-    if (nbs) {
-      if (nbs <= MAX_BOX_SRC) {
-        for (int q = 0; q < nbs; ++q)
-          if (s_src[q] == e) ds += s_amp[q];
-      } else {
-        for (int q = 0; q < S.nsrc; ++q) {
-          const int2 w = src_xy[q];
-          if (w.x == gx && w.y == gz) ds += amp ? (float)amp[q] : S.amp_const;
+        for (int h = 0; h < 3; ++h) {
+          const float4 f = rowp[h];
+          xs[k][4 * h] = f.x; xs[k][4 * h + 1] = f.y; xs[k][4 * h + 2] = f.z; xs[k][4 * h + 3] = f.w;
         }
       }
+#pragma unroll
+      for (int k = 0; k < 2 * R + 1; ++k) {
+        // szy row r0 + k holds szy(gz0 + k - R) for gz0 = global z of row r0
+        const int rr = min(r0 + k, T::SZH - 1);
+        const float4 f = *reinterpret_cast<const float4*>(s_szy + rr * W + c0);
+        zs[k][0] = f.x; zs[k][1] = f.y; zs[k][2] = f.z; zs[k][3] = f.w;
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int rr = r0 + k;
+        if (rr >= T::BH) break;
+        const int gz = bz0 + rr;
+        const bool zin = gz >= R && gz <= nz - R - 1;
+        const float4 v4 = *reinterpret_cast<const float4*>(s_v + rr * W + c0);
+        const float4 b4 = *reinterpret_cast<const float4*>(s_b + rr * W + c0);
+        const float4 t4 = *reinterpret_cast<const float4*>(s_t + rr * W + c0);
+        float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (inj) i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
+        const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
+        const float tt[4] = {t4.x, t4.y, t4.z, t4.w}, ii[4] = {i4.x, i4.y, i4.z, i4.w};
+        float out[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int gx = vx0 + c0 + e;
+          float ds = 0.f;
+          if (gx >= R && gx <= nx - R - 1) {
+            // sxy(gx + m - 1) is xs[k][e + 3 + m], sxy(gx - m) is xs[k][e + 4 - m]
+            float acc = 0.f;
+#pragma unroll
+            for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (xs[k][e + 3 + m] - xs[k][e + 4 - m]);
+            ds = acc * G.inv_dx;
+          }
+          if (zin) {
+            // szy(gz + m - 1) is zs[k + R + m - 1], szy(gz - m) is zs[k + R - m]
+            float acc = 0.f;
+#pragma unroll
+            for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (zs[k + R + m - 1][e] - zs[k + R - m][e]);
+            ds += acc * G.inv_dz;
+          }
+          if (nbs) {
+            const int idx = rr * W + c0 + e;
+            if (nbs <= MAX_BOX_SRC) {
+              for (int qq = 0; qq < nbs; ++qq)
+                if (s_src[qq] == idx) ds += s_amp[qq];
+            } else {
+              for (int qq = 0; qq < S.nsrc; ++qq) {
+                const int2 w = src_xy[qq];
+                if (w.x == gx && w.y == gz) ds += amp ? (float)amp[qq] : S.amp_const;
+              }
+            }
+          }
+          if (inj) ds += ii[e];
+          out[e] = (vv[e] + ds * bb[e]) * tt[e];
+        }
+        *reinterpret_cast<float4*>(s_vn + rr * W + c0) = make_float4(out[0], out[1], out[2], out[3]);
+      }
     }
-    const int bo = rr * T::BWa + cc + 5 - R;
-    if (inj) ds += s_i[bo];
-    s_vn[e] = (s_v[bo] + ds * s_b[bo]) * s_t[bo];
-  };
-  for (int rr = ty0; rr < T::BH; rr += NR) vnew(rr, tx0);
-  for (int f = tid; f < FW * T::BH; f += NT) {
-    const int rr = f / FW;
-    vnew(rr, TX + f - rr * FW);
   }
   __syncthreads();
 
-  // ---- stress, displacement and outputs on the tile -----------------------------------
-  const int tx = tx0;
+  // ---- stress, displacement and outputs: each thread a 4-wide row segment -----------
+  {
+    constexpr int NQ2 = TX / 4;  // 8 quads per row, TZ rows: NQ2 * TZ == NT
+    const int q = tid % NQ2, tz = tid / NQ2;
+    const int j = z0 + tz;
+    const int i0 = x0 + 4 * q;
+    if (tz < TZ && j < nz && i0 < nx) {
+      const int rr = tz + R - 1;  // box row of output row j
+      const int cv = 4 + 4 * q;   // box column of element 0
+      // vx = box columns cv-4 .. cv+7: v(i) is vx[e + 4], v(i + m) is vx[e + m + 4],
+      // v(i - m + 1) is vx[e - m + 5]
+      float vx[12];
+      {
+        const float4* rowp = reinterpret_cast<const float4*>(s_vn + rr * W + cv - 4);
 #pragma unroll
-  for (int tz = ty0; tz < TZ; tz += NR) {
-    const int e = tz * TX + tx;
-    const int i = x0 + tx, j = z0 + tz;
-    if (i >= nx || j >= nz) continue;
-    const int64_t p = lo + i + P * j;
-    const int rr = tz + R - 1, cc = tx + R - 1;
-    const float* vrow = s_vn + rr * T::BWc + cc;
-    const float vn = vrow[0];
-    if (S.snap_pre) S.snap_pre[i + nx * j] = S.snap_pre_u ? s_u[e] : s_v[rr * T::BWa + tx + 4];
-    S.vo[p] = vn;
-    const float dtmu = s_mu[e];
-    if (i <= nx - 2) {
-      float nw = s_sxy[rr * T::SXWa + tx + 8];
-      if (i >= R - 1 && i <= nx - R - 1) {
-        float acc = 0.f;
-#pragma unroll
-        for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (vrow[m] - vrow[1 - m]);
-        nw += dtmu * (acc * G.inv_dx);
+        for (int h = 0; h < 3; ++h) {
+          const float4 f = rowp[h];
+          vx[4 * h] = f.x; vx[4 * h + 1] = f.y; vx[4 * h + 2] = f.z; vx[4 * h + 3] = f.w;
+        }
       }
-      S.sxyo[p] = nw;
-    }
-    if (j <= nz - 2) {
-      float nw = s_szy[(tz + 2 * R - 1) * T::BWa + tx + 4];
-      if (j >= R - 1 && j <= nz - R - 1) {
-        float acc = 0.f;
+      float vz[2 * R][4];  // box rows rr - R + 1 .. rr + R
 #pragma unroll
-        for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (vrow[m * T::BWc] - vrow[(1 - m) * T::BWc]);
-        nw += dtmu * (acc * G.inv_dz);
+      for (int k = 0; k < 2 * R; ++k) {
+        const float4 f = *reinterpret_cast<const float4*>(s_vn + (rr - R + 1 + k) * W + cv);
+        vz[k][0] = f.x; vz[k][1] = f.y; vz[k][2] = f.z; vz[k][3] = f.w;
       }
-      S.szyo[p] = nw;
+      const float4 mu4 = *reinterpret_cast<const float4*>(s_mu + tz * TX + 4 * q);
+      const float4 sx4 = *reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + 8 + 4 * q);
+      const float4 sz4 = *reinterpret_cast<const float4*>(s_szy + (tz + 2 * R - 1) * W + 4 + 4 * q);
+      float4 u4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (S.has_u) u4 = *reinterpret_cast<const float4*>(s_u + tz * TX + 4 * q);
+      const float mu[4] = {mu4.x, mu4.y, mu4.z, mu4.w}, sxo[4] = {sx4.x, sx4.y, sx4.z, sx4.w};
+      const float szo[4] = {sz4.x, sz4.y, sz4.z, sz4.w}, uo[4] = {u4.x, u4.y, u4.z, u4.w};
+      const bool zin = j >= R - 1 && j <= nz - R - 1;
+      float nsx[4], nsz[4], nu[4], vn[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = i0 + e;
+        vn[e] = vx[e + 4];
+        float nw = sxo[e];
+        if (i >= R - 1 && i <= nx - R - 1) {
+          float acc = 0.f;
+#pragma unroll
+          for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (vx[e + m + 4] - vx[e - m + 5]);
+          nw += mu[e] * (acc * G.inv_dx);
+        }
+        nsx[e] = nw;
+        nw = szo[e];
+        if (zin) {
+          float acc = 0.f;
+#pragma unroll
+          for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (vz[R - 1 + m][e] - vz[R - m][e]);
+          nw += mu[e] * (acc * G.inv_dz);
+        }
+        nsz[e] = nw;
+        nu[e] = S.has_u ? uo[e] + vn[e] * G.dt : vn[e];
+      }
+      const int64_t p = lo + i0 + (int64_t)P * j;
+      if (i0 + 3 < nx) {
+        // whole quad inside the grid: vector stores
+        *reinterpret_cast<float4*>(S.vo + p) = make_float4(vn[0], vn[1], vn[2], vn[3]);
+        if (i0 + 3 <= nx - 2) {
+          *reinterpret_cast<float4*>(S.sxyo + p) = make_float4(nsx[0], nsx[1], nsx[2], nsx[3]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
+        }
+        if (j <= nz - 2) *reinterpret_cast<float4*>(S.szyo + p) = make_float4(nsz[0], nsz[1], nsz[2], nsz[3]);
+        if (S.has_u) *reinterpret_cast<float4*>(S.uo + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
+        if (S.snap_dft) *reinterpret_cast<float4*>(S.snap_dft + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (i0 + e >= nx) break;
+          S.vo[p + e] = vn[e];
+          if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
+          if (j <= nz - 2) S.szyo[p + e] = nsz[e];
+          if (S.has_u) S.uo[p + e] = nu[e];
+          if (S.snap_dft) S.snap_dft[p + e] = nu[e];
+        }
+      }
+      if (S.snap_pre) {
+        const float* old = S.snap_pre_u ? s_u + tz * TX + 4 * q : s_v + rr * W + cv;
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (i0 + e < nx) S.snap_pre[i0 + e + nx * j] = old[e];
+      }
     }
-    float x = vn;
-    if (S.has_u) {
-      x = s_u[e] + vn * G.dt;
-      S.uo[p] = x;
-    }
-    if (S.snap_dft) S.snap_dft[p] = x;
   }
+  // the next step may start its launch and prologue now
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   if (S.nrec) {
     __syncthreads();
     const int2* rec_xy = S.rec_xy + (int64_t)lane * S.nrec;
@@ -435,9 +531,22 @@ struct Run {
   int64_t lanes_ps() const { return (int64_t)S * ps; }
 };
 
+// Step launches carry the programmatic-stream-serialization attribute: a step
+// may be scheduled while the previous one drains; k32_step waits for it with
+// griddepcontrol.wait before touching the fields.
 template <int R>
 void launch_step_r(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
-  k32_step<R><<<r.sgrid, NT, Tile<R>::BYTES, ctx->stream>>>(r.G, r.maps[par], s);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = r.sgrid;
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = Tile<R>::BYTES;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k32_step<R>, r.G, r.maps[par], s);
 }
 
 // Opt the step kernels in to their dynamic shared memory (once, before any capture).
