@@ -87,7 +87,8 @@ def eval_objective_and_gradient(mu, rho, spectrum, source_dist, ref_stat, array,
         zero = 0.0 * c_ref
         j_s, ad_s = be.measure(c, c_ref, zero, t, veldis, measurement_source, "1st")
         j_t, ad_t = be.measure(c, c_ref, zero, t, veldis, measurement_structure, "1st")
-        j_n = (1.0 - weighting) * np.asarray(j_s) + weighting * np.asarray(j_t)
+        with np.errstate(invalid="ignore"):  # 0 * inf when the data are zero, as in MATLAB
+            j_n = (1.0 - weighting) * np.asarray(j_s) + weighting * np.asarray(j_t)
         adstf = (1.0 - weighting) * np.asarray(ad_s) + weighting * np.asarray(ad_t)
         j += float(np.sum(j_n))
         if only_objective:
@@ -107,3 +108,95 @@ def eval_objective_and_gradient(mu, rho, spectrum, source_dist, ref_stat, array,
         k = np.asarray(K1, dtype=np.float64) + np.asarray(K2, dtype=np.float64)
         grad = k if grad is None else grad + k
     return j, grad, c_all
+
+
+def _nonzero(a) -> bool:
+    return a is not None and bool(np.any(np.asarray(a) != 0))
+
+
+def eval_hessian_vector_product(mu, rho, spectrum, source_dist, ref_stat, array, c_data, t, dmu,
+                                source_dist_pert=None, *, cfg, type="structure", veldis="dis",
+                                measurement_source="log_amplitude_ratio",
+                                measurement_structure="log_amplitude_ratio", weighting=0.5,
+                                precision="fp32", device=0, backend: Optional[Backend] = None):
+    """Hessian applied to (source_dist_pert, dmu) in parameter space, summed over
+    stations: inversion/optlib_callback_fct/eval_hessian_vector_product.m:45-184
+    (the chain Green, Born Green, correlation, Born correlation, first- and
+    second-order adjoint sources, then the YELLOW mode-13, GRAY mode-11, BLACK
+    mode-12 and RED mode-10 adjoint runs).  Born runs consume stored fields every
+    step, so the configuration needs fw_nth == 1.  Returns nx-by-nz-by-planes
+    FP64 (source planes, then mu)."""
+    if type not in ("source", "structure", "joint"):
+        raise ValueError("type must be 'source', 'structure' or 'joint'")
+    if cfg.fw_nth != 1:
+        raise ValueError("the Hessian-vector product needs fw_nth == 1 (Born runs read every step)")
+    be = backend or gpu_backend(cfg, precision, device)
+    ref_stat = np.asarray(ref_stat, dtype=np.float64).reshape(-1, 2)
+    t = np.asarray(t, dtype=np.float64).ravel()
+    nt = t.size
+    n_ref = ref_stat.shape[0]
+    n_rec = np.asarray(array).shape[0] - 1
+    c_data = np.asarray(c_data, dtype=np.float64)
+    has_dmu = _nonzero(dmu)
+    has_ds = _nonzero(source_dist_pert)
+    H = None
+    for i in range(n_ref):
+        src = ref_stat[i:i + 1]
+        rec = receivers_of(array, src)
+        data = c_data[i * n_rec:(i + 1) * n_rec]
+        G_fft, G, _ = be.forward1(mu, rho, src, rec, 1, None, None)
+        dG_fft, dG = 0.0, None
+        if has_dmu:
+            dG_fft, dG, _ = be.forward1(mu, rho, src, rec, 5, dmu, G)
+        c_ref, C = be.correlation(mu, rho, G_fft, spectrum, source_dist, rec, 1, None, None)
+        c_ref = np.asarray(c_ref).reshape(n_rec, nt)
+        c_pert = np.zeros((n_rec, nt))
+        dC = None
+        if has_dmu:
+            c1, dC = be.correlation(mu, rho, dG_fft, spectrum, source_dist, rec, 1, dmu, C)
+            c_pert = c_pert + np.asarray(c1).reshape(n_rec, nt)
+        if has_ds:
+            c2, dC2 = be.correlation(mu, rho, G_fft, spectrum, source_dist_pert, rec, 1, None, None)
+            c_pert = c_pert + np.asarray(c2).reshape(n_rec, nt)
+            dC = dC2 if dC is None else np.asarray(dC) + np.asarray(dC2)
+
+        def adstf(order):
+            _, a_s = be.measure(c_ref, data, c_pert, t, veldis, measurement_source, order)
+            _, a_t = be.measure(c_ref, data, c_pert, t, veldis, measurement_structure, order)
+            return ((1.0 - weighting) * np.asarray(a_s) + weighting * np.asarray(a_t)).astype(np.complex128)
+
+        a1, a2 = adstf("1st"), adstf("2nd")
+        planes = None
+        K1 = K2 = K4 = 0.0
+        u_dag = None
+        if type != "source":
+            # YELLOW: u_dagger
+            dG_in = dG_fft if has_dmu else None
+            K1, uT, u_dag, _ = be.adjoint(mu, rho, dC, a1, rec, None, spectrum, None, dG_in, 13, None, None)
+            K1 = np.array(K1, dtype=np.float64)
+            if type == "structure":
+                K1[:, :, :-1] = 0.0
+            p = None
+            if has_dmu:  # GRAY: p (dmu dmu)
+                K2, _, p, _ = be.adjoint(mu, rho, dG, uT, rec, None, spectrum, source_dist, None, 11, None, None)
+                K2 = np.asarray(K2, dtype=np.float64)
+            if type == "joint" and has_ds:  # GRAY: p (ds dmu)
+                K2b, _, pb, _ = be.adjoint(mu, rho, G, uT, rec, None, spectrum, source_dist_pert, None, 11, None,
+                                           None)
+                K2 = K2 + np.asarray(K2b, dtype=np.float64)
+                p = pb if p is None else np.asarray(p) + np.asarray(pb)
+        # BLACK: k
+        K3, kT, _, _ = be.adjoint(mu, rho, C, a2, rec, None, spectrum, None, G_fft, 12, dmu if has_dmu else None,
+                                  u_dag)
+        K3 = np.array(K3, dtype=np.float64)
+        if type == "source":
+            K3[:, :, -1] = 0.0
+        elif type == "structure":
+            K3[:, :, :-1] = 0.0
+        if type != "source":  # RED: w and l
+            K4, _, _, _ = be.adjoint(mu, rho, G, kT, rec, None, spectrum, source_dist, None, 10,
+                                     dmu if has_dmu else None, p)
+            K4 = np.asarray(K4, dtype=np.float64)
+        h = K1 + K2 + K3 + K4
+        H = h if H is None else H + h
+    return H

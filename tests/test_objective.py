@@ -101,3 +101,50 @@ def test_gpu_gradient_matches_finite_differences(fd2d_lib):
     # FP32: the misfit difference at h=1e-4 is near FP32 resolution; h=1e-2 carries it
     _, _, errs32 = fd_check(cfg, p, None, "fp32", [1e-2])
     assert max(errs32) < 2e-2, errs32
+
+
+def hvp(cfg, p, c_data, backend=None, precision="fp64", type="structure", ds=None):
+    from fd2d_noise_gb300.objective import eval_hessian_vector_product
+    return eval_hessian_vector_product(p["mu0"], p["rho"], p["spec"], p["sd"], p["ref"], p["arr"], c_data, p["t"],
+                                       p["dmu"], ds, cfg=cfg, weighting=1.0, type=type, backend=backend,
+                                       precision=precision)
+
+
+def probe(cfg):
+    nx = cfg.nx
+    X, Z = np.meshgrid(np.linspace(0, cfg.Lx, nx), np.linspace(0, cfg.Lz, nx), indexing="ij")
+    return 4.8e10 * np.exp(-((X - 0.5e6) ** 2 + (Z - 0.45e6) ** 2) / 1.5e5 ** 2)
+
+
+def test_oracle_hessian_matches_gradient_differences():
+    """inversion/optlib/optlib_check_hessian.m:66-116: (H dm1)' dm2 against
+    ((g(m + h dm1) - g(m)) / h)' dm2."""
+    cfg = cfg4(fw=1)
+    p = problem(cfg)
+    be = oracle_backend(cfg)
+    _, _, c_data = run(cfg, p, p["mu_true"], np.zeros((3, cfg.ntc)), be, only=True)
+    H = hvp(cfg, p, c_data, be)
+    dm2 = probe(cfg)
+    pred = float(np.sum(H[:, :, -1] * dm2))
+    _, g0, _ = run(cfg, p, p["mu0"], c_data, be)
+    h = 1e-3
+    _, g1, _ = run(cfg, p, p["mu0"] + h * p["dmu"], c_data, be)
+    fd = float(np.sum((g1[:, :, -1] - g0[:, :, -1]) / h * dm2))
+    assert abs(fd - pred) <= 1e-2 * abs(fd), (fd, pred)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("type", ["structure", "joint"])
+def test_gpu_hessian_matches_oracle(fd2d_lib, type):
+    cfg = cfg4(fw=1)
+    p = problem(cfg)
+    be = oracle_backend(cfg)
+    _, _, c_data = run(cfg, p, p["mu_true"], np.zeros((3, cfg.ntc)), be, only=True)
+    ds = 0.1 * p["sd"] if type == "joint" else None
+    Hr = hvp(cfg, p, c_data, be, type=type, ds=ds)
+    for prec, tol in (("fp64", 1e-10), ("fp32", 1e-3)):
+        H = hvp(cfg, p, c_data, precision=prec, type=type, ds=ds)
+        for q in range(H.shape[2]):
+            n = np.linalg.norm(Hr[:, :, q])
+            if n > 0:
+                assert np.linalg.norm(H[:, :, q] - Hr[:, :, q]) <= tol * n, (prec, q)
