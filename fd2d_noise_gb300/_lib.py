@@ -32,7 +32,7 @@ EXPORTED = [
     "fd2d_forward1_green", "fd2d_forward2_correlation", "fd2d_noise_adjoint",
     "fd2d_ctx_set_timing", "fd2d_ctx_timing", "fd2d_contract_f32",
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
-    "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch",
+    "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch", "fd2d_ctx_release", "fd2d_ctx_workspace_bytes",
 ]
 MEAS_WAVEFORM_DIFFERENCE = 0
 MEAS_LOG_AMPLITUDE_RATIO = 1
@@ -88,6 +88,9 @@ def load(path: str = LIB_PATH):
         L.fd2d_ctx_kernel_launches.restype = _i64
         L.fd2d_ctx_last_batch.argtypes = [_vp, ctypes.POINTER(ctypes.c_int32), _i32]
         L.fd2d_ctx_last_batch.restype = _i32
+        L.fd2d_ctx_workspace_bytes.argtypes = [_vp]
+        L.fd2d_ctx_workspace_bytes.restype = _i64
+        L.fd2d_ctx_release.argtypes = [_vp, ctypes.POINTER(_i64)]
         L.fd2d_last_error.argtypes = [_vp]
         L.fd2d_last_error.restype = ctypes.c_char_p
         L.fd2d_query_sizes.argtypes = [_cfgp, _i32, ctypes.POINTER(FD2DSizes)]
@@ -108,7 +111,7 @@ def load(path: str = LIB_PATH):
             _vp, _i32, _vp, _i32, _vp, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp]
         for name in EXPORTED:
             if name not in ("fd2d_abi_version", "fd2d_ctx_kernel_launches", "fd2d_last_error",
-                            "fd2d_ctx_last_batch"):
+                            "fd2d_ctx_last_batch", "fd2d_ctx_workspace_bytes"):
                 getattr(L, name).restype = _i32
         _lib = L
         return L
@@ -163,6 +166,16 @@ class Context:
     @property
     def kernel_launches(self) -> int:
         return int(self.L.fd2d_ctx_kernel_launches(self.h))
+
+    def release(self) -> int:
+        """Frees the workspace and cached graphs; returns the bytes freed."""
+        b = _i64(0)
+        check(self.L.fd2d_ctx_release(self.h, ctypes.byref(b)), self.h)
+        return int(b.value)
+
+    @property
+    def workspace_bytes(self) -> int:
+        return int(self.L.fd2d_ctx_workspace_bytes(self.h))
 
     def last_batch(self):
         """Lane counts of the launch groups of the last batch."""

@@ -24,6 +24,10 @@ fd2d_status set_error(fd2d_ctx* ctx, fd2d_status s, const std::string& msg) {
   return s;
 }
 
+// Workspace buffers come from the device's stream-ordered memory pool
+// (cudaMallocAsync / cudaFreeAsync on the context's stream): no implicit
+// device-wide synchronisation, so contexts working concurrently on other
+// streams are not stalled when one of them grows or releases its buffers.
 fd2d_status workspace(fd2d_ctx* ctx, const char* name_in, size_t bytes, void** out) {
   const std::string key = ctx->ws_prefix + name_in;
   const char* name = key.c_str();
@@ -33,12 +37,11 @@ fd2d_status workspace(fd2d_ctx* ctx, const char* name_in, size_t bytes, void** o
         *out = kv.second.ptr;
         return FD2D_OK;
       }
-      // grow: the stream must not be using the old buffer any more
-      cudaStreamSynchronize(ctx->stream);
-      cudaFree(kv.second.ptr);
+      // grow: stream-ordered, after the work already queued that uses the old buffer
+      cudaFreeAsync(kv.second.ptr, ctx->stream);
       kv.second.ptr = nullptr;
       kv.second.bytes = 0;
-      cudaError_t e = cudaMalloc(&kv.second.ptr, bytes);
+      cudaError_t e = cudaMallocAsync(&kv.second.ptr, bytes, ctx->stream);
       if (e != cudaSuccess) {
         cudaGetLastError();
         return set_error(ctx, FD2D_ERR_OOM, std::string("cudaMalloc(") + name + ", " +
@@ -51,7 +54,7 @@ fd2d_status workspace(fd2d_ctx* ctx, const char* name_in, size_t bytes, void** o
     }
   }
   DevBuf b;
-  cudaError_t e = cudaMalloc(&b.ptr, bytes);
+  cudaError_t e = cudaMallocAsync(&b.ptr, bytes, ctx->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_error(ctx, FD2D_ERR_OOM, std::string("cudaMalloc(") + name + ", " +
@@ -76,7 +79,7 @@ fd2d_status workspace_tag(fd2d_ctx* ctx, const char* name, size_t bytes, uint64_
 }
 
 void free_workspace(fd2d_ctx* ctx) {
-  for (auto& kv : ctx->bufs) cudaFree(kv.second.ptr);
+  for (auto& kv : ctx->bufs) cudaFreeAsync(kv.second.ptr, ctx->stream);
   ctx->bufs.clear();
 }
 
@@ -368,6 +371,15 @@ fd2d_status fd2d_ctx_create(int32_t device, int32_t precision, fd2d_ctx** out) {
     return set_error(nullptr, FD2D_ERR_ARG, "precision must be FD2D_PREC_FP64 or FD2D_PREC_FP32");
   e = cudaSetDevice(device);
   if (e != cudaSuccess) return set_error(nullptr, FD2D_ERR_CUDA, cudaGetErrorString(e));
+  {
+    // keep freed workspace in the device's pool for reuse by any context
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
   fd2d_ctx* c = new fd2d_ctx();
   c->device = device;
   c->precision = precision;
@@ -394,6 +406,7 @@ fd2d_status fd2d_ctx_destroy(fd2d_ctx* ctx) {
   for (auto s : ctx->side_streams) cudaStreamDestroy(s);
   for (auto e : ctx->fork_events) cudaEventDestroy(e);
   free_workspace(ctx);
+  cudaStreamSynchronize(ctx->stream);
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -401,14 +414,33 @@ fd2d_status fd2d_ctx_destroy(fd2d_ctx* ctx) {
   return FD2D_OK;
 }
 
+fd2d_status fd2d_ctx_release(fd2d_ctx* ctx, int64_t* bytes) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  FD2D_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  int64_t b = 0;
+  for (const auto& kv : ctx->bufs) b += (int64_t)kv.second.bytes;
+  if (bytes) *bytes = b;
+  for (auto& kv : ctx->graphs) destroy_graph(kv.second);
+  ctx->graphs.clear();
+  free_workspace(ctx);
+  return FD2D_OK;
+}
+
+int64_t fd2d_ctx_workspace_bytes(const fd2d_ctx* ctx) {
+  if (!ctx) return 0;
+  int64_t b = 0;
+  for (const auto& kv : ctx->bufs) b += (int64_t)kv.second.bytes;
+  return b;
+}
+
 fd2d_status fd2d_ctx_set_stream(fd2d_ctx* ctx, void* stream) {
   if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
   cudaSetDevice(ctx->device);
+  // workspace is stream-ordered on the current stream: drain it before switching
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (stream) {
-    if (ctx->own_stream && ctx->stream) {
-      cudaStreamSynchronize(ctx->stream);
-      cudaStreamDestroy(ctx->stream);
-    }
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     ctx->stream = (cudaStream_t)stream;
     ctx->own_stream = false;
   } else if (!ctx->own_stream) {
@@ -826,6 +858,15 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
   if (budget == 0) {
     size_t free_b = 0, total_b = 0;
     FD2D_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+    // memory the stream-ordered pool holds but no buffer uses is free for us too
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) {
+      uint64_t reserved = 0, used = 0;
+      if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+          cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+        free_b += (size_t)(reserved - used);
+    }
+    cudaGetLastError();
     budget = free_b / 10 * 8;
   }
   int j0 = 0;

@@ -1,0 +1,289 @@
+"""Continuous-batching request loop on one GPU.
+
+Requests of three kinds arrive at any time:
+
+  'correlation'  the Green function and correlation wavefield of each of its
+                 reference stations (code/calculate_data.m:189-202) -- one
+                 fd2d_correlation_batch call, stations of one grid as lanes;
+  'kernel'       misfit and structure kernel summed over its stations
+                 (inversion/optlib_callback_fct/eval_objective_and_gradient.m);
+  'hvp'          Hessian-vector product along dmu
+                 (inversion/optlib_callback_fct/eval_hessian_vector_product.m).
+
+The server owns ``slots`` worker threads, each with its own libfd2d context
+(own CUDA stream, workspace and cached graphs).  A queued request is admitted
+when a slot is idle and its device-memory footprint fits in what the admitted
+requests leave of the budget; it then runs on its slot's stream while the
+other slots' requests keep running, so their kernels overlap on the GPU.  The
+queue is served in arrival order, except that a request that fits may pass a
+head request that does not, at most ``max_bypass`` times per head request (no
+starvation).  A request larger than the whole budget fails at submission.
+After each request the slot releases its workspace back to the device pool.
+
+Results are the same as those of the request run alone: every request runs on
+its own stream with its own buffers, and the kernels are deterministic.
+"""
+from __future__ import annotations
+
+import threading
+import time
+from collections import deque
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+from typing import Callable, Optional
+
+import numpy as np
+
+from .config import Config, n_fw_corr, n_fw_green
+
+
+class AdmissionError(RuntimeError):
+    pass
+
+
+@dataclass
+class Request:
+    kind: str                       # 'correlation' | 'kernel' | 'hvp'
+    cfg: Config
+    mu: np.ndarray
+    rho: np.ndarray
+    spectrum: np.ndarray
+    source_dist: np.ndarray
+    ref_stat: np.ndarray            # n_ref-by-2
+    receivers: np.ndarray           # correlation: nr-by-2; kernel / hvp: the station array
+    c_data: Optional[np.ndarray] = None
+    dmu: Optional[np.ndarray] = None
+    measurement: str = "log_amplitude_ratio"
+    weighting: float = 1.0
+    arrival: float = field(default_factory=time.perf_counter)
+
+    def gpt(self) -> int:
+        """Grid-point updates of the request (Green + correlation + adjoint runs)."""
+        c = self.cfg
+        n_ref = np.asarray(self.ref_stat).reshape(-1, 2).shape[0]
+        runs = {"correlation": c.nt + c.ntc, "kernel": c.nt + c.ntc + c.ntc + c.nt,
+                "hvp": 2 * c.nt + 2 * c.ntc + 4 * c.ntc}[self.kind]
+        return c.npts * runs * n_ref
+
+
+def footprint(req: Request) -> int:
+    """Upper bound of the device bytes a request holds while it runs (FP32
+    form): per-lane fields and coefficient planes, the DFT snapshot chunk, FP64
+    spectra, injection planes, and for kernel / Hessian requests the staged
+    snapshot stacks of the Green and correlation runs."""
+    c = req.cfg
+    P = (c.nx + 31) // 32 * 32
+    plane = ((P * c.nz + 127) // 128 * 128) * 4
+    np_, K = c.npts, c.n_sample
+    n_ref = np.asarray(req.ref_stat).reshape(-1, 2).shape[0]
+    nr = max(np.asarray(req.receivers).reshape(-1, 2).shape[0], 1)
+    n_dft = min(c.nt // max(c.freq_samp, 1) + 1, 1024, (2 << 30) // plane)
+    n_inj = min(c.ntc // max(c.freq_samp, 1), (4 << 30) // plane)
+    per = (11 * plane + n_dft * plane + 16 * np_ * K + 2 * K * plane + n_inj * plane
+           + 8 * nr * (c.nt + c.ntc) + 8 * np_ * (3 + np.asarray(req.source_dist).size // max(np_, 1)))
+    if req.kind == "correlation":
+        return int(n_ref * per + (1 << 20))
+    snaps = (n_fw_green(c) + n_fw_corr(c)) * np_ * 4
+    extra = 2 * snaps + 3 * 16 * np_ * K  # staged inputs and outputs of the adjoint runs
+    if req.kind == "hvp":
+        extra = 3 * extra
+    return int(per + extra + (1 << 20))
+
+
+def run_request(req: Request, precision: str = "fp32", device: int = 0):
+    """Runs one request on the calling thread's bound context (see
+    solvers.bound_context) and returns its result dict."""
+    from . import objective
+    t = (-(req.cfg.nt - 1) + np.arange(req.cfg.ntc)) * req.cfg.dt
+    if req.kind == "correlation":
+        return {"correlations": _correlations(req, precision, device)}
+    if req.kind == "kernel":
+        j, g, c = objective.eval_objective_and_gradient(
+            req.mu, req.rho, req.spectrum, req.source_dist, req.ref_stat, req.receivers, req.c_data, t,
+            cfg=req.cfg, type="structure", measurement_source=req.measurement,
+            measurement_structure=req.measurement, weighting=req.weighting, precision=precision, device=device)
+        return {"misfit": j, "gradient": g, "correlations": c}
+    if req.kind == "hvp":
+        H = objective.eval_hessian_vector_product(
+            req.mu, req.rho, req.spectrum, req.source_dist, req.ref_stat, req.receivers, req.c_data, t, req.dmu,
+            cfg=req.cfg, type="structure", measurement_source=req.measurement,
+            measurement_structure=req.measurement, weighting=req.weighting, precision=precision, device=device)
+        return {"hvp": H}
+    raise ValueError(f"unknown request kind {req.kind!r}")
+
+
+def _correlations(req: Request, precision: str, device: int) -> np.ndarray:
+    import ctypes
+    from . import _lib
+    from .solvers import context
+    ctx = context(device, precision)
+    c = req.cfg
+    cc = c.to_c()
+    ref = np.asarray(req.ref_stat, dtype=np.float64).reshape(-1, 2)
+    rec = np.asfortranarray(np.asarray(req.receivers, dtype=np.float64).reshape(-1, 2))
+    mu = np.asfortranarray(req.mu, dtype=np.float64)
+    rho = np.asfortranarray(req.rho, dtype=np.float64)
+    spec = np.asfortranarray(np.asarray(req.spectrum, dtype=np.float64).reshape(c.n_sample, -1))
+    sd = np.asfortranarray(req.source_dist, dtype=np.float64)
+    n_dist = 1 if sd.ndim == 2 else sd.shape[2]
+    nr = rec.shape[0]
+    out = np.zeros((ref.shape[0], nr, c.ntc))
+    srcs = [np.asfortranarray(ref[i:i + 1]) for i in range(ref.shape[0])]
+    outs = [np.zeros((nr, c.ntc), order="F") for _ in srcs]
+    jobs = (_lib.FD2DJob * len(srcs))()
+    for i, s in enumerate(srcs):
+        jobs[i].cfg = ctypes.pointer(cc)
+        jobs[i].mu, jobs[i].rho = mu.ctypes.data, rho.ctypes.data
+        jobs[i].spectrum, jobs[i].n_noise_sources = spec.ctypes.data, spec.shape[1]
+        jobs[i].source_dist, jobs[i].n_dist = sd.ctypes.data, n_dist
+        jobs[i].src, jobs[i].rec, jobs[i].nr = s.ctypes.data, rec.ctypes.data, nr
+        jobs[i].correlations = outs[i].ctypes.data
+    _lib.check(ctx.L.fd2d_correlation_batch(ctx.h, jobs, len(srcs)), ctx.h)
+    for i, o in enumerate(outs):
+        out[i] = o
+    return out
+
+
+@dataclass
+class _Entry:
+    req: Request
+    fut: Future
+    bytes: int
+    bypassed: int = 0
+
+
+class Server:
+    def __init__(self, budget_bytes: int, slots: int = 4, device: int = 0, precision: str = "fp32",
+                 max_bypass: int = 4, runner: Optional[Callable] = None, footprint_fn: Callable = footprint,
+                 contexts: bool = True):
+        """``runner(req)`` replaces run_request and ``contexts=False`` skips the
+        per-slot libfd2d contexts (host-only tests of the admission logic)."""
+        if slots < 1 or budget_bytes <= 0:
+            raise ValueError("need at least one slot and a positive budget")
+        self.budget = int(budget_bytes)
+        self.free = int(budget_bytes)
+        self.max_bypass = max_bypass
+        self.device, self.precision = device, precision
+        self.runner = runner or (lambda r: run_request(r, precision, device))
+        self.footprint = footprint_fn
+        self.queue: deque = deque()
+        self.cv = threading.Condition()
+        self.stop = False
+        self.running = 0
+        self.peak_bytes = 0
+        self.peak_running = 0
+        self.log = []  # (kind, arrival, start, finish, bytes, gpt)
+        self.threads = [threading.Thread(target=self._worker, args=(i, contexts), daemon=True)
+                        for i in range(slots)]
+        for t in self.threads:
+            t.start()
+
+    # -- client side --------------------------------------------------------------
+    def submit(self, req: Request) -> Future:
+        fut: Future = Future()
+        b = int(self.footprint(req))
+        if b > self.budget:
+            fut.set_exception(AdmissionError(f"request needs {b} B of device memory; the budget is {self.budget} B"))
+            return fut
+        with self.cv:
+            if self.stop:
+                raise RuntimeError("server closed")
+            self.queue.append(_Entry(req, fut, b))
+            self.cv.notify_all()
+        return fut
+
+    def close(self):
+        with self.cv:
+            self.stop = True
+            self.cv.notify_all()
+        for t in self.threads:
+            t.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- admission ----------------------------------------------------------------
+    def _pick(self) -> Optional[_Entry]:
+        """First queued entry that fits (called with the lock held)."""
+        if not self.queue:
+            return None
+        head = self.queue[0]
+        if head.bytes <= self.free:
+            return self.queue.popleft()
+        if head.bypassed >= self.max_bypass:
+            return None  # the head waits for memory; nobody passes it any more
+        for k in range(1, len(self.queue)):
+            e = self.queue[k]
+            if e.bytes <= self.free:
+                head.bypassed += 1
+                del self.queue[k]
+                return e
+        return None
+
+    def _worker(self, slot: int, contexts: bool):
+        ctx = None
+        bind = None
+        if contexts:
+            from . import _lib, solvers
+            from .solvers import _prec
+            ctx = _lib.Context(self.device, _prec(self.precision))
+            bind = solvers.bound_context(ctx)
+            bind.__enter__()
+        try:
+            while True:
+                with self.cv:
+                    e = None
+                    while not self.stop:
+                        e = self._pick()
+                        if e is not None:
+                            break
+                        self.cv.wait()
+                    if e is None:
+                        return
+                    self.free -= e.bytes
+                    self.running += 1
+                    self.peak_bytes = max(self.peak_bytes, self.budget - self.free)
+                    self.peak_running = max(self.peak_running, self.running)
+                start = time.perf_counter()
+                try:
+                    res = self.runner(e.req)
+                    err = None
+                except BaseException as x:  # reported through the future
+                    res, err = None, x
+                finally:
+                    if ctx is not None:
+                        try:
+                            ctx.release()
+                        except Exception:
+                            pass
+                finish = time.perf_counter()
+                with self.cv:
+                    self.free += e.bytes
+                    self.running -= 1
+                    self.log.append((e.req.kind, e.req.arrival, start, finish, e.bytes, e.req.gpt()))
+                    self.cv.notify_all()
+                if err is not None:
+                    e.fut.set_exception(err)
+                else:
+                    e.fut.set_result(res)
+        finally:
+            if bind is not None:
+                bind.__exit__(None, None, None)
+            if ctx is not None:
+                ctx.close()
+
+    # -- statistics ---------------------------------------------------------------
+    def latency_stats(self):
+        lat = np.array([f - a for (_, a, _, f, _, _) in self.log])
+        if lat.size == 0:
+            return {}
+        t0 = min(a for (_, a, _, _, _, _) in self.log)
+        t1 = max(f for (_, _, _, f, _, _) in self.log)
+        gpt = sum(g for (*_, g) in self.log)
+        return {"requests": int(lat.size), "p50_s": float(np.percentile(lat, 50)),
+                "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
+                "throughput_req_s": lat.size / (t1 - t0), "gpt_per_s": gpt / (t1 - t0),
+                "peak_concurrent": self.peak_running, "peak_bytes": self.peak_bytes}

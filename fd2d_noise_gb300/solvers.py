@@ -20,6 +20,7 @@ plain FP64 form, ``'fp32'`` (default) the FP32 / split-TF32 tensor-core form.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import threading
 from typing import Optional
@@ -31,10 +32,29 @@ from .config import Config, get_config, n_fw_corr, n_fw_green, n_kernel_planes
 
 _ctx_lock = threading.Lock()
 _ctxs: dict = {}
+_local = threading.local()
+
+
+@contextlib.contextmanager
+def bound_context(ctx: _lib.Context):
+    """Within the block, this thread's solver calls use ``ctx`` (its own stream
+    and workspace) instead of the process-wide context."""
+    prev = getattr(_local, "ctx", None)
+    _local.ctx = ctx
+    try:
+        yield ctx
+    finally:
+        _local.ctx = prev
 
 
 def context(device: int = 0, precision: str = "fp32") -> _lib.Context:
-    """The process-wide context of ``device`` (created on first use)."""
+    """The context bound to this thread, else the process-wide context of
+    ``device`` (created on first use)."""
+    c = getattr(_local, "ctx", None)
+    if c is not None:
+        c.set_memspace(_lib.MEM_HOST)
+        c.set_precision(_prec(precision))
+        return c
     with _ctx_lock:
         c = _ctxs.get(device)
         if c is None:

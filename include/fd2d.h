@@ -112,6 +112,11 @@ fd2d_status fd2d_ctx_set_memspace(fd2d_ctx* ctx, int32_t memspace);
 fd2d_status fd2d_ctx_set_precision(fd2d_ctx* ctx, int32_t precision);
 /* Wait for all work queued on the context's stream. */
 fd2d_status fd2d_ctx_synchronize(fd2d_ctx* ctx);
+/* Device memory the context keeps between calls (workspace buffers). */
+int64_t fd2d_ctx_workspace_bytes(const fd2d_ctx* ctx);
+/* Wait for the stream, then free the workspace and the cached CUDA graphs;
+ * *bytes (may be NULL) receives the workspace size that was freed. */
+fd2d_status fd2d_ctx_release(fd2d_ctx* ctx, int64_t* bytes);
 /* Kernels launched by this context since creation (instrumentation). */
 int64_t fd2d_ctx_kernel_launches(const fd2d_ctx* ctx);
 /* Device-time instrumentation.  When enabled, every launch of the classes
