@@ -39,10 +39,12 @@ namespace {
 
 constexpr int TX = 32, TZ = 16, NT = 128;
 constexpr int MAX_BOX_SRC = 64;
+constexpr int MAX_TILE_REC = 32;  // receivers of one tile kept in shared memory
 
 struct Grid32 {
   int nx, nz, P;  // P: row pitch of internal arrays (floats)
-  int S;          // lanes: solves of this grid advanced by one launch (blockIdx.z)
+  int S;          // lanes: solves of this grid advanced by one launch
+  int ntx, ntz;   // step tiles per lane along x and z
   int64_t ps;     // plane stride of the pitched arrays; lane l's plane starts at l*ps
   float c[4];
   float inv_dx, inv_dz, dt;
@@ -68,7 +70,7 @@ struct Tile {
   static constexpr int O_U = O_MU + al(TZ * TX);
   static constexpr int O_VN = O_U + al(TZ * TX);
   static constexpr int TOTAL = O_VN + al(BH * BWa);  // new v on the 40-wide box (x from x0-4)
-  static constexpr int BYTES = TOTAL * 4 + 128;  // + alignment slack
+  static constexpr int BYTES = TOTAL * 4 + 128;      // + alignment slack
 };
 
 struct alignas(64) StepMaps {
@@ -90,287 +92,325 @@ struct Step32 {
   float* snap_dft;               // new field (v or u) into the DFT snapshot plane (pitched); per lane + l*ps
   const int2* rec_xy;            // per lane + l*nrec
   int nrec;
+  const int2* tile_rec;          // per (lane, tile): {first entry, count} of its receivers
+  const int2* rec_ent;           // receiver entries {k, (z - z0)*TX + (x - x0)}
   double* seis_col;              // seismograms(:, n); per lane + l*seis_lane
   int64_t seis_lane;
   int rec_u;
 };
 
+// One CTA per tile; tiles of all lanes form one list (blockIdx.x).
 template <int R>
-__global__ __launch_bounds__(NT) void k32_step(Grid32 G, const __grid_constant__ StepMaps M, Step32 S) {
+__device__ __forceinline__ void tile_coords(const Grid32& G, int t, int& x0, int& z0, int& lane) {
+  const int per = G.ntx * G.ntz;
+  lane = t / per;
+  const int r = t - lane * per;
+  z0 = (r / G.ntx) * TZ;
+  x0 = (r - (r / G.ntx) * G.ntx) * TX;
+}
+
+template <int R>
+__device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, const Step32& S, float* buf,
+                                           uint64_t* bar, int t, bool coeffs, bool fields) {
+  using T = Tile<R>;
+  int x0, z0, lane;
+  tile_coords<R>(G, t, x0, z0, lane);
+  const int bz0 = z0 - R + 1;
+  if (coeffs) {
+    uint32_t bytes = 4u * (T::BH * T::SXWa + T::SZH * T::BWa + 3 * T::BH * T::BWa + TZ * TX);
+    if (S.has_u) bytes += 4u * TZ * TX;
+    if (S.inj_plane >= 0) bytes += 4u * T::BH * T::BWa;
+    mbar_expect_tx(bar, bytes);
+    tma_load_3d(buf + T::O_B, &M.b, x0 - 4, bz0, lane, bar);
+    tma_load_3d(buf + T::O_T, &M.taper, x0 - 4, bz0, lane, bar);
+    tma_load_3d(buf + T::O_MU, &M.dtmu, x0, z0, lane, bar);
+  }
+  if (fields) {
+    tma_load_3d(buf + T::O_SXY, &M.sxy, x0 - 8, bz0, lane, bar);
+    tma_load_3d(buf + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, lane, bar);
+    tma_load_3d(buf + T::O_V, &M.v, x0 - 4, bz0, lane, bar);
+    if (S.has_u) tma_load_3d(buf + T::O_U, &M.u, x0, z0, lane, bar);
+    if (S.inj_plane >= 0) tma_load_3d(buf + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, bar);
+  }
+}
+
+template <int R>
+__global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constant__ StepMaps M, Step32 S) {
   using T = Tile<R>;
   extern __shared__ __align__(128) unsigned char sm_raw[];
   // TMA destinations: 128-byte aligned regardless of the static smem in front
-  float* sm = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm_raw) + 127) & ~uintptr_t(127));
+  // (offset arithmetic on the shared array keeps the pointer in the shared
+  // address space, so the float4 accesses below compile to shared loads)
+  float* sm = reinterpret_cast<float*>(sm_raw + ((128u - (smem_u32(sm_raw) & 127u)) & 127u));
+  float cf[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) cf[m] = G.c[m];
+  const float inv_dx = G.inv_dx, inv_dz = G.inv_dz, gdt = G.dt;
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_src[MAX_BOX_SRC];
   __shared__ float s_amp[MAX_BOX_SRC];
   __shared__ int s_nsrc;
+  __shared__ int2 s_rec[MAX_TILE_REC];
+  __shared__ int s_nrec;
 
   const int tid = threadIdx.x;
   const int nx = G.nx, nz = G.nz, P = G.P;
-  const int x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
-  const int bx0 = x0 - R + 1, bz0 = z0 - R + 1;
-  const int lane = blockIdx.z;
-  const int64_t lo = (int64_t)lane * G.ps;
-  const int2* src_xy = S.src_xy + (int64_t)lane * S.nsrc;
-  const double* amp = S.amp ? S.amp + (int64_t)lane * S.nsrc : nullptr;
-
-  if (tid == 0) {
-    s_nsrc = 0;
-    mbar_init(&bar, 1);
-    fence_mbar_init();
-    uint32_t bytes = 4u * (T::BH * T::SXWa + T::SZH * T::BWa + 3 * T::BH * T::BWa + TZ * TX);
-    if (S.has_u) bytes += 4u * TZ * TX;
-    if (S.inj_plane >= 0) bytes += 4u * T::BH * T::BWa;
-    mbar_expect_tx(&bar, bytes);
-    // coefficient planes are not written by the time loop: their loads may
-    // overlap the end of the previous step (programmatic dependent launch)
-    tma_load_3d(sm + T::O_B, &M.b, x0 - 4, bz0, lane, &bar);
-    tma_load_3d(sm + T::O_T, &M.taper, x0 - 4, bz0, lane, &bar);
-    tma_load_3d(sm + T::O_MU, &M.dtmu, x0, z0, lane, &bar);
-  }
-  // Everything below reads what the previous launch wrote, or writes what it
-  // read (ping-pong buffers): wait for it to complete.
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  if (tid == 0) {
-    tma_load_3d(sm + T::O_SXY, &M.sxy, x0 - 8, bz0, lane, &bar);
-    tma_load_3d(sm + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, lane, &bar);
-    tma_load_3d(sm + T::O_V, &M.v, x0 - 4, bz0, lane, &bar);
-    if (S.has_u) tma_load_3d(sm + T::O_U, &M.u, x0, z0, lane, &bar);
-    if (S.inj_plane >= 0) tma_load_3d(sm + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, &bar);
-  }
-  // point sources of the box (global loads overlap the TMA traffic); the box
-  // of new v is 40 columns wide from x0-4 (4-aligned for vector loads)
-  const int vx0 = x0 - 4;
-  int2 my_src = make_int2(-1 << 30, -1 << 30);
-  float my_amp = 0.f;
-  if (tid < S.nsrc) {
-    my_src = src_xy[tid];
-    my_amp = amp ? (float)amp[tid] : S.amp_const;
-  }
-  __syncthreads();  // barrier initialised, s_nsrc cleared
-  {
-    const int gx = my_src.x, gz = my_src.y;
-    if (gx >= vx0 && gx < vx0 + T::BWa && gz >= bz0 && gz < bz0 + T::BH) {
-      const int slot = atomicAdd(&s_nsrc, 1);
-      if (slot < MAX_BOX_SRC) {
-        s_src[slot] = (gz - bz0) * T::BWa + (gx - vx0);
-        s_amp[slot] = my_amp;
-      }
-    }
-  }
-  for (int k = tid + NT; k < S.nsrc; k += NT) {  // more sources than threads: rare
-    const int2 q = src_xy[k];
-    if (q.x >= vx0 && q.x < vx0 + T::BWa && q.y >= bz0 && q.y < bz0 + T::BH) {
-      const int slot = atomicAdd(&s_nsrc, 1);
-      if (slot < MAX_BOX_SRC) {
-        s_src[slot] = (q.y - bz0) * T::BWa + (q.x - vx0);
-        s_amp[slot] = amp ? (float)amp[k] : S.amp_const;
-      }
-    }
-  }
-  const bool ok = mbar_wait_bounded(&bar, 0);
-  if (__syncthreads_or(!ok)) {
-    if (tid == 0) set_error_flag(G.err, 1);
-    return;
-  }
-  const int nbs = s_nsrc;
-  const float* s_sxy = sm + T::O_SXY;
-  const float* s_szy = sm + T::O_SZY;
-  const float* s_v = sm + T::O_V;
-  const float* s_b = sm + T::O_B;
-  const float* s_t = sm + T::O_T;
-  const float* s_i = sm + T::O_I;
-  const float* s_mu = sm + T::O_MU;
-  const float* s_u = sm + T::O_U;
+  const int n_tiles = G.ntx * G.ntz * G.S;
+  constexpr int W = T::BWa;  // 40: row stride of the box regions
   float* s_vn = sm + T::O_VN;
   const bool inj = S.inj_plane >= 0;
-  constexpr int W = T::BWa;  // 40: row stride of the box regions
 
-  // ---- new v on the box: each thread a 4-wide, 2-tall block ------------------------
-  // DS = div_s(sxy, szy) (+ sources) (+ injection); v = (v + DS*dt/rho)*taper.
-  // Sums are formed in the same order as the scalar form (m = 1..R).
+  const int t = blockIdx.x;
+  if (t >= n_tiles) return;
+  if (tid == 0) {
+    s_nsrc = 0;
+    s_nrec = 0;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    // coefficient planes are not written by the time loop: their loads may
+    // overlap the end of the previous step (programmatic dependent launch)
+    issue_tile<R>(G, M, S, sm, &bar, t, true, false);
+  }
   {
-    constexpr int NQ = W / 4, NRB = (T::BH + 1) / 2;
-    if (tid < NQ * NRB) {
-      const int q = tid % NQ, r0 = 2 * (tid / NQ);
-      const int c0 = 4 * q;  // box column of element 0; global x = vx0 + c0 + e
-      float xs[2][12];       // sxy columns c0 .. c0+11 (x from x0-8 = box column - 4)
-      float zs[2 * R + 1][4];
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int rr = min(r0 + k, T::BH - 1);
-        const float4* rowp = reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + c0);
-#pragma unroll
-        for (int h = 0; h < 3; ++h) {
-          const float4 f = rowp[h];
-          xs[k][4 * h] = f.x; xs[k][4 * h + 1] = f.y; xs[k][4 * h + 2] = f.z; xs[k][4 * h + 3] = f.w;
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < 2 * R + 1; ++k) {
-        // szy row r0 + k holds szy(gz0 + k - R) for gz0 = global z of row r0
-        const int rr = min(r0 + k, T::SZH - 1);
-        const float4 f = *reinterpret_cast<const float4*>(s_szy + rr * W + c0);
-        zs[k][0] = f.x; zs[k][1] = f.y; zs[k][2] = f.z; zs[k][3] = f.w;
-      }
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int rr = r0 + k;
-        if (rr >= T::BH) break;
-        const int gz = bz0 + rr;
-        const bool zin = gz >= R && gz <= nz - R - 1;
-        const float4 v4 = *reinterpret_cast<const float4*>(s_v + rr * W + c0);
-        const float4 b4 = *reinterpret_cast<const float4*>(s_b + rr * W + c0);
-        const float4 t4 = *reinterpret_cast<const float4*>(s_t + rr * W + c0);
-        float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (inj) i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
-        const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
-        const float tt[4] = {t4.x, t4.y, t4.z, t4.w}, ii[4] = {i4.x, i4.y, i4.z, i4.w};
-        float out[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int gx = vx0 + c0 + e;
-          float ds = 0.f;
-          if (gx >= R && gx <= nx - R - 1) {
-            // sxy(gx + m - 1) is xs[k][e + 3 + m], sxy(gx - m) is xs[k][e + 4 - m]
-            float acc = 0.f;
-#pragma unroll
-            for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (xs[k][e + 3 + m] - xs[k][e + 4 - m]);
-            ds = acc * G.inv_dx;
-          }
-          if (zin) {
-            // szy(gz + m - 1) is zs[k + R + m - 1], szy(gz - m) is zs[k + R - m]
-            float acc = 0.f;
-#pragma unroll
-            for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (zs[k + R + m - 1][e] - zs[k + R - m][e]);
-            ds += acc * G.inv_dz;
-          }
-          if (nbs) {
-            const int idx = rr * W + c0 + e;
-            if (nbs <= MAX_BOX_SRC) {
-              for (int qq = 0; qq < nbs; ++qq)
-                if (s_src[qq] == idx) ds += s_amp[qq];
-            } else {
-              for (int qq = 0; qq < S.nsrc; ++qq) {
-                const int2 w = src_xy[qq];
-                if (w.x == gx && w.y == gz) ds += amp ? (float)amp[qq] : S.amp_const;
-              }
-            }
-          }
-          if (inj) ds += ii[e];
-          out[e] = (vv[e] + ds * bb[e]) * tt[e];
-        }
-        *reinterpret_cast<float4*>(s_vn + rr * W + c0) = make_float4(out[0], out[1], out[2], out[3]);
+    const float* buf = sm;
+    int x0, z0, lane;
+    tile_coords<R>(G, t, x0, z0, lane);
+    const int bz0 = z0 - R + 1, vx0 = x0 - 4;
+    const int64_t lo = (int64_t)lane * G.ps;
+    const int2* src_xy = S.src_xy + (int64_t)lane * S.nsrc;
+    const double* amp = S.amp ? S.amp + (int64_t)lane * S.nsrc : nullptr;
+    __syncthreads();  // barrier initialised, lists cleared
+    // receivers and point sources of this tile (static tables)
+    if (S.nrec && tid < 32) {
+      if (S.tile_rec) {
+        const int2 se = S.tile_rec[t];
+        if (tid == 0) s_nrec = se.y <= MAX_TILE_REC ? se.y : -1;
+        for (int q = tid; q < se.y && q < MAX_TILE_REC; q += 32) s_rec[q] = S.rec_ent[se.x + q];
+      } else if (tid == 0) {
+        s_nrec = -1;  // no tables: search the receiver list after the update
       }
     }
-  }
-  __syncthreads();
+    for (int k = tid; k < S.nsrc; k += NT) {
+      const int2 q = src_xy[k];
+      if (q.x >= vx0 && q.x < vx0 + W && q.y >= bz0 && q.y < bz0 + T::BH) {
+        const int slot = atomicAdd(&s_nsrc, 1);
+        if (slot < MAX_BOX_SRC) {
+          s_src[slot] = (q.y - bz0) * W + (q.x - vx0);
+          s_amp[slot] = amp ? (float)amp[k] : S.amp_const;
+        }
+      }
+    }
+    // Everything below reads what the previous launch wrote, or writes what it
+    // read (ping-pong buffers): wait for it to complete.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (tid == 0) issue_tile<R>(G, M, S, sm, &bar, t, false, true);
+    // one warp waits for the tile (suspending); the others wait at the barrier
+    bool ok = true;
+    if (tid < 32) ok = mbar_wait_bounded_sleep(&bar, 0);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        set_error_flag(G.err, 1);
+        mbar_wait_bounded_sleep(&bar, 0, 100000000ull);  // let started copies land (bounded)
+      }
+      return;
+    }
+    const int nbs = s_nsrc;
+    const float* s_sxy = buf + T::O_SXY;
+    const float* s_szy = buf + T::O_SZY;
+    const float* s_v = buf + T::O_V;
+    const float* s_b = buf + T::O_B;
+    const float* s_t = buf + T::O_T;
+    const float* s_i = buf + T::O_I;
+    const float* s_mu = buf + T::O_MU;
+    const float* s_u = buf + T::O_U;
 
-  // ---- stress, displacement and outputs: each thread a 4-wide row segment -----------
-  {
-    constexpr int NQ2 = TX / 4;  // 8 quads per row, TZ rows: NQ2 * TZ == NT
-    const int q = tid % NQ2, tz = tid / NQ2;
-    const int j = z0 + tz;
-    const int i0 = x0 + 4 * q;
-    if (tz < TZ && j < nz && i0 < nx) {
-      const int rr = tz + R - 1;  // box row of output row j
-      const int cv = 4 + 4 * q;   // box column of element 0
-      // vx = box columns cv-4 .. cv+7: v(i) is vx[e + 4], v(i + m) is vx[e + m + 4],
-      // v(i - m + 1) is vx[e - m + 5]
-      float vx[12];
-      {
-        const float4* rowp = reinterpret_cast<const float4*>(s_vn + rr * W + cv - 4);
+    // ---- new v on the box: each thread a 4-wide, 2-tall block ----------------------
+    // DS = div_s(sxy, szy) (+ sources) (+ injection); v = (v + DS*dt/rho)*taper.
+    // Sums are formed in the same order as the scalar form (m = 1..R).
+    {
+      constexpr int NQ = W / 4, NRB = (T::BH + 1) / 2;
+      if (tid < NQ * NRB) {
+        const int q = tid % NQ, r0 = 2 * (tid / NQ);
+        const int c0 = 4 * q;  // box column of element 0; global x = vx0 + c0 + e
+        float xs[2][12];       // sxy columns c0 .. c0+11 (x from x0-8 = box column - 4)
+        float zs[2 * R + 1][4];
 #pragma unroll
-        for (int h = 0; h < 3; ++h) {
-          const float4 f = rowp[h];
-          vx[4 * h] = f.x; vx[4 * h + 1] = f.y; vx[4 * h + 2] = f.z; vx[4 * h + 3] = f.w;
+        for (int k = 0; k < 2; ++k) {
+          const int rr = min(r0 + k, T::BH - 1);
+          const float4* rowp = reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + c0);
+#pragma unroll
+          for (int h = 0; h < 3; ++h) {
+            const float4 f = rowp[h];
+            xs[k][4 * h] = f.x; xs[k][4 * h + 1] = f.y; xs[k][4 * h + 2] = f.z; xs[k][4 * h + 3] = f.w;
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 2 * R + 1; ++k) {
+          // szy row r0 + k holds szy(gz0 + k - R) for gz0 = global z of row r0
+          const int rr = min(r0 + k, T::SZH - 1);
+          const float4 f = *reinterpret_cast<const float4*>(s_szy + rr * W + c0);
+          zs[k][0] = f.x; zs[k][1] = f.y; zs[k][2] = f.z; zs[k][3] = f.w;
+        }
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const int rr = r0 + k;
+          if (rr >= T::BH) break;
+          const int gz = bz0 + rr;
+          const bool zin = gz >= R && gz <= nz - R - 1;
+          const float4 v4 = *reinterpret_cast<const float4*>(s_v + rr * W + c0);
+          const float4 b4 = *reinterpret_cast<const float4*>(s_b + rr * W + c0);
+          const float4 t4 = *reinterpret_cast<const float4*>(s_t + rr * W + c0);
+          float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (inj) i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
+          const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
+          const float tt[4] = {t4.x, t4.y, t4.z, t4.w}, ii[4] = {i4.x, i4.y, i4.z, i4.w};
+          float out[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int gx = vx0 + c0 + e;
+            // both sums are formed everywhere and selected (no divergent branches)
+            // sxy(gx + m - 1) is xs[k][e + 3 + m], sxy(gx - m) is xs[k][e + 4 - m]
+            float ax = 0.f;
+#pragma unroll
+            for (int m = 1; m <= R; ++m) ax += cf[m - 1] * (xs[k][e + 3 + m] - xs[k][e + 4 - m]);
+            // szy(gz + m - 1) is zs[k + R + m - 1], szy(gz - m) is zs[k + R - m]
+            float az = 0.f;
+#pragma unroll
+            for (int m = 1; m <= R; ++m) az += cf[m - 1] * (zs[k + R + m - 1][e] - zs[k + R - m][e]);
+            float ds = (gx >= R && gx <= nx - R - 1) ? ax * inv_dx : 0.f;
+            ds = zin ? ds + az * inv_dz : ds;
+            if (nbs) {
+              const int idx = rr * W + c0 + e;
+              if (nbs <= MAX_BOX_SRC) {
+                for (int qq = 0; qq < nbs; ++qq)
+                  if (s_src[qq] == idx) ds += s_amp[qq];
+              } else {
+                for (int qq = 0; qq < S.nsrc; ++qq) {
+                  const int2 w = src_xy[qq];
+                  if (w.x == gx && w.y == gz) ds += amp ? (float)amp[qq] : S.amp_const;
+                }
+              }
+            }
+            if (inj) ds += ii[e];
+            out[e] = (vv[e] + ds * bb[e]) * tt[e];
+          }
+          *reinterpret_cast<float4*>(s_vn + rr * W + c0) = make_float4(out[0], out[1], out[2], out[3]);
         }
       }
-      float vz[2 * R][4];  // box rows rr - R + 1 .. rr + R
+    }
+    __syncthreads();
+
+    // ---- stress, displacement and outputs: each thread a 4-wide row segment ---------
+    {
+      constexpr int NQ2 = TX / 4;  // 8 quads per row, TZ rows: NQ2 * TZ == NT
+      const int q = tid % NQ2, tz = tid / NQ2;
+      const int j = z0 + tz;
+      const int i0 = x0 + 4 * q;
+      if (tz < TZ && j < nz && i0 < nx) {
+        const int rr = tz + R - 1;  // box row of output row j
+        const int cv = 4 + 4 * q;   // box column of element 0
+        // vx = box columns cv-4 .. cv+7: v(i) is vx[e + 4], v(i + m) is vx[e + m + 4],
+        // v(i - m + 1) is vx[e - m + 5]
+        float vx[12];
+        {
+          const float4* rowp = reinterpret_cast<const float4*>(s_vn + rr * W + cv - 4);
 #pragma unroll
-      for (int k = 0; k < 2 * R; ++k) {
-        const float4 f = *reinterpret_cast<const float4*>(s_vn + (rr - R + 1 + k) * W + cv);
-        vz[k][0] = f.x; vz[k][1] = f.y; vz[k][2] = f.z; vz[k][3] = f.w;
-      }
-      const float4 mu4 = *reinterpret_cast<const float4*>(s_mu + tz * TX + 4 * q);
-      const float4 sx4 = *reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + 8 + 4 * q);
-      const float4 sz4 = *reinterpret_cast<const float4*>(s_szy + (tz + 2 * R - 1) * W + 4 + 4 * q);
-      float4 u4 = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (S.has_u) u4 = *reinterpret_cast<const float4*>(s_u + tz * TX + 4 * q);
-      const float mu[4] = {mu4.x, mu4.y, mu4.z, mu4.w}, sxo[4] = {sx4.x, sx4.y, sx4.z, sx4.w};
-      const float szo[4] = {sz4.x, sz4.y, sz4.z, sz4.w}, uo[4] = {u4.x, u4.y, u4.z, u4.w};
-      const bool zin = j >= R - 1 && j <= nz - R - 1;
-      float nsx[4], nsz[4], nu[4], vn[4];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int i = i0 + e;
-        vn[e] = vx[e + 4];
-        float nw = sxo[e];
-        if (i >= R - 1 && i <= nx - R - 1) {
-          float acc = 0.f;
-#pragma unroll
-          for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (vx[e + m + 4] - vx[e - m + 5]);
-          nw += mu[e] * (acc * G.inv_dx);
+          for (int h = 0; h < 3; ++h) {
+            const float4 f = rowp[h];
+            vx[4 * h] = f.x; vx[4 * h + 1] = f.y; vx[4 * h + 2] = f.z; vx[4 * h + 3] = f.w;
+          }
         }
-        nsx[e] = nw;
-        nw = szo[e];
-        if (zin) {
-          float acc = 0.f;
+        float vz[2 * R][4];  // box rows rr - R + 1 .. rr + R
 #pragma unroll
-          for (int m = 1; m <= R; ++m) acc += G.c[m - 1] * (vz[R - 1 + m][e] - vz[R - m][e]);
-          nw += mu[e] * (acc * G.inv_dz);
+        for (int k = 0; k < 2 * R; ++k) {
+          const float4 f = *reinterpret_cast<const float4*>(s_vn + (rr - R + 1 + k) * W + cv);
+          vz[k][0] = f.x; vz[k][1] = f.y; vz[k][2] = f.z; vz[k][3] = f.w;
         }
-        nsz[e] = nw;
-        nu[e] = S.has_u ? uo[e] + vn[e] * G.dt : vn[e];
-      }
-      const int64_t p = lo + i0 + (int64_t)P * j;
-      if (i0 + 3 < nx) {
-        // whole quad inside the grid: vector stores
-        *reinterpret_cast<float4*>(S.vo + p) = make_float4(vn[0], vn[1], vn[2], vn[3]);
-        if (i0 + 3 <= nx - 2) {
-          *reinterpret_cast<float4*>(S.sxyo + p) = make_float4(nsx[0], nsx[1], nsx[2], nsx[3]);
-        } else {
-#pragma unroll
-          for (int e = 0; e < 4; ++e)
-            if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
-        }
-        if (j <= nz - 2) *reinterpret_cast<float4*>(S.szyo + p) = make_float4(nsz[0], nsz[1], nsz[2], nsz[3]);
-        if (S.has_u) *reinterpret_cast<float4*>(S.uo + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
-        if (S.snap_dft) *reinterpret_cast<float4*>(S.snap_dft + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
-      } else {
+        const float4 mu4 = *reinterpret_cast<const float4*>(s_mu + tz * TX + 4 * q);
+        const float4 sx4 = *reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + 8 + 4 * q);
+        const float4 sz4 = *reinterpret_cast<const float4*>(s_szy + (tz + 2 * R - 1) * W + 4 + 4 * q);
+        float4 u4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (S.has_u) u4 = *reinterpret_cast<const float4*>(s_u + tz * TX + 4 * q);
+        const float mu[4] = {mu4.x, mu4.y, mu4.z, mu4.w}, sxo[4] = {sx4.x, sx4.y, sx4.z, sx4.w};
+        const float szo[4] = {sz4.x, sz4.y, sz4.z, sz4.w}, uo[4] = {u4.x, u4.y, u4.z, u4.w};
+        const bool zin = j >= R - 1 && j <= nz - R - 1;
+        float nsx[4], nsz[4], nu[4], vn[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-          if (i0 + e >= nx) break;
-          S.vo[p + e] = vn[e];
-          if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
-          if (j <= nz - 2) S.szyo[p + e] = nsz[e];
-          if (S.has_u) S.uo[p + e] = nu[e];
-          if (S.snap_dft) S.snap_dft[p + e] = nu[e];
+          const int i = i0 + e;
+          vn[e] = vx[e + 4];
+          float ax = 0.f, az = 0.f;
+#pragma unroll
+          for (int m = 1; m <= R; ++m) ax += cf[m - 1] * (vx[e + m + 4] - vx[e - m + 5]);
+#pragma unroll
+          for (int m = 1; m <= R; ++m) az += cf[m - 1] * (vz[R - 1 + m][e] - vz[R - m][e]);
+          nsx[e] = (i >= R - 1 && i <= nx - R - 1) ? sxo[e] + mu[e] * (ax * inv_dx) : sxo[e];
+          nsz[e] = zin ? szo[e] + mu[e] * (az * inv_dz) : szo[e];
+          nu[e] = S.has_u ? uo[e] + vn[e] * gdt : vn[e];
+        }
+        const int64_t p = lo + i0 + (int64_t)P * j;
+        if (i0 + 3 < nx) {
+          // whole quad inside the grid: vector stores
+          *reinterpret_cast<float4*>(S.vo + p) = make_float4(vn[0], vn[1], vn[2], vn[3]);
+          if (i0 + 3 <= nx - 2) {
+            *reinterpret_cast<float4*>(S.sxyo + p) = make_float4(nsx[0], nsx[1], nsx[2], nsx[3]);
+          } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
+          }
+          if (j <= nz - 2) *reinterpret_cast<float4*>(S.szyo + p) = make_float4(nsz[0], nsz[1], nsz[2], nsz[3]);
+          if (S.has_u) *reinterpret_cast<float4*>(S.uo + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
+          if (S.snap_dft) *reinterpret_cast<float4*>(S.snap_dft + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            if (i0 + e >= nx) break;
+            S.vo[p + e] = vn[e];
+            if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
+            if (j <= nz - 2) S.szyo[p + e] = nsz[e];
+            if (S.has_u) S.uo[p + e] = nu[e];
+            if (S.snap_dft) S.snap_dft[p + e] = nu[e];
+          }
+        }
+        if (S.nrec && s_nrec > 0) {
+          // receivers in this quad take the new value straight from registers
+          double* seis = S.seis_col + lane * S.seis_lane;
+          const int l0 = tz * TX + 4 * q;
+          for (int r = 0; r < s_nrec; ++r) {
+            const int2 e = s_rec[r];
+            const int d = e.y - l0;
+            if (d >= 0 && d < 4) {
+              const float xu = d == 0 ? nu[0] : d == 1 ? nu[1] : d == 2 ? nu[2] : nu[3];
+              const float xv = d == 0 ? vn[0] : d == 1 ? vn[1] : d == 2 ? vn[2] : vn[3];
+              seis[e.x] = (double)(S.rec_u ? xu : xv);
+            }
+          }
+        }
+        if (S.snap_pre) {
+          const float* old = S.snap_pre_u ? s_u + tz * TX + 4 * q : s_v + rr * W + cv;
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (i0 + e < nx) S.snap_pre[i0 + e + nx * j] = old[e];
         }
       }
-      if (S.snap_pre) {
-        const float* old = S.snap_pre_u ? s_u + tz * TX + 4 * q : s_v + rr * W + cv;
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-          if (i0 + e < nx) S.snap_pre[i0 + e + nx * j] = old[e];
+    }
+    if (S.nrec && s_nrec < 0) {
+      // more receivers in this tile than the shared list holds: read them back
+      __syncthreads();
+      const int2* rec_xy = S.rec_xy + (int64_t)lane * S.nrec;
+      double* seis = S.seis_col + lane * S.seis_lane;
+      for (int k = tid; k < S.nrec; k += NT) {
+        const int2 q = rec_xy[k];
+        if (q.x >= x0 && q.x < x0 + TX && q.y >= z0 && q.y < z0 + TZ) {
+          const int64_t p = lo + q.x + P * q.y;
+          seis[k] = (double)(S.rec_u ? S.uo[p] : S.vo[p]);
+        }
       }
     }
   }
   // the next step may start its launch and prologue now
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  if (S.nrec) {
-    __syncthreads();
-    const int2* rec_xy = S.rec_xy + (int64_t)lane * S.nrec;
-    double* seis = S.seis_col + lane * S.seis_lane;
-    for (int k = tid; k < S.nrec; k += NT) {
-      const int2 q = rec_xy[k];
-      if (q.x >= x0 && q.x < x0 + TX && q.y >= z0 && q.y < z0 + TZ) {
-        const int64_t p = lo + q.x + P * q.y;
-        seis[k] = (double)(S.rec_u ? S.uo[p] : S.vo[p]);
-      }
-    }
-  }
 }
 
 // ---- point kernels ---------------------------------------------------------------
@@ -525,6 +565,8 @@ struct Run {
   int R = 2;
   int2* rec_xy = nullptr;
   int2* src_xy = nullptr;
+  int2* tile_rec = nullptr;  // per (lane, tile): {first entry, count}
+  int2* rec_ent = nullptr;   // {receiver k, offset in the tile}
   int64_t np = 0;   // nx*nz
   int64_t ps = 0;   // pitched plane size P*nz rounded up to 128
   int S = 1;        // lanes; every internal array holds S planes (lane l at l*ps)
@@ -562,6 +604,8 @@ fd2d_status step_attributes(fd2d_ctx* ctx) {
 }
 
 fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, int par, Step32 s) {
+  s.tile_rec = r.tile_rec;
+  s.rec_ent = r.rec_ent;
   s.vo = r.v[1 - par];
   s.sxyo = r.sxy[1 - par];
   s.szyo = r.szy[1 - par];
@@ -609,6 +653,37 @@ fd2d_status set_inj_map(fd2d_ctx* ctx, Run& r, const float* planes, int n_planes
   for (int q = 0; q < 2; ++q)
     FD2D_TRY(make_tmap_f32(ctx, &r.maps[q].inj, planes, r.G.nx, r.G.nz, r.G.P, BWa, BH, n_planes, r.ps));
   return FD2D_OK;
+}
+
+// CSR of receivers by (lane, tile) of the step grid: table[(l*ntz + tz)*ntx + tx]
+// = {first, count} into ent = {k, (z - tz*TZ)*TX + (x - tx*TX)}.
+void build_tile_receivers_idx(int nx, int nz, const std::vector<const std::vector<int>*>& lanes,
+                              std::vector<int2>& table, std::vector<int2>& ent) {
+  const int ntx = (nx + TX - 1) / TX, ntz = (nz + TZ - 1) / TZ;
+  const int S = (int)lanes.size();
+  table.assign((size_t)S * ntx * ntz, make_int2(0, 0));
+  std::vector<std::vector<int2>> per(table.size());
+  for (int l = 0; l < S; ++l) {
+    const std::vector<int>& rec = *lanes[l];
+    for (int k = 0; k < (int)rec.size(); ++k) {
+      const int x = rec[k] % nx, z = rec[k] / nx;
+      const int tx = x / TX, tz = z / TZ;
+      per[((size_t)l * ntz + tz) * ntx + tx].push_back(make_int2(k, (z - tz * TZ) * TX + (x - tx * TX)));
+    }
+  }
+  ent.clear();
+  for (size_t t = 0; t < per.size(); ++t) {
+    table[t] = make_int2((int)ent.size(), (int)per[t].size());
+    ent.insert(ent.end(), per[t].begin(), per[t].end());
+  }
+  if (ent.empty()) ent.push_back(make_int2(0, 0));
+}
+
+void build_tile_receivers(int nx, int nz, const SolveArgs* a, int S, std::vector<int2>& table,
+                          std::vector<int2>& ent) {
+  std::vector<const std::vector<int>*> lanes;
+  for (int l = 0; l < S; ++l) lanes.push_back(&a[l].rec_idx);
+  build_tile_receivers_idx(nx, nz, lanes, table, ent);
 }
 
 // Buffers, coefficient planes and tensor maps of S lanes a[0..S-1] (solves of
@@ -671,7 +746,16 @@ fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S
   };
   FD2D_TRY(upload(ctx, "f32.rec", xy(true), &r.rec_xy));
   FD2D_TRY(upload(ctx, "f32.src", xy(false), &r.src_xy));
-  r.sgrid = dim3((nx + TX - 1) / TX, (nz + TZ - 1) / TZ, S);
+  {
+    // receivers grouped by step tile, so each CTA finds its own in one read
+    std::vector<int2> table, ent;
+    build_tile_receivers(nx, nz, a, S, table, ent);
+    FD2D_TRY(upload(ctx, "f32.tile_rec", table, &r.tile_rec));
+    FD2D_TRY(upload(ctx, "f32.rec_ent", ent, &r.rec_ent));
+  }
+  r.G.ntx = (nx + TX - 1) / TX;
+  r.G.ntz = (nz + TZ - 1) / TZ;
+  r.sgrid = dim3(r.G.ntx * r.G.ntz * S);
   r.pgrid = dim3((nx + 31) / 32, (nz + 7) / 8);
   FD2D_TRY(step_attributes(ctx));
   FD2D_TRY(contract_prepare(ctx));
@@ -1344,7 +1428,9 @@ extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg,
     r.szy[q] = planes + (7 + q) * ps;
     r.u[q] = nullptr;
   }
-  r.sgrid = dim3((nx + TX - 1) / TX, (nz + TZ - 1) / TZ);
+  r.G.ntx = (nx + TX - 1) / TX;
+  r.G.ntz = (nz + TZ - 1) / TZ;
+  r.sgrid = dim3(r.G.ntx * r.G.ntz);
   r.pgrid = dim3((P + 31) / 32, (nz + 7) / 8);
   // The array keeps the previous call's contents: clear what must start at zero.
   FD2D_CUDA(nullptr, cudaMemsetAsync(d_err, 0, sizeof(int), stream));
