@@ -19,12 +19,20 @@
 
 namespace fd2d {
 
+// Column tile and K block of the tensor-core contraction.
+constexpr int CONTRACT_BN = 128, CONTRACT_BK = 32;
+
 struct ContractArgs {
-  const float* A = nullptr;  // Kd planes, plane stride lda (>= M)
-  int64_t lda = 0;
-  const float* B = nullptr;  // Kd rows of N values, row stride ldb
-  int64_t ldb = 0;
   int M = 0, N = 0, Kd = 0;
+  // A (Kd planes of M points) as its split image (contract_image), a_nkb K
+  // blocks per row tile
+  const float* aimg = nullptr;
+  int a_nkb = 0;
+  // B as its split image (contract_image): column n of this call is column
+  // img_nt0*CONTRACT_BN + n of the imaged table, K row k is its row
+  // img_kb0*CONTRACT_BK + k; img_nkb = K blocks of the imaged table.
+  const float* bimg = nullptr;
+  int img_nt0 = 0, img_kb0 = 0, img_nkb = 0;
   // FP64 accumulation: column n < nsplit -> acc0[n*ldacc + m], else acc1[(n-nsplit)*ldacc + m]
   double* acc0 = nullptr;
   double* acc1 = nullptr;
@@ -45,6 +53,11 @@ struct ContractArgs {
 };
 
 fd2d_status contract(fd2d_ctx* ctx, cudaStream_t stream, const ContractArgs& a);
+// Split image of a K-by-X matrix (Kd rows of X values, row stride ld): floats
+// needed, and the kernel that writes it (queued on `stream`).
+size_t contract_image_floats(int X, int Kd);
+fd2d_status contract_image(fd2d_ctx* ctx, cudaStream_t stream, const float* src, int64_t ld, int X, int Kd,
+                           float* img);
 // One-time kernel attributes; call before any stream capture that contracts.
 fd2d_status contract_prepare(fd2d_ctx* ctx);
 

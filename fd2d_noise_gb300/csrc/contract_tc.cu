@@ -7,37 +7,38 @@
 // lo*lo (~2^-22 relative), and accumulates in FP32 in tensor memory.  Spectra
 // are then accumulated across snapshot chunks in FP64.
 //
-// CTA tile: 128 points (M) x 256 columns (N), K blocks of 32.
-//   warps 0-7 : producers -- read A (points contiguous) and B (columns
-//               contiguous) from global memory, split them, and store them
-//               transposed into K-major, 128-byte-swizzled shared memory;
-//   warp 8    : allocates TMEM, one lane issues tcgen05.mma (M=128, N=256,
-//               K=8 per instruction, 12 per K block) and commits to mbarriers;
-//   warps 0-3 : epilogue -- tcgen05.ld of their 32 TMEM lanes, FP64
-//               accumulation (optionally remapped from the pitched grid to
-//               MATLAB layout) or FP32 store.
+// Both operands are first split into "images" (k_image): for each 128-row
+// tile and 32-deep K block, the hi and lo halves already in the K-major,
+// 128-byte-swizzled layout the tensor core reads, so the contraction kernel
+// itself only moves blocks with bulk copies and issues MMAs.  A is the
+// wavefield snapshot chunk or the injection planes (points contiguous), B the
+// DFT / inverse-DFT basis (one image per table, shared by every CTA).
+//
+// k_contract_tc is persistent (one CTA per SM) over 128 x 128 output tiles,
+// with a 3-stage ring of 64 KB stages (A and B blocks, hi and lo) and two TMEM
+// accumulators, so the epilogue of one tile overlaps the main loop of the next.
 // Every mbarrier wait is bounded in time; a wait that gives up sets the
-// context's error flag and the CTA drains and frees its TMEM.
+// context's error flag, the CTA lets its own copies land (bounded) and frees
+// its TMEM.
 #include "contract.cuh"
 #include "tma.cuh"
+
+#include <algorithm>
 
 namespace fd2d {
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 32, STAGES = 2;
-constexpr int NPROD = 256;                  // producer threads (warps 0-7)
-constexpr int NTHREADS = NPROD + 32;        // + MMA warp
+constexpr int BM = 128, BN = CONTRACT_BN, BK = CONTRACT_BK, STAGES = 3;
 constexpr int A_BYTES = BM * BK * 4;        // 16 KB per split half
-constexpr int B_BYTES = BN * BK * 4;        // 32 KB per split half
+constexpr int B_BYTES = BN * BK * 4;        // 16 KB per split half
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;  // + 1024-byte alignment slack
-constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t TMEM_COLS = BN;
 
 // Instruction descriptor, kind::tf32: D = F32 (bits 4-5 = 1), A = B = TF32
 // (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
-// The N field (bits 17-22) is set per launch: the N tile is the smallest
-// multiple of 16 that covers N in ceil(N/256) tiles.
-constexpr uint32_t IDESC_BASE = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BM >> 4) << 24);
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
 // 1024 bytes apart (SBO), descriptor version 1.
@@ -46,8 +47,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
          ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
-// Byte offset of element (row r, k) in a K-major SW128 tile of 32 TF32 per row.
-__device__ __forceinline__ uint32_t sw128(int r, int chunk) {
+// Byte offset of the 16-byte chunk `chunk` (4 TF32) of row r in a K-major SW128
+// tile of 32 TF32 per row.
+__host__ __device__ __forceinline__ uint32_t sw128(int r, int chunk) {
   return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((chunk ^ (r & 7)) << 4));
 }
 
@@ -56,16 +58,11 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
   lo = x - hi;
 }
 
-__device__ __forceinline__ void st_shared_v4(uint32_t addr, float a, float b, float c, float d) {
-  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
-               : "memory");
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
       : "memory");
 }
 
@@ -73,6 +70,13 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
@@ -91,20 +95,61 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__global__ __launch_bounds__(NTHREADS, 1) void k_contract_tc(ContractArgs a, int bn, int* err) {
+// Image of a K-by-X matrix src (row k at src + k*ld, X values contiguous): for
+// each 128-row tile of X and 32-deep K block, the hi and lo halves in the
+// K-major SW128 layout of sw128() (rows x, 32 TF32 per row), block (xt, kb) at
+// ((xt * nkb) + kb) * 2 * TILE_BYTES.  Entries outside the matrix are zero.
+// One CTA per block: a coalesced load of the 32 x 128 tile into shared memory
+// (row stride 129: conflict-free column reads), then coalesced 16-byte stores.
+constexpr int TILE_BYTES = 128 * BK * 4;  // 16 KB: one split half of one block
+static_assert(TILE_BYTES == A_BYTES && TILE_BYTES == B_BYTES, "A and B tiles share the image format");
+
+__global__ __launch_bounds__(256) void k_image(const float* __restrict__ src, int64_t ld, int X, int Kd, int nkb,
+                                               float* __restrict__ img) {
+  __shared__ float tile[BK][129];
+  const int xt = blockIdx.x, kb = blockIdx.y, tid = threadIdx.x;
+  for (int e = tid; e < BK * 128; e += 256) {
+    const int k = e >> 7, x = e & 127;
+    const int gk = kb * BK + k, gx = xt * 128 + x;
+    tile[k][x] = (gk < Kd && gx < X) ? src[(int64_t)gk * ld + gx] : 0.f;
+  }
+  __syncthreads();
+  unsigned char* blk = reinterpret_cast<unsigned char*>(img) + ((size_t)xt * nkb + kb) * 2 * TILE_BYTES;
+  for (int q = tid; q < 2 * 128 * (BK / 4); q += 256) {
+    const int half = q >> 10, r = (q >> 3) & 127, c = q & 7;
+    float v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float hi, lo;
+      split_tf32(tile[c * 4 + j][r], hi, lo);
+      v[j] = half ? lo : hi;
+    }
+    *reinterpret_cast<float4*>(blk + half * TILE_BYTES + sw128(r, c)) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+}
+
+// Persistent contraction over output tiles (m_tile, n_tile), column tile
+// fastest, tile = blockIdx.x, blockIdx.x + gridDim.x, ...  Both operands come
+// as images: one bulk copy of A's block and one of B's per stage.
+//   warp 0   : one lane issues the bulk copies (STAGES-deep ring);
+//   warp 1   : allocates TMEM (two 128-column accumulators); one lane issues
+//              the MMAs (12 per K block) and commits stages and accumulators;
+//   warps 2-5: epilogue, TMEM lanes 32*(warp%4) .. +31 of the accumulator the
+//              MMAs are not writing -- it overlaps the next tile's main loop.
+constexpr int NTHREADS_P = 192;
+
+__global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, int ntn, int n_tiles, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t full_bar[STAGES];
-  __shared__ __align__(8) uint64_t empty_bar[STAGES];
-  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ __align__(8) uint64_t full_bar[STAGES];   // both blocks of the stage landed (tx)
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];  // MMAs done reading the stage
+  __shared__ __align__(8) uint64_t accf_bar[2];        // accumulator complete
+  __shared__ __align__(8) uint64_t acce_bar[2];        // accumulator read out (4 epilogue warps)
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * bn;
-  const uint32_t idesc = IDESC_BASE | ((uint32_t)(bn >> 3) << 17);
   const int nkb = (a.Kd + BK - 1) / BK;
-  unsigned char* smem = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sbase = smem_u32(smem);
   auto a_hi = [&](int s) { return sbase + s * STAGE_BYTES; };
   auto a_lo = [&](int s) { return sbase + s * STAGE_BYTES + A_BYTES; };
@@ -113,16 +158,19 @@ __global__ __launch_bounds__(NTHREADS, 1) void k_contract_tc(ContractArgs a, int
 
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&full_bar[s], NPROD / 32);
+      mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(&done_bar, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf_bar[b], 1);
+      mbar_init(&acce_bar[b], 4);
+    }
     fail = 0;
     fence_mbar_init();
   }
-  if (warp == 8) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(TMEM_COLS)
+                 "r"(2 * TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -131,146 +179,163 @@ __global__ __launch_bounds__(NTHREADS, 1) void k_contract_tc(ContractArgs a, int
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
 
-  if (warp < 8) {
-    // ---------------- producers ----------------
-    const int r = tid;  // B row (column n0 + r); A row m0 + r for r < 128
-    const int n = n0 + r;
-    const int m = m0 + r;
-    for (int kb = 0; kb < nkb; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (kb / STAGES) & 1;
-      if (!mbar_wait_bounded(&empty_bar[s], ph ^ 1)) {
-        atomicExch(&fail, 1);
-        break;
-      }
-      const int k0 = kb * BK;
-      // all global loads of the K block first (column n of B, row m of A) ...
-      float xb[BK], xa[BK];
-#pragma unroll
-      for (int k = 0; k < BK; ++k)
-        xb[k] = (r < bn && n < a.N && k0 + k < a.Kd) ? __ldg(a.B + (int64_t)(k0 + k) * a.ldb + n) : 0.f;
-      if (r < BM) {
-#pragma unroll
-        for (int k = 0; k < BK; ++k)
-          xa[k] = (m < a.M && k0 + k < a.Kd) ? a.A[(int64_t)(k0 + k) * a.lda + m] : 0.f;
-      }
-      // ... then split and store the transposed, swizzled rows
-#pragma unroll
-      for (int c = 0; c < BK / 4; ++c) {
-        float h[4], l[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) split_tf32(xb[c * 4 + q], h[q], l[q]);
-        st_shared_v4(b_hi(s) + sw128(r, c), h[0], h[1], h[2], h[3]);
-        st_shared_v4(b_lo(s) + sw128(r, c), l[0], l[1], l[2], l[3]);
-      }
-      if (r < BM) {
-#pragma unroll
-        for (int c = 0; c < BK / 4; ++c) {
-          float h[4], l[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) split_tf32(xa[c * 4 + q], h[q], l[q]);
-          st_shared_v4(a_hi(s) + sw128(r, c), h[0], h[1], h[2], h[3]);
-          st_shared_v4(a_lo(s) + sw128(r, c), l[0], l[1], l[2], l[3]);
+  if (warp == 0) {
+    // ---------------- bulk copies ----------------
+    if (lane == 0) {
+      const unsigned char* ai = reinterpret_cast<const unsigned char*>(a.aimg);
+      const unsigned char* bi = reinterpret_cast<const unsigned char*>(a.bimg);
+      int g = 0;  // stage uses so far
+      bool bad = false;
+      for (int t = blockIdx.x; t < n_tiles && !bad; t += gridDim.x) {
+        const int mt = t / ntn, nt = a.img_nt0 + (t - mt * ntn);
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          const int s = g % STAGES;
+          if (!mbar_wait_bounded_sleep(&empty_bar[s], ((g / STAGES) & 1) ^ 1) || fail) {
+            atomicExch(&fail, 1);
+            bad = true;
+            break;
+          }
+          mbar_expect_tx(&full_bar[s], 2 * A_BYTES + 2 * B_BYTES);
+          bulk_copy(a_hi(s), ai + ((size_t)mt * a.a_nkb + kb) * 2 * A_BYTES, 2 * A_BYTES, &full_bar[s]);
+          bulk_copy(b_hi(s), bi + ((size_t)nt * a.img_nkb + a.img_kb0 + kb) * 2 * B_BYTES, 2 * B_BYTES,
+                    &full_bar[s]);
         }
       }
-      // generic-proxy smem writes -> visible to the tensor core (async proxy)
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&full_bar[s]);
+      if (bad) {
+        // let this CTA's copies land before it exits (bounded)
+        for (int h = (g > STAGES ? g - STAGES : 0); h < g; ++h)
+          mbar_wait_bounded_sleep(&full_bar[h % STAGES], (h / STAGES) & 1, 100000000ull);
+      }
     }
-  } else {
-    // ---------------- MMA issuer (warp 8) ----------------
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
     if (lane == 0) {
+      int g = 0, i = 0;
       bool ok = true;
-      for (int kb = 0; kb < nkb && ok; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (kb / STAGES) & 1;
-        if (!mbar_wait_bounded(&full_bar[s], ph)) {
-          atomicExch(&fail, 1);
+      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++i) {
+        const int acc = i & 1;
+        const uint32_t d = tmem + (uint32_t)(acc * TMEM_COLS);
+        if (!mbar_wait_bounded(&acce_bar[acc], ((i >> 1) & 1) ^ 1)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          const int s = g % STAGES;
+          if (!mbar_wait_bounded(&full_bar[s], (g / STAGES) & 1)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-        for (int kk = 0; kk < BK / 8; ++kk) {
-          const uint64_t ah = smem_desc(a_hi(s) + kk * 32), al = smem_desc(a_lo(s) + kk * 32);
-          const uint64_t bh = smem_desc(b_hi(s) + kk * 32), bl = smem_desc(b_lo(s) + kk * 32);
-          mma_tf32(tmem, ah, bh, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
-          mma_tf32(tmem, ah, bl, idesc, 1u);
-          mma_tf32(tmem, al, bh, idesc, 1u);
+          for (int kk = 0; kk < BK / 8; ++kk) {
+            const uint64_t ah = smem_desc(a_hi(s) + kk * 32), al = smem_desc(a_lo(s) + kk * 32);
+            const uint64_t bh = smem_desc(b_hi(s) + kk * 32), bl = smem_desc(b_lo(s) + kk * 32);
+            mma_tf32(d, ah, bh, (kb > 0 || kk > 0) ? 1u : 0u);
+            mma_tf32(d, ah, bl, 1u);
+            mma_tf32(d, al, bh, 1u);
+          }
+          mma_commit(&empty_bar[s]);  // frees the stage once these MMAs have read it
         }
-        mma_commit(&empty_bar[s]);  // frees the stage once these MMAs have read it
+        if (ok) mma_commit(&accf_bar[acc]);  // accumulator ready for the epilogue
       }
-      mma_commit(&done_bar);  // all issued MMAs complete -> accumulator ready
+      if (!ok) atomicExch(&fail, 1);
     }
     __syncwarp();
-  }
-
-  // ---------------- epilogue (warps 0-3: TMEM lanes 32*warp .. +31) ----------------
-  if (warp < 4) {
-    const bool ok = mbar_wait_bounded(&done_bar, 0);
-    if (!ok) atomicExch(&fail, 1);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int row = warp * 32 + lane;
-    const int m = m0 + row;
-    int64_t q = m;
-    bool valid = ok && m < a.M;
-    if (valid && a.remap_pitch) {
-      int64_t mm = m, lane_off = 0;
-      if (a.lane_m) {
-        const int64_t l = mm / a.lane_m;
-        mm -= l * a.lane_m;
-        lane_off = l * a.acc_lane;
+  } else {
+    // ---------------- epilogue: warps 2-5 ----------------
+    const int quarter = warp & 3;  // TMEM lanes 32*quarter .. +31
+    int i = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++i) {
+      const int acc = i & 1;
+      const bool ok = mbar_wait_bounded_sleep(&accf_bar[acc], (i >> 1) & 1);
+      // warp-uniform decision: tcgen05.ld below needs every lane
+      if (__any_sync(0xffffffffu, !ok || fail)) {
+        if (lane == 0) atomicExch(&fail, 1);
+        break;
       }
-      const int ii = (int)(mm % a.remap_pitch), jj = (int)(mm / a.remap_pitch);
-      valid = ii < a.remap_nx && jj < a.remap_nz;
-      q = lane_off + ii + (int64_t)a.remap_nx * jj;
-    }
-    for (int c0 = 0; c0 < bn; c0 += 32) {
-      float v[32];
-      // all lanes of the warp take part in tcgen05.ld (sync.aligned)
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (!valid) continue;
-      if (a.out32) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int n = n0 + c0 + j;
-          if (n < a.N && c0 + j < bn) a.out32[(int64_t)n * a.ldo + m] = v[j];
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int mt = t / ntn, n0 = (t - mt * ntn) * BN;
+      const int m = mt * BM + quarter * 32 + lane;
+      int64_t q = m;
+      bool valid = m < a.M;
+      if (valid && a.remap_pitch) {
+        int64_t mm = m, lane_off = 0;
+        if (a.lane_m) {
+          const int64_t l = mm / a.lane_m;
+          mm -= l * a.lane_m;
+          lane_off = l * a.acc_lane;
         }
+        const int ii = (int)(mm % a.remap_pitch), jj = (int)(mm / a.remap_pitch);
+        valid = ii < a.remap_nx && jj < a.remap_nz;
+        q = lane_off + ii + (int64_t)a.remap_nx * jj;
       }
-      if (a.acc0) {
-        // Column n of the tile goes to plane n (acc0) or n - nsplit (acc1).
-        // Overwrite: plain stores.  Accumulate: 8 loads in flight per group.
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        // all lanes of the warp take part in tcgen05.ld (sync.aligned)
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TMEM_COLS + c0), v);
+        if (c0 + 32 == BN) {
+          // the accumulator is in registers: hand it back to the MMAs
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acce_bar[acc]);
+        }
+        if (!valid) continue;
+        if (a.out32) {
 #pragma unroll
-        for (int g = 0; g < 32; g += 8) {
-          double* p[8];
-          double old[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int n = n0 + c0 + g + j;
-            const bool in = n < a.N && c0 + g + j < bn;
-            p[j] = !in ? nullptr
-                       : (n < a.nsplit ? a.acc0 + (int64_t)n * a.ldacc + q
-                                       : a.acc1 + (int64_t)(n - a.nsplit) * a.ldacc + q);
-            old[j] = (p[j] && !a.overwrite) ? *p[j] : 0.0;
+          for (int j = 0; j < 32; ++j) {
+            const int n = n0 + c0 + j;
+            if (n < a.N) a.out32[(int64_t)n * a.ldo + m] = v[j];
           }
+        }
+        if (a.acc0) {
+          // Column n of the tile goes to plane n (acc0) or n - nsplit (acc1).
+          // Overwrite: plain stores.  Accumulate: 8 loads in flight per group.
 #pragma unroll
-          for (int j = 0; j < 8; ++j)
-            if (p[j]) *p[j] = old[j] + (double)v[g + j];
+          for (int gg = 0; gg < 32; gg += 8) {
+            double* p[8];
+            double old[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int n = n0 + c0 + gg + j;
+              p[j] = n >= a.N ? nullptr
+                              : (n < a.nsplit ? a.acc0 + (int64_t)n * a.ldacc + q
+                                              : a.acc1 + (int64_t)(n - a.nsplit) * a.ldacc + q);
+              old[j] = (p[j] && !a.overwrite) ? *p[j] : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+              if (p[j]) *p[j] = old[j] + (double)v[gg + j];
+          }
         }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 8) {
+  if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TMEM_COLS)
+                 : "memory");
   }
   if (tid == 0 && fail) set_error_flag(err, 2);
 }
 
 }  // namespace
+
+size_t contract_image_floats(int X, int Kd) {
+  const size_t nxt = (size_t)(X + 127) / 128, nkb = (size_t)(Kd + BK - 1) / BK;
+  return std::max<size_t>(1, nxt * nkb) * 2 * 128 * BK;
+}
+
+fd2d_status contract_image(fd2d_ctx* ctx, cudaStream_t stream, const float* src, int64_t ld, int X, int Kd,
+                           float* img) {
+  if (X <= 0 || Kd <= 0) return FD2D_OK;
+  dim3 grid((X + 127) / 128, (Kd + BK - 1) / BK);
+  k_image<<<grid, 256, 0, stream>>>(src, ld, X, Kd, (Kd + BK - 1) / BK, img);
+  return after_launch(ctx, "k_image");
+}
 
 fd2d_status contract_prepare(fd2d_ctx* ctx) {
   static bool attr = false;
@@ -283,11 +348,15 @@ fd2d_status contract_prepare(fd2d_ctx* ctx) {
 
 fd2d_status contract(fd2d_ctx* ctx, cudaStream_t stream, const ContractArgs& a) {
   if (a.M <= 0 || a.N <= 0 || a.Kd <= 0) return FD2D_OK;
-  const int ntiles = (a.N + BN - 1) / BN;
-  const int bn = ((a.N + ntiles - 1) / ntiles + 15) / 16 * 16;
-  dim3 grid((a.M + BM - 1) / BM, ntiles);
+  const int nkb = (a.Kd + BK - 1) / BK;
+  if (!a.aimg || !a.bimg || a.a_nkb < nkb || a.img_nkb < nkb + a.img_kb0)
+    return set_error(ctx, FD2D_ERR_ARG, "contraction without operand images covering its K blocks");
+  const int ntn = (a.N + BN - 1) / BN;
+  const int64_t tiles = (int64_t)((a.M + BM - 1) / BM) * ntn;
+  if (tiles > 0x7fffffff) return set_error(ctx, FD2D_ERR_SHAPE, "contraction too large for one launch");
+  const int grid = (int)std::min<int64_t>(tiles, std::max(ctx->sm_count, 1));
   const int t0 = timer_begin(ctx, stream);
-  k_contract_tc<<<grid, NTHREADS, SMEM_BYTES, stream>>>(a, bn, ctx->d_err);
+  k_contract_tc<<<grid, NTHREADS_P, SMEM_BYTES, stream>>>(a, ntn, (int)tiles, ctx->d_err);
   timer_end(ctx, stream, t0, FD2D_TIMER_CONTRACT, (int64_t)a.M * a.N * a.Kd);
   return after_launch(ctx, "k_contract_tc");
 }
@@ -303,7 +372,15 @@ extern "C" fd2d_status fd2d_contract_f32(fd2d_ctx* ctx, const float* A, int64_t 
     return set_error(ctx, FD2D_ERR_ARG, "bad contraction arguments");
   cudaSetDevice(ctx->device);
   FD2D_TRY(contract_prepare(ctx));
+  if (M == 0 || N == 0 || Kd == 0) return FD2D_OK;
+  float *aimg = nullptr, *bimg = nullptr;
+  FD2D_TRY(workspace_t(ctx, "contract.aimg", contract_image_floats(M, Kd), &aimg));
+  FD2D_TRY(workspace_t(ctx, "contract.bimg", contract_image_floats(N, Kd), &bimg));
+  FD2D_TRY(contract_image(ctx, ctx->stream, A, lda, M, Kd, aimg));
+  FD2D_TRY(contract_image(ctx, ctx->stream, B, ldb, N, Kd, bimg));
   ContractArgs c;
-  c.A = A; c.lda = lda; c.B = B; c.ldb = ldb; c.M = M; c.N = N; c.Kd = Kd; c.out32 = R; c.ldo = ldr;
+  c.M = M; c.N = N; c.Kd = Kd; c.out32 = R; c.ldo = ldr;
+  c.aimg = aimg; c.a_nkb = (Kd + CONTRACT_BK - 1) / CONTRACT_BK;
+  c.bimg = bimg; c.img_nkb = c.a_nkb;
   return contract(ctx, ctx->stream, c);
 }

@@ -812,7 +812,9 @@ size_t job_footprint(const Geometry& g, int nr, int n_dist, bool host_inputs) {
   const size_t T = std::min<size_t>({n_dft, 1024, ((size_t)2 << 30) / plane});
   const size_t n_inj = g.ntc / g.fs;
   const size_t chunk = std::min<size_t>(n_inj, ((size_t)4 << 30) / plane);
-  size_t b = 11 * plane + T * plane + 16 * np * g.K + 2 * (size_t)g.K * plane + chunk * plane;
+  // fields and coefficients, snapshot chunk and its split image (x2), FP64
+  // spectra, P planes and their split image (x2), injection planes
+  size_t b = 11 * plane + 3 * T * plane + 16 * np * g.K + 3 * 2 * (size_t)g.K * plane + chunk * plane;
   b += (size_t)nr * (g.nt + g.ntc) * 8 + ((size_t)1 << 20);
   if (host_inputs) b += np * 8 * (2 + n_dist) + (size_t)nr * g.ntc * 8;
   return b;

@@ -806,6 +806,8 @@ struct Injection {
   int chunk = 0, first = 0, count = 0;  // events [first, first+count) resident
   float* P = nullptr;              // 2K planes of S lanes: [k][lane][ps]
   float* B = nullptr;              // [2K][n_events] float
+  float* bimg = nullptr;           // split image of B for the tensor cores
+  float* aimg = nullptr;           // split image of the P planes
   int n_events = 0;
 };
 
@@ -839,8 +841,14 @@ fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, Run& r, const doub
   };
   FD2D_TRY(upload_tagged<float>(ctx, "f32.injB", table_tag(g, 2, inj.row_of_event),
                                 (size_t)2 * K * inj.n_events, fill, &inj.B));
+  FD2D_TRY(workspace_t(ctx, "f32.inj_bimg", contract_image_floats(inj.n_events, 2 * K), &inj.bimg));
+  FD2D_TRY(workspace_t(ctx, "f32.inj_aimg", contract_image_floats((int)sps, 2 * K), &inj.aimg));
+  FD2D_TRY(contract_image(ctx, ctx->stream, inj.P, sps, (int)sps, 2 * K, inj.aimg));
+  FD2D_TRY(contract_image(ctx, ctx->stream, inj.B, inj.n_events, inj.n_events, 2 * K, inj.bimg));
   const size_t cap = (size_t)4 << 30;  // resident injection planes <= 4 GiB
   inj.chunk = (int)std::max<int64_t>(1, std::min<int64_t>(inj.n_events, (int64_t)(cap / (sps * 4))));
+  // chunks start on column tiles of the image
+  if (inj.chunk < inj.n_events) inj.chunk = std::max(CONTRACT_BN, inj.chunk / CONTRACT_BN * CONTRACT_BN);
   FD2D_TRY(workspace_t(ctx, "f32.inj", (size_t)sps * inj.chunk, &inj.planes));
   inj.first = 0;
   inj.count = 0;
@@ -853,11 +861,12 @@ fd2d_status injection_plane(fd2d_ctx* ctx, const Run& r, const Geometry& g, Inje
     inj.first = j;
     inj.count = std::min(inj.chunk, inj.n_events - j);
     ContractArgs c;
-    c.A = inj.P;
-    c.lda = r.lanes_ps();
+    c.aimg = inj.aimg;
+    c.a_nkb = (2 * g.K + CONTRACT_BK - 1) / CONTRACT_BK;
     c.Kd = 2 * g.K;
-    c.B = inj.B + j;
-    c.ldb = inj.n_events;
+    c.bimg = inj.bimg;
+    c.img_nt0 = j / CONTRACT_BN;
+    c.img_nkb = (2 * g.K + CONTRACT_BK - 1) / CONTRACT_BK;
     c.M = (int)r.lanes_ps();
     c.N = inj.count;
     c.out32 = inj.planes;
@@ -875,12 +884,14 @@ struct Dft {
   int done = 0;       // events already contracted
   float* snaps = nullptr;
   struct Target {
-    float* B = nullptr;  // [n_events][2K] rows
+    float* B = nullptr;     // [n_events][2K] rows
+    float* bimg = nullptr;  // their split image
     double *re = nullptr, *im = nullptr;  // lane 0's spectra; lane l's start l*lane_stride later
     int64_t lane_stride = 0;
   };
   std::vector<Target> targets;
   int n_events = 0;
+  float* aimg = nullptr;  // split image of the snapshot chunk
 };
 
 fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
@@ -889,9 +900,12 @@ fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
   const size_t cap = (size_t)2 << 30;  // snapshot chunk <= 2 GiB
   const int64_t sps = r.lanes_ps();
   d.T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)n_events, (int64_t)1024, (int64_t)(cap / (sps * 4))}));
+  // chunks start on K blocks of the coefficient image
+  if (d.T < n_events) d.T = std::max(CONTRACT_BK, d.T / CONTRACT_BK * CONTRACT_BK);
   FD2D_TRY(workspace_t(ctx, "f32.dft_snaps", (size_t)sps * d.T, &d.snaps));
   // the pitch padding of the snapshot planes is never written by the stencil
   FD2D_CUDA(ctx, cudaMemsetAsync(d.snaps, 0, (size_t)sps * d.T * 4, ctx->stream));
+  FD2D_TRY(workspace_t(ctx, "f32.dft_aimg", contract_image_floats((int)sps, d.T), &d.aimg));
   return FD2D_OK;
 }
 
@@ -902,6 +916,9 @@ fd2d_status dft_add_target(fd2d_ctx* ctx, const char* name, uint64_t tag, size_t
                            double* im, int64_t lane_stride, Dft& d) {
   Dft::Target t;
   FD2D_TRY(upload_tagged<float>(ctx, name, tag, count, fill, &t.B));
+  const int K2 = (int)(count / std::max(d.n_events, 1));  // 2K columns
+  FD2D_TRY(workspace_t(ctx, (std::string(name) + ".img").c_str(), contract_image_floats(K2, d.n_events), &t.bimg));
+  FD2D_TRY(contract_image(ctx, ctx->stream, t.B, K2, K2, d.n_events, t.bimg));
   t.re = re;
   t.im = im;
   t.lane_stride = lane_stride;
@@ -913,13 +930,15 @@ float* dft_slot(const Run& r, Dft& d) { return d.snaps + (size_t)d.filled * r.la
 
 fd2d_status dft_flush(fd2d_ctx* ctx, const Run& r, const Geometry& g, Dft& d) {
   if (d.filled == 0) return FD2D_OK;
+  FD2D_TRY(contract_image(ctx, ctx->stream, d.snaps, r.lanes_ps(), (int)r.lanes_ps(), d.filled, d.aimg));
   for (auto& t : d.targets) {
     ContractArgs c;
-    c.A = d.snaps;
-    c.lda = r.lanes_ps();
+    c.aimg = d.aimg;
+    c.a_nkb = (d.filled + CONTRACT_BK - 1) / CONTRACT_BK;
     c.Kd = d.filled;
-    c.B = t.B + (size_t)d.done * 2 * g.K;
-    c.ldb = 2 * g.K;
+    c.bimg = t.bimg;
+    c.img_kb0 = d.done / CONTRACT_BK;
+    c.img_nkb = (d.n_events + CONTRACT_BK - 1) / CONTRACT_BK;
     c.M = (int)r.lanes_ps();
     if (r.S > 1) {
       c.lane_m = r.ps;
@@ -967,12 +986,12 @@ void sig_args(Sig& sg, const Geometry& g, const SolveArgs& a) {
 }
 
 void sig_dft(Sig& sg, const Dft& d) {
-  sg.add(d.T); sg.add(d.n_events); sg.add(d.snaps); sg.add(d.targets.size());
-  for (const auto& t : d.targets) { sg.add(t.B); sg.add(t.re); sg.add(t.im); }
+  sg.add(d.T); sg.add(d.n_events); sg.add(d.snaps); sg.add(d.aimg); sg.add(d.targets.size());
+  for (const auto& t : d.targets) { sg.add(t.B); sg.add(t.bimg); sg.add(t.re); sg.add(t.im); sg.add(t.lane_stride); }
 }
 
 void sig_inj(Sig& sg, const Injection& j) {
-  sg.add(j.n_events); sg.add(j.chunk); sg.add(j.planes); sg.add(j.P); sg.add(j.B);
+  sg.add(j.n_events); sg.add(j.chunk); sg.add(j.planes); sg.add(j.P); sg.add(j.B); sg.add(j.bimg); sg.add(j.aimg);
   sg.add_vec(j.step_of_event);
 }
 

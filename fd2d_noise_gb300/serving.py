@@ -79,7 +79,7 @@ def footprint(req: Request) -> int:
     nr = max(np.asarray(req.receivers).reshape(-1, 2).shape[0], 1)
     n_dft = min(c.nt // max(c.freq_samp, 1) + 1, 1024, (2 << 30) // plane)
     n_inj = min(c.ntc // max(c.freq_samp, 1), (4 << 30) // plane)
-    per = (11 * plane + n_dft * plane + 16 * np_ * K + 2 * K * plane + n_inj * plane
+    per = (11 * plane + 3 * n_dft * plane + 16 * np_ * K + 3 * 2 * K * plane + n_inj * plane
            + 8 * nr * (c.nt + c.ntc) + 8 * np_ * (3 + np.asarray(req.source_dist).size // max(np_, 1)))
     if req.kind == "correlation":
         return int(n_ref * per + (1 << 20))
