@@ -224,18 +224,21 @@ __global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constan
     const float* s_mu = buf + T::O_MU;
     const float* s_u = buf + T::O_U;
 
-    // ---- new v on the box: each thread a 4-wide, 2-tall block ----------------------
+    // ---- new v on the box: 4-wide blocks of rows ---------------------------------------
     // DS = div_s(sxy, szy) (+ sources) (+ injection); v = (v + DS*dt/rho)*taper.
     // Sums are formed in the same order as the scalar form (m = 1..R).
     {
-      constexpr int NQ = W / 4, NRB = (T::BH + 1) / 2;
-      if (tid < NQ * NRB) {
-        const int q = tid % NQ, r0 = 2 * (tid / NQ);
+      // work item: a 4-wide block of NB1 rows; NB1 = 1 keeps the register
+      // footprint small enough for 6 resident CTAs per SM without spills
+      constexpr int NB1 = 1;
+      constexpr int NQ = W / 4, NRB = (T::BH + NB1 - 1) / NB1;
+      for (int item = tid; item < NQ * NRB; item += NT) {
+        const int q = item % NQ, r0 = NB1 * (item / NQ);
         const int c0 = 4 * q;  // box column of element 0; global x = vx0 + c0 + e
-        float xs[2][12];       // sxy columns c0 .. c0+11 (x from x0-8 = box column - 4)
-        float zs[2 * R + 1][4];
+        float xs[NB1][12];     // sxy columns c0 .. c0+11 (x from x0-8 = box column - 4)
+        float zs[2 * R + NB1 - 1][4];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < NB1; ++k) {
           const int rr = min(r0 + k, T::BH - 1);
           const float4* rowp = reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + c0);
 #pragma unroll
@@ -245,14 +248,14 @@ __global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constan
           }
         }
 #pragma unroll
-        for (int k = 0; k < 2 * R + 1; ++k) {
+        for (int k = 0; k < 2 * R + NB1 - 1; ++k) {
           // szy row r0 + k holds szy(gz0 + k - R) for gz0 = global z of row r0
           const int rr = min(r0 + k, T::SZH - 1);
           const float4 f = *reinterpret_cast<const float4*>(s_szy + rr * W + c0);
           zs[k][0] = f.x; zs[k][1] = f.y; zs[k][2] = f.z; zs[k][3] = f.w;
         }
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < NB1; ++k) {
           const int rr = r0 + k;
           if (rr >= T::BH) break;
           const int gz = bz0 + rr;
