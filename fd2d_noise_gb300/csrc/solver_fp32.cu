@@ -51,8 +51,10 @@ struct Grid32 {
   int* err;       // device error flag (bounded waits)
 };
 
-// Shared-memory layout of one tile (floats, regions 128-byte aligned).
-template <int R>
+// Shared-memory layout of one tile (floats, regions 128-byte aligned); the
+// displacement (HU) and injection (HI) regions exist only in the variants
+// that load them.
+template <int R, bool HU = true, bool HI = true>
 struct Tile {
   static constexpr int BWc = TX + 2 * R - 1;  // computed v box width (x from x0-R+1)
   static constexpr int BH = TZ + 2 * R - 1;   // box rows (z from z0-R+1)
@@ -66,11 +68,14 @@ struct Tile {
   static constexpr int O_B = O_V + al(BH * BWa);
   static constexpr int O_T = O_B + al(BH * BWa);
   static constexpr int O_I = O_T + al(BH * BWa);
-  static constexpr int O_MU = O_I + al(BH * BWa);
+  static constexpr int O_MU = O_I + (HI ? al(BH * BWa) : 0);
   static constexpr int O_U = O_MU + al(TZ * TX);
-  static constexpr int O_VN = O_U + al(TZ * TX);
+  static constexpr int O_VN = O_U + (HU ? al(TZ * TX) : 0);
   static constexpr int TOTAL = O_VN + al(BH * BWa);  // new v on the 40-wide box (x from x0-4)
   static constexpr int BYTES = TOTAL * 4 + 128;      // + alignment slack
+  // resident CTAs per SM the shared memory allows (228 KB per SM, 1 KB per CTA
+  // reserved, ~1 KB of static shared variables), at most 8
+  static constexpr int CTAS = (228 * 1024) / (BYTES + 2048) < 8 ? (228 * 1024) / (BYTES + 2048) : 8;
 };
 
 struct alignas(64) StepMaps {
@@ -109,17 +114,17 @@ __device__ __forceinline__ void tile_coords(const Grid32& G, int t, int& x0, int
   x0 = (r - (r / G.ntx) * G.ntx) * TX;
 }
 
-template <int R>
+template <int R, bool HU, bool HI>
 __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, const Step32& S, float* buf,
                                            uint64_t* bar, int t, bool coeffs, bool fields) {
-  using T = Tile<R>;
+  using T = Tile<R, HU, HI>;
   int x0, z0, lane;
   tile_coords<R>(G, t, x0, z0, lane);
   const int bz0 = z0 - R + 1;
   if (coeffs) {
     uint32_t bytes = 4u * (T::BH * T::SXWa + T::SZH * T::BWa + 3 * T::BH * T::BWa + TZ * TX);
-    if (S.has_u) bytes += 4u * TZ * TX;
-    if (S.inj_plane >= 0) bytes += 4u * T::BH * T::BWa;
+    if (HU) bytes += 4u * TZ * TX;
+    if (HI) bytes += 4u * T::BH * T::BWa;
     mbar_expect_tx(bar, bytes);
     tma_load_3d(buf + T::O_B, &M.b, x0 - 4, bz0, lane, bar);
     tma_load_3d(buf + T::O_T, &M.taper, x0 - 4, bz0, lane, bar);
@@ -129,14 +134,15 @@ __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, c
     tma_load_3d(buf + T::O_SXY, &M.sxy, x0 - 8, bz0, lane, bar);
     tma_load_3d(buf + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, lane, bar);
     tma_load_3d(buf + T::O_V, &M.v, x0 - 4, bz0, lane, bar);
-    if (S.has_u) tma_load_3d(buf + T::O_U, &M.u, x0, z0, lane, bar);
-    if (S.inj_plane >= 0) tma_load_3d(buf + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, bar);
+    if (HU) tma_load_3d(buf + T::O_U, &M.u, x0, z0, lane, bar);
+    if (HI) tma_load_3d(buf + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, bar);
   }
 }
 
-template <int R>
-__global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constant__ StepMaps M, Step32 S) {
-  using T = Tile<R>;
+template <int R, bool HU, bool HI>
+__global__ __launch_bounds__(NT, Tile<R, HU, HI>::CTAS) void k32_step(
+    Grid32 G, const __grid_constant__ StepMaps M, Step32 S) {
+  using T = Tile<R, HU, HI>;
   extern __shared__ __align__(128) unsigned char sm_raw[];
   // TMA destinations: 128-byte aligned regardless of the static smem in front
   // (offset arithmetic on the shared array keeps the pointer in the shared
@@ -158,7 +164,7 @@ __global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constan
   const int n_tiles = G.ntx * G.ntz * G.S;
   constexpr int W = T::BWa;  // 40: row stride of the box regions
   float* s_vn = sm + T::O_VN;
-  const bool inj = S.inj_plane >= 0;
+  constexpr bool inj = HI;
 
   const int t = blockIdx.x;
   if (t >= n_tiles) return;
@@ -169,7 +175,7 @@ __global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constan
     fence_mbar_init();
     // coefficient planes are not written by the time loop: their loads may
     // overlap the end of the previous step (programmatic dependent launch)
-    issue_tile<R>(G, M, S, sm, &bar, t, true, false);
+    issue_tile<R, HU, HI>(G, M, S, sm, &bar, t, true, false);
   }
   {
     const float* buf = sm;
@@ -203,7 +209,7 @@ __global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constan
     // Everything below reads what the previous launch wrote, or writes what it
     // read (ping-pong buffers): wait for it to complete.
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    if (tid == 0) issue_tile<R>(G, M, S, sm, &bar, t, false, true);
+    if (tid == 0) issue_tile<R, HU, HI>(G, M, S, sm, &bar, t, false, true);
     // one warp waits for the tile (suspending); the others wait at the barrier
     bool ok = true;
     if (tid < 32) ok = mbar_wait_bounded_sleep(&bar, 0);
@@ -333,7 +339,7 @@ __global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constan
         const float4 sx4 = *reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + 8 + 4 * q);
         const float4 sz4 = *reinterpret_cast<const float4*>(s_szy + (tz + 2 * R - 1) * W + 4 + 4 * q);
         float4 u4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (S.has_u) u4 = *reinterpret_cast<const float4*>(s_u + tz * TX + 4 * q);
+        if (HU) u4 = *reinterpret_cast<const float4*>(s_u + tz * TX + 4 * q);
         const float mu[4] = {mu4.x, mu4.y, mu4.z, mu4.w}, sxo[4] = {sx4.x, sx4.y, sx4.z, sx4.w};
         const float szo[4] = {sz4.x, sz4.y, sz4.z, sz4.w}, uo[4] = {u4.x, u4.y, u4.z, u4.w};
         const bool zin = j >= R - 1 && j <= nz - R - 1;
@@ -349,7 +355,7 @@ __global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constan
           for (int m = 1; m <= R; ++m) az += cf[m - 1] * (vz[R - 1 + m][e] - vz[R - m][e]);
           nsx[e] = (i >= R - 1 && i <= nx - R - 1) ? sxo[e] + mu[e] * (ax * inv_dx) : sxo[e];
           nsz[e] = zin ? szo[e] + mu[e] * (az * inv_dz) : szo[e];
-          nu[e] = S.has_u ? uo[e] + vn[e] * gdt : vn[e];
+          nu[e] = HU ? uo[e] + vn[e] * gdt : vn[e];
         }
         const int64_t p = lo + i0 + (int64_t)P * j;
         if (i0 + 3 < nx) {
@@ -363,7 +369,7 @@ __global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constan
               if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
           }
           if (j <= nz - 2) *reinterpret_cast<float4*>(S.szyo + p) = make_float4(nsz[0], nsz[1], nsz[2], nsz[3]);
-          if (S.has_u) *reinterpret_cast<float4*>(S.uo + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
+          if (HU) *reinterpret_cast<float4*>(S.uo + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
           if (S.snap_dft) *reinterpret_cast<float4*>(S.snap_dft + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
         } else {
 #pragma unroll
@@ -372,7 +378,7 @@ __global__ __launch_bounds__(NT, 6) void k32_step(Grid32 G, const __grid_constan
             S.vo[p + e] = vn[e];
             if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
             if (j <= nz - 2) S.szyo[p + e] = nsz[e];
-            if (S.has_u) S.uo[p + e] = nu[e];
+            if (HU) S.uo[p + e] = nu[e];
             if (S.snap_dft) S.snap_dft[p + e] = nu[e];
           }
         }
@@ -579,29 +585,54 @@ struct Run {
 // Step launches carry the programmatic-stream-serialization attribute: a step
 // may be scheduled while the previous one drains; k32_step waits for it with
 // griddepcontrol.wait before touching the fields.
-template <int R>
-void launch_step_r(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
+template <int R, bool HU, bool HI>
+void launch_step_v(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = r.sgrid;
   cfg.blockDim = dim3(NT);
-  cfg.dynamicSmemBytes = Tile<R>::BYTES;
+  cfg.dynamicSmemBytes = Tile<R, HU, HI>::BYTES;
   cfg.stream = ctx->stream;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k32_step<R>, r.G, r.maps[par], s);
+  cudaLaunchKernelEx(&cfg, k32_step<R, HU, HI>, r.G, r.maps[par], s);
+}
+
+template <int R>
+void launch_step_r(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
+  const bool hi = s.inj_plane >= 0;
+  if (s.has_u) {
+    if (hi) launch_step_v<R, true, true>(ctx, r, par, s);
+    else launch_step_v<R, true, false>(ctx, r, par, s);
+  } else {
+    if (hi) launch_step_v<R, false, true>(ctx, r, par, s);
+    else launch_step_v<R, false, false>(ctx, r, par, s);
+  }
+}
+
+template <int R>
+fd2d_status step_attributes_r(fd2d_ctx* ctx) {
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, false, false>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, false, true>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, true, false>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, true, true>::BYTES));
+  return FD2D_OK;
 }
 
 // Opt the step kernels in to their dynamic shared memory (once, before any capture).
 fd2d_status step_attributes(fd2d_ctx* ctx) {
   static bool done = false;
   if (done) return FD2D_OK;
-  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<1>::BYTES));
-  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<2>::BYTES));
-  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<3>::BYTES));
-  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<4>::BYTES));
+  FD2D_TRY(step_attributes_r<1>(ctx));
+  FD2D_TRY(step_attributes_r<2>(ctx));
+  FD2D_TRY(step_attributes_r<3>(ctx));
+  FD2D_TRY(step_attributes_r<4>(ctx));
   done = true;
   return FD2D_OK;
 }
@@ -1485,10 +1516,10 @@ extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg,
     s.szyo = r.szy[1 - par];
     s.uo = nullptr;
     switch (r.R) {
-      case 1: k32_step<1><<<r.sgrid, NT, Tile<1>::BYTES, stream>>>(r.G, r.maps[par], s); break;
-      case 2: k32_step<2><<<r.sgrid, NT, Tile<2>::BYTES, stream>>>(r.G, r.maps[par], s); break;
-      case 3: k32_step<3><<<r.sgrid, NT, Tile<3>::BYTES, stream>>>(r.G, r.maps[par], s); break;
-      default: k32_step<4><<<r.sgrid, NT, Tile<4>::BYTES, stream>>>(r.G, r.maps[par], s); break;
+      case 1: k32_step<1, false, false><<<r.sgrid, NT, Tile<1, false, false>::BYTES, stream>>>(r.G, r.maps[par], s); break;
+      case 2: k32_step<2, false, false><<<r.sgrid, NT, Tile<2, false, false>::BYTES, stream>>>(r.G, r.maps[par], s); break;
+      case 3: k32_step<3, false, false><<<r.sgrid, NT, Tile<3, false, false>::BYTES, stream>>>(r.G, r.maps[par], s); break;
+      default: k32_step<4, false, false><<<r.sgrid, NT, Tile<4, false, false>::BYTES, stream>>>(r.G, r.maps[par], s); break;
     }
     FD2D_CUDA(nullptr, cudaGetLastError());
   }
