@@ -173,6 +173,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=40,
+                    help="requests of the serving measurement (0: skip it)")
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="mean Poisson arrival rate [1/s]")
     ap.add_argument("--no-timing", action="store_true",
                     help="do not bracket kernels with CUDA events (no roofline)")
     args = ap.parse_args()
@@ -192,6 +195,9 @@ def main():
 
     build()
     torch.cuda.set_device(local)
+    if hasattr(w, "stations"):
+        run_batch_workload(args, w, local, world, rank)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -319,6 +325,9 @@ def main():
     if rank == 0 and not args.no_e2e:
         result["e2e"] = e2e(args, w, dev)
 
+    if rank == 0 and args.serve_requests > 0:
+        result["serving"] = serving_run(args, dev)
+
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         v, dt, gpt, ccfg = cpu_sample(w, args.cpu_nt, threads)
@@ -331,6 +340,112 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_batch_workload(args, w, dev, world, rank):
+    """Reference stations on uneven grids in one fd2d_correlation_batch call per
+    step (device buffers); stations of one configuration share launches, the
+    others run as parallel graph branches."""
+    import numpy as np
+    import torch
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    st0 = w.stations[0]
+    sess = DeviceSession(st0.cfg, dev, "fp32")
+    cache = {}
+    batch = []
+    for s in w.stations:
+        key = id(s.mu)
+        if key not in cache:
+            cache[key] = dict(mu=to_device(s.mu, np.float64, dev), rho=to_device(s.rho, np.float64, dev),
+                              spectrum=to_device(s.spectrum, np.float64, dev),
+                              source_dist=to_device(s.source_dist, np.float64, dev),
+                              rec=to_device(s.receivers, np.float64, dev))
+        c = cache[key]
+        n_dist = s.source_dist.shape[2] if s.source_dist.ndim == 3 else 1
+        batch.append(dict(cfg=s.cfg, mu=c["mu"], rho=c["rho"], spectrum=c["spectrum"], source_dist=c["source_dist"],
+                          n_dist=n_dist, src=to_device(s.ref_stations, np.float64, dev), rec=c["rec"],
+                          nr=s.receivers.shape[0],
+                          out=sess.zeros(s.receivers.shape[0] * s.cfg.ntc, torch.float64)))
+    for _ in range(max(args.warmup, 0)):
+        sess.correlation_batch(batch)
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    launches0 = sess.ctx.kernel_launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(sess.stream)
+    for _ in range(args.steps):
+        sess.correlation_batch(batch)
+    ev1.record(sess.stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    gpt = w.gpt_per_step()
+    value = world * gpt * args.steps / (ms / 1e3) / 1e9
+    sizes = {}
+    for s in w.stations:
+        sizes[s.cfg.nx] = sizes.get(s.cfg.nx, 0) + 1
+    line = {"metric": METRIC, "value": value, "unit": "Gpt-updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w.name, "stations": len(w.stations), "grids": sizes,
+                       "gpt_per_step": gpt, "launch_groups": sess.ctx.last_batch(),
+                       "l2": "inputs > L2 per step (FP64 Green spectra of every station)"},
+            "gpu_launches": sess.ctx.kernel_launches - launches0, "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def serving_run(args, dev):
+    """Continuous-batching serving loop: a seeded Poisson stream of correlation
+    (60 %), kernel (30 %) and Hessian-vector (10 %) requests, grids 256-384
+    square, nt 800-1600 (stretched to cover the 100-200 s measurement window),
+    1-4 reference stations per correlation request; p50/p99 of arrival-to-result
+    latency."""
+    import torch
+    from fd2d_noise_gb300.serving import Server, make_request, poisson_mix
+    mix = poisson_mix(args.serve_requests, args.serve_rate)
+    reqs = [make_request(kind, nx, nt, n_ref=n_ref, seed=sd) for (_, kind, nx, nt, n_ref, sd) in mix]
+    free, _ = torch.cuda.mem_get_info(dev)
+    budget = int(free * 0.6)
+    with Server(budget_bytes=budget, slots=4, device=dev) as srv:
+        # warm-up: one request of each kind alone (graph capture, tables)
+        seen = set()
+        for r in reqs:
+            if r.kind not in seen:
+                seen.add(r.kind)
+                srv.submit(r).result()
+        srv.log.clear()
+        srv.peak_running = srv.peak_bytes = 0
+        t0 = time.perf_counter()
+        futs = []
+        for (off, *_), r in zip(mix, reqs):
+            now = time.perf_counter() - t0
+            if off > now:
+                time.sleep(off - now)
+            r.arrival = time.perf_counter()
+            futs.append(srv.submit(r))
+        for f in futs:
+            f.result()
+        st = srv.latency_stats()
+    kinds = {}
+    for (kind, *_rest) in srv.log:
+        kinds[kind] = kinds.get(kind, 0) + 1
+    st.update({"offered_rate_req_s": args.serve_rate, "slots": 4, "budget_bytes": budget, "mix": kinds,
+               "workload": "synthetic Poisson stream, grids 256-384, nt 800-1600, 1-4 stations, FP32 form"})
+    return st
 
 
 def e2e(args, w, dev):

@@ -287,3 +287,63 @@ class Server:
                 "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
                 "throughput_req_s": lat.size / (t1 - t0), "gpt_per_s": gpt / (t1 - t0),
                 "peak_concurrent": self.peak_running, "peak_bytes": self.peak_bytes}
+
+
+def make_request(kind: str, nx: int, nt: int, n_ref: int = 1, K: int = 64, nr: int = 8, seed: int = 0,
+                 arrival: Optional[float] = None) -> Request:
+    """A seeded synthetic request on an nx-by-nx grid of 4e5 m: random medium
+    (5 % std), Gaussian noise source, ``n_ref`` reference stations and ``nr``
+    receivers; kernel and Hessian requests get synthetic data traces.  The
+    time axis is stretched so that it covers the 100-200 s measurement window
+    (tools/measurement/make_adjoint_sources.m:87-88)."""
+    from .config import Config, matlab_colon
+    from .media import interior_points, random_media
+    from .noise_source import make_noise_source
+    L = 4.0e5
+    dx = L / (nx - 1)
+    dt = 0.45 * dx / 4000.0
+    nt = max(int(nt), int(np.ceil(130.0 / dt)) + 1)
+    f = matlab_colon(0.01, (0.2 - 0.01) / (K - 1), 0.2)[:K]
+    cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=dt, nt=nt, order=4, f_sample=f, freq_samp=5,
+                 fw_nth=1 if kind == "hvp" else 5, absorb_width=20 * dx, source_type="gaussian")
+    mu, rho = random_media(cfg, std=0.05, corr_len=2.0e4, seed=seed)
+    sd, spec = make_noise_source("gaussian", 0, cfg,
+                                 spectrum_kw=dict(f_peak=[0.1], bandwidth=[0.03], strength=[1.0]),
+                                 x_c=[0.3 * L], z_c=[0.6 * L], width=[0.1 * L], magnitude=[6.0])
+    pts = interior_points(cfg, n_ref + nr, seed=seed + 1, margin_frac=0.2)
+    ref = pts[:n_ref]
+    recv = pts[n_ref:] if kind == "correlation" else pts
+    c_data = dmu = None
+    if kind != "correlation":
+        rng = np.random.default_rng(seed + 2)
+        n_rec = pts.shape[0] - 1
+        tt = (-(cfg.nt - 1) + np.arange(cfg.ntc)) * cfg.dt
+        c_data = np.zeros((n_ref * n_rec, cfg.ntc))
+        for r in range(c_data.shape[0]):
+            for sgn in (1.0, -1.0):
+                t0 = sgn * rng.uniform(110.0, 190.0)
+                c_data[r] += rng.uniform(0.5, 2.0) * np.exp(-((tt - t0) / 12.0) ** 2)
+        if kind == "hvp":
+            dmu = 0.01 * mu * rng.standard_normal(mu.shape)
+    r = Request(kind, cfg, mu, rho, spec, sd, ref, recv, c_data=c_data, dmu=dmu)
+    if arrival is not None:
+        r.arrival = arrival
+    return r
+
+
+def poisson_mix(n_requests: int, rate: float, seed: int = 6, sizes=(256, 320, 384), nt_range=(800, 1600),
+                mix=(0.6, 0.3, 0.1), max_ref: int = 4):
+    """[(arrival offset s, kind, nx, nt, n_ref, seed)] for a seeded Poisson stream
+    of correlation / kernel / Hessian requests in the proportions ``mix``."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    kinds = ("correlation", "kernel", "hvp")
+    for i in range(n_requests):
+        t += rng.exponential(1.0 / rate)
+        kind = kinds[int(rng.choice(3, p=np.asarray(mix) / np.sum(mix)))]
+        nx = int(rng.choice(sizes))
+        nt = int(rng.integers(nt_range[0], nt_range[1] + 1))
+        n_ref = int(rng.integers(1, max_ref + 1)) if kind == "correlation" else 1
+        out.append((t, kind, nx if kind != "hvp" else min(sizes), nt, n_ref, seed * 1000 + i))
+    return out

@@ -9,6 +9,9 @@
                             (10 % std, 20 km correlation length), ring source.
 * ``structure_512``      -- 512x512, nt 2500, snapshots every 5 steps, 200
                             frequencies, 1 reference station, 20 receivers.
+* ``batch_uneven``       -- 32 reference stations on grids of 256, 384, 512 or
+                            800 points square, nt 1500-4000, order 4, 4
+                            frequency bands (see :func:`batch_uneven`).
 
 The domain is 4e5 m square in every workload (the reference's "small setup").
 """
@@ -96,8 +99,46 @@ def structure_512(nt: int = 2500) -> Workload:
     return Workload("structure_512", cfg, mu, rho, ref, rec, spec, sd)
 
 
+@dataclasses.dataclass
+class BatchWorkload:
+    """Reference stations on grids of different sizes (one Workload per station)."""
+    name: str
+    stations: list
+
+    def gpt_per_step(self) -> int:
+        return sum(w.gpt_per_station() for w in self.stations)
+
+
+def batch_uneven(n_stations: int = 32, n_basis: int = 4, K: int = 200, nr: int = 20, seed: int = 4,
+                 nt_range=(1500, 4000), sizes=(256, 384, 512, 800)) -> BatchWorkload:
+    """Reference stations on grids drawn from ``sizes`` (square), nt uniform in
+    ``nt_range``, dt from CFL 0.5 at 4000 m/s, order 4, taper 30 points; one
+    random medium (5 % std) per grid size; the noise source has ``n_basis``
+    frequency bands (spectrum of ones, band-averaged Gaussian maps)."""
+    rng = np.random.default_rng(seed)
+    media, out = {}, []
+    for i in range(n_stations):
+        nx = int(rng.choice(sizes))
+        nt = int(rng.integers(nt_range[0], nt_range[1] + 1))
+        dx = L / (nx - 1)
+        cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.5 * dx / 4000.0, nt=nt, order=4, n_basis_fct=n_basis,
+                     f_sample=_freqs(0.01, 0.2, K), freq_samp=5, fw_nth=1, absorb_width=30 * dx,
+                     source_type="gaussian")
+        if nx not in media:
+            mu, rho = random_media(cfg, std=0.05, corr_len=2.0e4, seed=100 + nx)
+            sd, spec = make_noise_source("gaussian", n_basis, cfg,
+                                         spectrum_kw=dict(f_peak=[0.1], bandwidth=[0.03], strength=[1.0]),
+                                         x_c=[0.3 * L], z_c=[0.6 * L], width=[0.1 * L], magnitude=[6.0])
+            media[nx] = (mu, rho, sd, spec, interior_points(cfg, nr, seed=200 + nx, margin_frac=0.2))
+        mu, rho, sd, spec, rec = media[nx]
+        ref = interior_points(cfg, 1, seed=1000 + i, margin_frac=0.3)
+        out.append(Workload(f"station{i}_{nx}", cfg, mu, rho, ref, rec, spec, sd))
+    return BatchWorkload("batch_uneven", out)
+
+
 WORKLOADS: Dict[str, Callable[..., Workload]] = {
     "plain_cpu_300": plain_cpu_300,
     "single_600_o8": single_600_o8,
     "structure_512": structure_512,
+    "batch_uneven": batch_uneven,
 }
