@@ -33,6 +33,7 @@ EXPORTED = [
     "fd2d_ctx_set_timing", "fd2d_ctx_timing", "fd2d_contract_f32",
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
     "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch", "fd2d_ctx_release", "fd2d_ctx_workspace_bytes",
+    "fd2d_gaussblur2d",
 ]
 MEAS_WAVEFORM_DIFFERENCE = 0
 MEAS_LOG_AMPLITUDE_RATIO = 1
@@ -91,6 +92,7 @@ def load(path: str = LIB_PATH):
         L.fd2d_ctx_workspace_bytes.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.restype = _i64
         L.fd2d_ctx_release.argtypes = [_vp, ctypes.POINTER(_i64)]
+        L.fd2d_gaussblur2d.argtypes = [_vp, _vp, _i32, _i32, _vp, _vp, ctypes.c_double, ctypes.c_double, _vp]
         L.fd2d_last_error.argtypes = [_vp]
         L.fd2d_last_error.restype = ctypes.c_char_p
         L.fd2d_query_sizes.argtypes = [_cfgp, _i32, ctypes.POINTER(FD2DSizes)]

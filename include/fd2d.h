@@ -277,6 +277,14 @@ fd2d_status fd2d_make_adjoint_sources(fd2d_ctx* ctx, int32_t measurement, int32_
                                       const double* u, const double* u_0, const double* du, int32_t n_rec,
                                       int32_t nt, const double* t, double* misfit, double* adstf);
 
+/* ---- model maps -----------------------------------------------------------------
+ * GY = gaussblur2d(Y, x1, x2, sigma) -- tools/addons/gaussblur2d.m:2-38, FP64:
+ * Gaussian weights exp(-(d/sigma)^2/2) within sqrt(14)*sigma along each axis,
+ * normalised by the weight sums.  Y and GY are n1-by-n2; x1 (n1) and x2 (n2)
+ * the coordinates.  Arrays follow the context's memspace. */
+fd2d_status fd2d_gaussblur2d(fd2d_ctx* ctx, const double* Y, int32_t n1, int32_t n2, const double* x1,
+                             const double* x2, double sigma1, double sigma2, double* GY);
+
 /* ---- building block ----------------------------------------------------------
  * R[n*ldr + m] = sum_{k<Kd} A[k*lda + m] * B[k*ldb + n]  for m < M, n < N:
  * the split-TF32 tensor-core contraction behind the on-the-fly DFT

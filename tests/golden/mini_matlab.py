@@ -928,6 +928,14 @@ class Interpreter:
         fn = self.find_function(name)
         if fn is not None:
             return self.run_function(fn, args, nargout)
+        if name == "size" and nargout > 1 and len(args) == 1:
+            # [n1, n2, ...] = size(A): one output per dimension, the last one
+            # the product of the remaining dimensions
+            sh = list(A(args[0]).shape)
+            while len(sh) < nargout:
+                sh.append(1)
+            out = sh[:nargout - 1] + [int(np.prod(sh[nargout - 1:]))]
+            return [A(float(d)) for d in out]
         if name in BUILTINS:
             r = BUILTINS[name](*args)
             return r if isinstance(r, list) else [r]
