@@ -35,13 +35,16 @@ def _p(t) -> Optional[ctypes.c_void_p]:
 
 
 class DeviceSession:
-    def __init__(self, cfg: Config, device: int = 0, precision: str = "fp32"):
+    def __init__(self, cfg: Config, device: int = 0, precision: str = "fp32", ctx: Optional[_lib.Context] = None):
+        """``ctx``: an existing context to use (switched to device memspace and
+        this session's stream); otherwise the session creates its own."""
         import torch
         from .solvers import _prec
         self.torch = torch
         self.cfg = cfg
         self.device = device
-        self.ctx = _lib.Context(device, _prec(precision))
+        self.ctx = ctx if ctx is not None else _lib.Context(device, _prec(precision))
+        self.ctx.set_precision(_prec(precision))
         self.ctx.set_memspace(_lib.MEM_DEVICE)
         # time loops are captured as CUDA graphs, which the legacy default
         # stream does not allow: work on torch's current stream unless that is
@@ -56,7 +59,10 @@ class DeviceSession:
         self.ctx.set_precision(_prec(precision))
 
     def zeros(self, n, dtype):
-        return self.torch.zeros(int(n), dtype=dtype, device=f"cuda:{self.device}")
+        # filled on the session's stream, so the fill is ordered before the
+        # library's work on the buffer
+        with self.torch.cuda.stream(self.stream):
+            return self.torch.zeros(int(n), dtype=dtype, device=f"cuda:{self.device}")
 
     def green_outputs(self, nr: int, mode: int = 0):
         t = self.torch
@@ -70,6 +76,7 @@ class DeviceSession:
 
     def forward1_green(self, mu, rho, src, ns, rec, nr, G_re, G_im, seis, mode=0, G_out=None,
                        dmu=None, G_in=None, n_G_in=0):
+        self.ctx.set_memspace(_lib.MEM_DEVICE)  # the context may be shared with host-memspace calls
         st = self.ctx.L.fd2d_forward1_green(
             self.ctx.h, ctypes.byref(self.c), _p(mu), _p(rho), _p(src), int(ns), _p(rec), int(nr),
             int(mode), _p(dmu), _p(G_in), int(n_G_in), _p(G_re), _p(G_im), _p(G_out), _p(seis))
@@ -77,6 +84,7 @@ class DeviceSession:
 
     def forward2_correlation(self, mu, rho, G_re, G_im, spectrum, n_src, source_dist, n_dist,
                              rec, nr, seis, mode=0, C_out=None, dmu=None, C_in=None, n_C_in=0):
+        self.ctx.set_memspace(_lib.MEM_DEVICE)  # the context may be shared with host-memspace calls
         st = self.ctx.L.fd2d_forward2_correlation(
             self.ctx.h, ctypes.byref(self.c), _p(mu), _p(rho), _p(G_re), _p(G_im),
             int(self.cfg.n_sample), _p(spectrum), int(n_src), _p(source_dist), int(n_dist),
@@ -86,6 +94,7 @@ class DeviceSession:
     def noise_adjoint(self, mu, rho, u_fwd, n_u_fwd, stf_re, stf_im, stf_dims, src, ns, rec, nr,
                       spectrum, n_src, source_dist, n_dist, G_re, G_im, n_G, mode, K, sf_re, sf_im,
                       seis, u_out=None, dmu=None, u_in=None, n_u_in=0):
+        self.ctx.set_memspace(_lib.MEM_DEVICE)  # the context may be shared with host-memspace calls
         dims = (ctypes.c_int64 * 3)(*[int(v) for v in stf_dims])
         st = self.ctx.L.fd2d_noise_adjoint(
             self.ctx.h, ctypes.byref(self.c), _p(mu), _p(rho), _p(u_fwd), int(n_u_fwd),
@@ -97,6 +106,7 @@ class DeviceSession:
     def correlation_batch(self, jobs):
         """Runs fd2d_correlation_batch.  ``jobs``: list of dicts with keys cfg (Config),
         mu, rho, spectrum, n_src, source_dist, n_dist, src, rec, nr, out (tensors)."""
+        self.ctx.set_memspace(_lib.MEM_DEVICE)
         arr = (_lib.FD2DJob * len(jobs))()
         keep = []
         for j, d in enumerate(jobs):

@@ -36,6 +36,7 @@ class Backend:
     correlation: Callable
     adjoint: Callable
     measure: Callable
+    session: object = None
 
 
 def gpu_backend(cfg, precision: str = "fp32", device: int = 0) -> Backend:
@@ -47,6 +48,107 @@ def gpu_backend(cfg, precision: str = "fp32", device: int = 0) -> Backend:
         adjoint=lambda *a: solvers.run_noise_adjoint(*a, **kw),
         measure=lambda u, u0, du, t, vd, m, order: measurements.make_adjoint_sources(
             u, u0, du, t, vd, m, None, None, order, device=device))
+
+
+class DeviceSpectrum:
+    """A complex nx-by-nz-by-K spectrum kept on the device as real and
+    imaginary FP64 planes (flat tensors in MATLAB order)."""
+
+    def __init__(self, re, im, planes: int):
+        self.re, self.im, self.planes = re, im, planes
+
+
+def device_backend(cfg, precision: str = "fp32", device: int = 0, ctx=None) -> Backend:
+    """Solvers in device memspace: spectra and snapshot stacks stay on the GPU
+    between the runs of a station (DeviceSpectrum and float32 tensors); models,
+    positions and traces cross as numpy arrays."""
+    import torch
+    from . import measurements
+    from .config import n_fw_corr, n_fw_green, n_kernel_planes
+    from .device import DeviceSession, to_device
+    sess = DeviceSession(cfg, device, precision, ctx=ctx)
+    np_, K, nt, ntc = cfg.npts, cfg.n_sample, cfg.nt, cfg.ntc
+    keep = {}
+
+    def up(a):
+        if a is None or isinstance(a, torch.Tensor):
+            return a
+        key = id(a)
+        if key not in keep:
+            keep[key] = (a, to_device(np.asarray(a, dtype=np.float64), np.float64, device))
+        return keep[key][1]
+
+    def pts(a):
+        if a is None or np.size(a) == 0:
+            return None, 0
+        a = np.asarray(a, dtype=np.float64).reshape(-1, 2)
+        return to_device(a, np.float64, device), a.shape[0]
+
+    def planes(x):
+        return 0 if x is None else x.numel() // np_
+
+    def host(tns, shape):
+        sess.ctx.synchronize()
+        return tns.cpu().numpy().reshape(shape, order="F")
+
+    def forward1(mu, rho, src, rec, mode, dmu, G_in):
+        s, ns = pts(src)
+        r, nr = pts(rec)
+        G_re, G_im = sess.zeros(np_ * K, torch.float64), sess.zeros(np_ * K, torch.float64)
+        G_out = sess.zeros(np_ * n_fw_green(cfg), torch.float32) if mode else None
+        seis = sess.zeros(max(nr, 1) * nt, torch.float64)
+        sess.forward1_green(up(mu), up(rho), s, ns, r, nr, G_re, G_im, seis, mode, G_out, up(dmu), G_in,
+                            planes(G_in))
+        return DeviceSpectrum(G_re, G_im, K), G_out, host(seis, (max(nr, 1), nt))
+
+    def correlation(mu, rho, G_fft, spectrum, source_dist, rec, mode, dmu, C_in):
+        r, nr = pts(rec)
+        spec = np.asarray(spectrum, dtype=np.float64).reshape(K, -1, order="F")
+        seis = sess.zeros(max(nr, 1) * ntc, torch.float64)
+        C_out = sess.zeros(np_ * n_fw_corr(cfg), torch.float32) if mode else None
+        sess.forward2_correlation(up(mu), up(rho), G_fft.re, G_fft.im, up(spec), spec.shape[1], up(source_dist),
+                                  np.size(source_dist) // np_, r, nr, seis, mode, C_out, up(dmu), C_in,
+                                  planes(C_in))
+        return host(seis, (max(nr, 1), ntc)), C_out
+
+    def adjoint(mu, rho, u_fwd, stf, src, rec, spectrum, source_dist, G_fft, mode, dmu, u_in):
+        s, ns = pts(src)
+        r, nr = pts(rec)
+        if isinstance(stf, DeviceSpectrum):
+            stf_re, stf_im, dims = stf.re, stf.im, (cfg.nx, cfg.nz, stf.planes)
+        elif stf is None or np.size(stf) == 0:
+            stf_re = stf_im = None
+            dims = (0, 0, 0)
+        else:
+            st = np.asarray(stf)
+            stf_re, stf_im = up(np.ascontiguousarray(st.real)), up(np.ascontiguousarray(st.imag))
+            dims = (st.shape[0], st.shape[1], 1)
+        spec = None if spectrum is None else np.asarray(spectrum, dtype=np.float64).reshape(K, -1, order="F")
+        Kp = n_kernel_planes(cfg)
+        Kout = sess.zeros(np_ * Kp, torch.float64)
+        sf_re, sf_im = sess.zeros(np_ * K, torch.float64), sess.zeros(np_ * K, torch.float64)
+        u_out = sess.zeros(np_ * n_fw_corr(cfg), torch.float32) if mode in (11, 13) else None
+        seis = sess.zeros(max(nr, 1) * ntc, torch.float64)
+        G_re = G_fft.re if G_fft is not None else None
+        G_im = G_fft.im if G_fft is not None else None
+        sess.noise_adjoint(up(mu), up(rho), u_fwd, planes(u_fwd), stf_re, stf_im, dims, s, ns, r, nr, up(spec),
+                           0 if spec is None else spec.shape[1], up(source_dist),
+                           0 if source_dist is None else np.size(source_dist) // np_, G_re, G_im,
+                           0 if G_fft is None else G_fft.planes, mode, Kout, sf_re, sf_im, seis, u_out,
+                           up(dmu), u_in, planes(u_in))
+        return host(Kout, (cfg.nx, cfg.nz, Kp)), DeviceSpectrum(sf_re, sf_im, K), u_out, None
+
+    def measure(u, u0, du, t, vd, m, order):
+        return measurements.make_adjoint_sources(u, u0, du, t, vd, m, None, None, order, device=device)
+
+    be = Backend(forward1=forward1, correlation=correlation, adjoint=adjoint, measure=measure)
+    be.session = sess
+    return be
+
+
+def _sum(a, b):
+    """a + b for device tensors or host arrays (stored fields of Born runs)."""
+    return b if a is None else a + b
 
 
 def receivers_of(array, src):
@@ -65,7 +167,7 @@ def eval_objective_and_gradient(mu, rho, spectrum, source_dist, ref_stat, array,
     only_objective), c_all n_ref*n_rec-by-nt)."""
     if type not in ("source", "structure", "joint"):
         raise ValueError("type must be 'source', 'structure' or 'joint'")
-    be = backend or gpu_backend(cfg, precision, device)
+    be = backend or device_backend(cfg, precision, device)
     ref_stat = np.asarray(ref_stat, dtype=np.float64).reshape(-1, 2)
     t = np.asarray(t, dtype=np.float64).ravel()
     nt = t.size
@@ -130,7 +232,7 @@ def eval_hessian_vector_product(mu, rho, spectrum, source_dist, ref_stat, array,
         raise ValueError("type must be 'source', 'structure' or 'joint'")
     if cfg.fw_nth != 1:
         raise ValueError("the Hessian-vector product needs fw_nth == 1 (Born runs read every step)")
-    be = backend or gpu_backend(cfg, precision, device)
+    be = backend or device_backend(cfg, precision, device)
     ref_stat = np.asarray(ref_stat, dtype=np.float64).reshape(-1, 2)
     t = np.asarray(t, dtype=np.float64).ravel()
     nt = t.size
@@ -158,7 +260,7 @@ def eval_hessian_vector_product(mu, rho, spectrum, source_dist, ref_stat, array,
         if has_ds:
             c2, dC2 = be.correlation(mu, rho, G_fft, spectrum, source_dist_pert, rec, 1, None, None)
             c_pert = c_pert + np.asarray(c2).reshape(n_rec, nt)
-            dC = dC2 if dC is None else np.asarray(dC) + np.asarray(dC2)
+            dC = _sum(dC, dC2)
 
         def adstf(order):
             _, a_s = be.measure(c_ref, data, c_pert, t, veldis, measurement_source, order)
@@ -184,7 +286,7 @@ def eval_hessian_vector_product(mu, rho, spectrum, source_dist, ref_stat, array,
                 K2b, _, pb, _ = be.adjoint(mu, rho, G, uT, rec, None, spectrum, source_dist_pert, None, 11, None,
                                            None)
                 K2 = K2 + np.asarray(K2b, dtype=np.float64)
-                p = pb if p is None else np.asarray(p) + np.asarray(pb)
+                p = _sum(p, pb)
         # BLACK: k
         K3, kT, _, _ = be.adjoint(mu, rho, C, a2, rec, None, spectrum, None, G_fft, 12, dmu if has_dmu else None,
                                   u_dag)

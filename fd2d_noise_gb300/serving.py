@@ -94,20 +94,23 @@ def run_request(req: Request, precision: str = "fp32", device: int = 0):
     """Runs one request on the calling thread's bound context (see
     solvers.bound_context) and returns its result dict."""
     from . import objective
+    from .solvers import context
     t = (-(req.cfg.nt - 1) + np.arange(req.cfg.ntc)) * req.cfg.dt
     if req.kind == "correlation":
         return {"correlations": _correlations(req, precision, device)}
+    # kernel and Hessian requests keep spectra and snapshot stacks on the device
+    be = objective.device_backend(req.cfg, precision, device, ctx=context(device, precision))
     if req.kind == "kernel":
         j, g, c = objective.eval_objective_and_gradient(
             req.mu, req.rho, req.spectrum, req.source_dist, req.ref_stat, req.receivers, req.c_data, t,
             cfg=req.cfg, type="structure", measurement_source=req.measurement,
-            measurement_structure=req.measurement, weighting=req.weighting, precision=precision, device=device)
+            measurement_structure=req.measurement, weighting=req.weighting, backend=be)
         return {"misfit": j, "gradient": g, "correlations": c}
     if req.kind == "hvp":
         H = objective.eval_hessian_vector_product(
             req.mu, req.rho, req.spectrum, req.source_dist, req.ref_stat, req.receivers, req.c_data, t, req.dmu,
             cfg=req.cfg, type="structure", measurement_source=req.measurement,
-            measurement_structure=req.measurement, weighting=req.weighting, precision=precision, device=device)
+            measurement_structure=req.measurement, weighting=req.weighting, backend=be)
         return {"hvp": H}
     raise ValueError(f"unknown request kind {req.kind!r}")
 

@@ -75,15 +75,18 @@ def test_oracle_gradient_matches_finite_differences():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("memspace", ["device", "host"])
 @pytest.mark.parametrize("type", ["structure", "joint", "source"])
-def test_gpu_objective_matches_oracle(fd2d_lib, type):
+def test_gpu_objective_matches_oracle(fd2d_lib, type, memspace):
+    from fd2d_noise_gb300.objective import device_backend, gpu_backend
     cfg = cfg4()
     p = problem(cfg)
     be = oracle_backend(cfg)
     _, _, c_data = run(cfg, p, p["mu_true"], np.zeros((3, cfg.ntc)), be, only=True)
     jr, gr, cr = run(cfg, p, p["mu0"], c_data, be, type=type)
     for prec, tol in (("fp64", 1e-10), ("fp32", 1e-4)):
-        j, g, c = run(cfg, p, p["mu0"], c_data, precision=prec, type=type)
+        gb = (device_backend if memspace == "device" else gpu_backend)(cfg, prec)
+        j, g, c = run(cfg, p, p["mu0"], c_data, gb, type=type)
         assert abs(j - jr) <= tol * abs(jr), (prec, j, jr)
         assert np.linalg.norm(c - cr) <= tol * np.linalg.norm(cr), prec
         for q in range(g.shape[2]):
