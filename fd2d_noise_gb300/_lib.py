@@ -33,7 +33,7 @@ EXPORTED = [
     "fd2d_ctx_set_timing", "fd2d_ctx_timing", "fd2d_contract_f32",
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
     "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch", "fd2d_ctx_release", "fd2d_ctx_workspace_bytes",
-    "fd2d_gaussblur2d",
+    "fd2d_gaussblur2d", "fd2d_ctx_set_chunks",
 ]
 MEAS_WAVEFORM_DIFFERENCE = 0
 MEAS_LOG_AMPLITUDE_RATIO = 1

@@ -116,6 +116,8 @@ struct fd2d_ctx {
   // fork the jobs' loops into parallel branches of one captured graph
   std::string ws_prefix;
   int64_t mem_budget = 0;  // batch device-memory budget (0: 80 % of free memory)
+  int32_t max_dft_chunk = 0;  // snapshots per DFT contraction (0: 1024, within 2 GiB)
+  int32_t max_inj_chunk = 0;  // resident injection planes (0: within 4 GiB)
   std::vector<int32_t> last_lanes;  // lanes of each launch group of the last batch
   std::vector<cudaStream_t> side_streams;
   std::vector<cudaEvent_t> fork_events;

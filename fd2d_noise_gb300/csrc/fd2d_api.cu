@@ -830,6 +830,14 @@ extern "C" int32_t fd2d_ctx_last_batch(const fd2d_ctx* ctx, int32_t* lanes, int3
   return n;
 }
 
+extern "C" fd2d_status fd2d_ctx_set_chunks(fd2d_ctx* ctx, int32_t max_snapshots, int32_t max_injection_planes) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  if (max_snapshots < 0 || max_injection_planes < 0) return set_error(ctx, FD2D_ERR_ARG, "negative chunk size");
+  ctx->max_dft_chunk = max_snapshots;
+  ctx->max_inj_chunk = max_injection_planes;
+  return FD2D_OK;
+}
+
 extern "C" fd2d_status fd2d_ctx_set_memory_budget(fd2d_ctx* ctx, int64_t bytes) {
   if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
   if (bytes < 0) return set_error(ctx, FD2D_ERR_ARG, "negative memory budget");

@@ -881,6 +881,7 @@ fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, Run& r, const doub
   FD2D_TRY(contract_image(ctx, ctx->stream, inj.B, inj.n_events, inj.n_events, 2 * K, inj.bimg));
   const size_t cap = (size_t)4 << 30;  // resident injection planes <= 4 GiB
   inj.chunk = (int)std::max<int64_t>(1, std::min<int64_t>(inj.n_events, (int64_t)(cap / (sps * 4))));
+  if (ctx->max_inj_chunk > 0) inj.chunk = std::min(inj.chunk, (int)ctx->max_inj_chunk);
   // chunks start on column tiles of the image
   if (inj.chunk < inj.n_events) inj.chunk = std::max(CONTRACT_BN, inj.chunk / CONTRACT_BN * CONTRACT_BN);
   FD2D_TRY(workspace_t(ctx, "f32.inj", (size_t)sps * inj.chunk, &inj.planes));
@@ -933,7 +934,8 @@ fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
   if (n_events == 0) return FD2D_OK;
   const size_t cap = (size_t)2 << 30;  // snapshot chunk <= 2 GiB
   const int64_t sps = r.lanes_ps();
-  d.T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)n_events, (int64_t)1024, (int64_t)(cap / (sps * 4))}));
+  const int64_t lim = ctx->max_dft_chunk > 0 ? ctx->max_dft_chunk : 1024;
+  d.T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)n_events, lim, (int64_t)(cap / (sps * 4))}));
   // chunks start on K blocks of the coefficient image
   if (d.T < n_events) d.T = std::max(CONTRACT_BK, d.T / CONTRACT_BK * CONTRACT_BK);
   FD2D_TRY(workspace_t(ctx, "f32.dft_snaps", (size_t)sps * d.T, &d.snaps));

@@ -112,6 +112,12 @@ fd2d_status fd2d_ctx_set_memspace(fd2d_ctx* ctx, int32_t memspace);
 fd2d_status fd2d_ctx_set_precision(fd2d_ctx* ctx, int32_t precision);
 /* Wait for all work queued on the context's stream. */
 fd2d_status fd2d_ctx_synchronize(fd2d_ctx* ctx);
+/* Device-memory bounds of the FP32 form: at most `max_snapshots` stored
+ * snapshots per DFT contraction (rounded down to a multiple of 32; 0 = 1024)
+ * and `max_injection_planes` resident injection planes (rounded down to a
+ * multiple of 128; 0 = as many as fit in 4 GiB).  Smaller chunks use less
+ * memory at the cost of more, smaller contractions. */
+fd2d_status fd2d_ctx_set_chunks(fd2d_ctx* ctx, int32_t max_snapshots, int32_t max_injection_planes);
 /* Device memory the context keeps between calls (workspace buffers). */
 int64_t fd2d_ctx_workspace_bytes(const fd2d_ctx* ctx);
 /* Wait for the stream, then free the workspace and the cached CUDA graphs;
