@@ -21,6 +21,7 @@
 // context's error flag, the CTA lets its own copies land (bounded) and frees
 // its TMEM.
 #include "contract.cuh"
+#include "fp_bits.cuh"
 #include "tma.cuh"
 
 #include <algorithm>
@@ -306,7 +307,7 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
             }
 #pragma unroll
             for (int j = 0; j < 8; ++j)
-              if (p[j]) *p[j] = old[j] + (double)v[gg + j];
+              if (p[j]) *p[j] = a.overwrite ? widen_exact(v[gg + j]) : old[j] + widen_exact(v[gg + j]);
           }
         }
       }

@@ -30,6 +30,7 @@
 // cached CUDA graphs (run_captured).
 #include "common.cuh"
 #include "contract.cuh"
+#include "fp_bits.cuh"
 #include "tma.cuh"
 
 #include <algorithm>
@@ -509,12 +510,21 @@ __global__ void k32_pitched(const double* a, double s, int nx, int nz, int P, fl
   out[i + (int64_t)P * j] = i < nx ? (float)(s * a[i + (int64_t)nx * j]) : 0.f;
 }
 
-// P planes of the field source: P_k = spec(k) * (sum_b M(k,b) sd_b) * (Xre_k + i*sign*Xim_k)
-// as 2K pitched float planes [Re P_0..Re P_{K-1}, Im P_0..Im P_{K-1}], plane stride ps.
-__global__ void k32_make_P(int K, int ncol, const double* __restrict__ M, const double* __restrict__ sd,
-                           const double* __restrict__ spec, const double* __restrict__ Xre,
-                           const double* __restrict__ Xim, double sign, int nx, int nz, int P, int64_t ps,
-                           float* __restrict__ Pl) {
+// Band weights of the field source: W(k,b) = spec(k) * M(k,b), FP32 (K x ncol).
+__global__ void k32_band_weights(int K, int ncol, const double* M, const double* spec, float* W) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= K * ncol) return;
+  const int k = e % K;
+  W[e] = narrow_rn(spec[k] * M[e]);
+}
+
+// P planes of the field source: P_k = (sum_b W(k,b) sd_b) * (Xre_k + i*sign*Xim_k)
+// as 2K pitched float planes [Re P_0..Re P_{K-1}, Im P_0..Im P_{K-1}], plane
+// stride ps.  FP32 arithmetic on narrowed inputs (the planes are FP32 anyway):
+// the FP64 pipe of this part would otherwise bound the kernel.
+__global__ void k32_make_P(int K, int ncol, const float* __restrict__ W, const double* __restrict__ sd,
+                           const double* __restrict__ Xre, const double* __restrict__ Xim, float sign, int nx,
+                           int nz, int P, int64_t ps, float* __restrict__ Pl) {
   const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
   if (i >= P || j >= nz) return;
   const int64_t q = i + (int64_t)P * j;
@@ -523,8 +533,8 @@ __global__ void k32_make_P(int K, int ncol, const double* __restrict__ M, const 
     return;
   }
   const int64_t np = (int64_t)nx * nz, p = i + (int64_t)nx * j;
-  double sdv[8];
-  for (int b = 0; b < ncol && b < 8; ++b) sdv[b] = sd[p + np * b];
+  float sdv[8];
+  for (int b = 0; b < ncol && b < 8; ++b) sdv[b] = narrow_rn(sd[p + np * b]);
   // groups of 4 frequencies: all 8 spectrum loads are issued before any store
   constexpr int G = 4;
   for (int k0 = 0; k0 < K; k0 += G) {
@@ -539,11 +549,11 @@ __global__ void k32_make_P(int K, int ncol, const double* __restrict__ M, const 
     for (int g = 0; g < G; ++g) {
       const int k = k0 + g;
       if (k >= K) break;
-      double dist = 0.0;
-      for (int b = 0; b < ncol; ++b) dist += M[k + (int64_t)K * b] * (b < 8 ? sdv[b] : sd[p + np * b]);
-      const double Rk = spec[k] * dist;
-      Pl[q + ps * k] = (float)(Rk * xr[g]);
-      Pl[q + ps * (K + k)] = (float)(Rk * sign * xi[g]);
+      float dist = 0.f;
+      for (int b = 0; b < ncol; ++b)
+        dist += W[k + (int64_t)K * b] * (b < 8 ? sdv[b] : narrow_rn(sd[p + np * b]));
+      Pl[q + ps * k] = dist * narrow_rn(xr[g]);
+      Pl[q + ps * (K + k)] = dist * (sign * narrow_rn(xi[g]));
     }
   }
 }
@@ -856,9 +866,14 @@ fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, Run& r, const doub
   const int64_t sps = r.lanes_ps();
   FD2D_TRY(workspace_t(ctx, "f32.P", (size_t)sps * 2 * K, &inj.P));
   dim3 pg((r.G.P + 31) / 32, (g.nz + 7) / 8);
+  float* W;
+  FD2D_TRY(workspace_t(ctx, "f32.band_w", (size_t)K * ncol * r.S, &W));
   for (int l = 0; l < r.S; ++l) {
-    k32_make_P<<<pg, r.pblock, 0, ctx->stream>>>(K, ncol, M, sd[l], spec_eff + l * K, Xre[l], Xim[l], sign, g.nx,
-                                                 g.nz, r.G.P, sps, inj.P + l * r.ps);
+    float* Wl = W + (size_t)l * K * ncol;
+    k32_band_weights<<<(K * ncol + 127) / 128, 128, 0, ctx->stream>>>(K, ncol, M, spec_eff + l * K, Wl);
+    FD2D_TRY(after_launch(ctx, "k32_band_weights"));
+    k32_make_P<<<pg, r.pblock, 0, ctx->stream>>>(K, ncol, Wl, sd[l], Xre[l], Xim[l], (float)sign, g.nx, g.nz,
+                                                 r.G.P, sps, inj.P + l * r.ps);
     FD2D_TRY(after_launch(ctx, "k32_make_P"));
   }
   // B[k][j] = Re c(row_j, k); B[K+k][j] = -Im c(row_j, k)   (c = ifft_coeff, dw)
