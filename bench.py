@@ -170,6 +170,7 @@ def main():
     ap.add_argument("--workload", default="single_600_o8")
     ap.add_argument("--cpu-nt", type=int, default=120)
     ap.add_argument("--nt", type=int, default=0, help="override the workload's nt (profiling runs)")
+    ap.add_argument("--stations", type=int, default=0, help="override the number of reference stations")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -182,7 +183,10 @@ def main():
     world, rank, local = dist_setup()
 
     from fd2d_noise_gb300.workloads import WORKLOADS
-    w = WORKLOADS[args.workload](**({"nt": args.nt} if args.nt else {}))
+    kw = {"nt": args.nt} if args.nt else {}
+    if args.stations:
+        kw["n_ref"] = args.stations
+    w = WORKLOADS[args.workload](**kw)
     if args.impl == "reference":
         run_reference(args, w, world, rank)
         return

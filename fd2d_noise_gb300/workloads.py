@@ -68,7 +68,7 @@ def plain_cpu_300(nt: int = 1200) -> Workload:
     return Workload("plain_cpu_300", cfg, mu, rho, ref, rec, spec, sd)
 
 
-def single_600_o8(nt: int = 3000, K: int = 300) -> Workload:
+def single_600_o8(nt: int = 3000, K: int = 300, n_ref: int = 2) -> Workload:
     nx = 600
     dx = L / (nx - 1)
     cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.05, nt=nt, order=8, f_sample=_freqs(0.01, 0.2, K),
@@ -80,7 +80,7 @@ def single_600_o8(nt: int = 3000, K: int = 300) -> Workload:
                                  x_r=1.0e6 * s, z_r=1.0e6 * s, radius=6.8e5 * s, thickness=1e5 * s,
                                  radial_scale=9e8 * s * s)
     rec = interior_points(cfg, 40, seed=3, margin_frac=0.2)
-    ref = interior_points(cfg, 2, seed=13, margin_frac=0.3)
+    ref = interior_points(cfg, n_ref, seed=13, margin_frac=0.3)
     return Workload("single_600_o8", cfg, mu, rho, ref, rec, spec, sd)
 
 
