@@ -1,6 +1,6 @@
 // solver_fp32.cu -- the FP32 form of the three solvers.
 //
-// Per time step ONE fused kernel (k32_step) advances a 64x16 tile of the grid:
+// Per time step ONE fused kernel (k32_step) advances a 32x32 tile of the grid:
 //   DS  = div_s(sxy, szy) (+ point sources) (+ injected correlation source)
 //   v   = (v + DS * dt/rho) * absbound
 //   sxy += dt*mu * dx_v(v),  szy += dt*mu * dz_v(v),  u += v*dt
@@ -38,7 +38,7 @@
 namespace fd2d {
 namespace {
 
-constexpr int TX = 32, TZ = 16, NT = 128;
+constexpr int TX = 32, TZ = 32, NT = 256;
 constexpr int MAX_BOX_SRC = 64;
 constexpr int MAX_TILE_REC = 32;  // receivers of one tile kept in shared memory
 
@@ -77,6 +77,9 @@ struct Tile {
   // resident CTAs per SM the shared memory allows (228 KB per SM, 1 KB per CTA
   // reserved, ~1 KB of static shared variables), at most 8
   static constexpr int CTAS = (228 * 1024) / (BYTES + 2048) < 8 ? (228 * 1024) / (BYTES + 2048) : 8;
+  // CTAs per SM to ask of the register allocator: the shared-memory limit, but
+  // no fewer than 80 registers per thread (the kernel spills below that)
+  static constexpr int MINB = CTAS < 65536 / (NT * 80) ? CTAS : 65536 / (NT * 80);
 };
 
 struct alignas(64) StepMaps {
@@ -141,7 +144,7 @@ __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, c
 }
 
 template <int R, bool HU, bool HI>
-__global__ __launch_bounds__(NT, Tile<R, HU, HI>::CTAS) void k32_step(
+__global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
     Grid32 G, const __grid_constant__ StepMaps M, Step32 S) {
   using T = Tile<R, HU, HI>;
   extern __shared__ __align__(128) unsigned char sm_raw[];
