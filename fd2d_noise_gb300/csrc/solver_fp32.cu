@@ -152,10 +152,11 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
   // (offset arithmetic on the shared array keeps the pointer in the shared
   // address space, so the float4 accesses below compile to shared loads)
   float* sm = reinterpret_cast<float*>(sm_raw + ((128u - (smem_u32(sm_raw) & 127u)) & 127u));
-  float cf[4];
-#pragma unroll
-  for (int m = 0; m < 4; ++m) cf[m] = G.c[m];
-  const float inv_dx = G.inv_dx, inv_dz = G.inv_dz, gdt = G.dt;
+  // coefficients stay in the parameter bank (FFMA constant operands, no registers)
+  const float* cf = G.c;
+#define inv_dx G.inv_dx
+#define inv_dz G.inv_dz
+#define gdt G.dt
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_src[MAX_BOX_SRC];
   __shared__ float s_amp[MAX_BOX_SRC];
@@ -180,6 +181,12 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
     // coefficient planes are not written by the time loop: their loads may
     // overlap the end of the previous step (programmatic dependent launch)
     issue_tile<R, HU, HI>(G, M, S, sm, &bar, t, true, false);
+    // The fields are what the previous launch wrote (or will write what it
+    // read: ping-pong buffers): wait for it to complete, then load them.  The
+    // other threads touch those buffers only after this tile's loads land, so
+    // this thread's wait orders the whole CTA after the previous step.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    issue_tile<R, HU, HI>(G, M, S, sm, &bar, t, false, true);
   }
   {
     const float* buf = sm;
@@ -190,7 +197,8 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
     const int2* src_xy = S.src_xy + (int64_t)lane * S.nsrc;
     const double* amp = S.amp ? S.amp + (int64_t)lane * S.nsrc : nullptr;
     __syncthreads();  // barrier initialised, lists cleared
-    // receivers and point sources of this tile (static tables)
+    // receivers and point sources of this tile (static tables), read while
+    // the tile's loads are in flight
     if (S.nrec && tid < 32) {
       if (S.tile_rec) {
         const int2 se = S.tile_rec[t];
@@ -210,10 +218,6 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
         }
       }
     }
-    // Everything below reads what the previous launch wrote, or writes what it
-    // read (ping-pong buffers): wait for it to complete.
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    if (tid == 0) issue_tile<R, HU, HI>(G, M, S, sm, &bar, t, false, true);
     // one warp waits for the tile (suspending); the others wait at the barrier
     bool ok = true;
     if (tid < 32) ok = mbar_wait_bounded_sleep(&bar, 0);
@@ -238,25 +242,14 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
     // DS = div_s(sxy, szy) (+ sources) (+ injection); v = (v + DS*dt/rho)*taper.
     // Sums are formed in the same order as the scalar form (m = 1..R).
     {
-      // work item: a 4-wide block of NB1 rows; NB1 = 1 keeps the register
-      // footprint small enough for 6 resident CTAs per SM without spills
-      constexpr int NB1 = 1;
+      // work item: a 4-wide block of NB1 = 2 rows (the szy rows of the z sum
+      // are shared by both rows); at most one item per thread
+      constexpr int NB1 = 2;
       constexpr int NQ = W / 4, NRB = (T::BH + NB1 - 1) / NB1;
       for (int item = tid; item < NQ * NRB; item += NT) {
         const int q = item % NQ, r0 = NB1 * (item / NQ);
         const int c0 = 4 * q;  // box column of element 0; global x = vx0 + c0 + e
-        float xs[NB1][12];     // sxy columns c0 .. c0+11 (x from x0-8 = box column - 4)
         float zs[2 * R + NB1 - 1][4];
-#pragma unroll
-        for (int k = 0; k < NB1; ++k) {
-          const int rr = min(r0 + k, T::BH - 1);
-          const float4* rowp = reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + c0);
-#pragma unroll
-          for (int h = 0; h < 3; ++h) {
-            const float4 f = rowp[h];
-            xs[k][4 * h] = f.x; xs[k][4 * h + 1] = f.y; xs[k][4 * h + 2] = f.z; xs[k][4 * h + 3] = f.w;
-          }
-        }
 #pragma unroll
         for (int k = 0; k < 2 * R + NB1 - 1; ++k) {
           // szy row r0 + k holds szy(gz0 + k - R) for gz0 = global z of row r0
@@ -270,22 +263,24 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
           if (rr >= T::BH) break;
           const int gz = bz0 + rr;
           const bool zin = gz >= R && gz <= nz - R - 1;
-          const float4 v4 = *reinterpret_cast<const float4*>(s_v + rr * W + c0);
-          const float4 b4 = *reinterpret_cast<const float4*>(s_b + rr * W + c0);
-          const float4 t4 = *reinterpret_cast<const float4*>(s_t + rr * W + c0);
-          float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (inj) i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
-          const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
-          const float tt[4] = {t4.x, t4.y, t4.z, t4.w}, ii[4] = {i4.x, i4.y, i4.z, i4.w};
-          float out[4];
+          float xs[12];  // sxy columns c0 .. c0+11 (x from x0-8 = box column - 4)
+          {
+            const float4* rowp = reinterpret_cast<const float4*>(s_sxy + rr * T::SXWa + c0);
+#pragma unroll
+            for (int h = 0; h < 3; ++h) {
+              const float4 f = rowp[h];
+              xs[4 * h] = f.x; xs[4 * h + 1] = f.y; xs[4 * h + 2] = f.z; xs[4 * h + 3] = f.w;
+            }
+          }
+          float dsv[4];
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             const int gx = vx0 + c0 + e;
             // both sums are formed everywhere and selected (no divergent branches)
-            // sxy(gx + m - 1) is xs[k][e + 3 + m], sxy(gx - m) is xs[k][e + 4 - m]
+            // sxy(gx + m - 1) is xs[e + 3 + m], sxy(gx - m) is xs[e + 4 - m]
             float ax = 0.f;
 #pragma unroll
-            for (int m = 1; m <= R; ++m) ax += cf[m - 1] * (xs[k][e + 3 + m] - xs[k][e + 4 - m]);
+            for (int m = 1; m <= R; ++m) ax += cf[m - 1] * (xs[e + 3 + m] - xs[e + 4 - m]);
             // szy(gz + m - 1) is zs[k + R + m - 1], szy(gz - m) is zs[k + R - m]
             float az = 0.f;
 #pragma unroll
@@ -304,7 +299,21 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
                 }
               }
             }
-            if (inj) ds += ii[e];
+            dsv[e] = ds;
+          }
+          // the point-wise operands are read once the stencil sums are formed
+          // (fewer live registers)
+          const float4 v4 = *reinterpret_cast<const float4*>(s_v + rr * W + c0);
+          const float4 b4 = *reinterpret_cast<const float4*>(s_b + rr * W + c0);
+          const float4 t4 = *reinterpret_cast<const float4*>(s_t + rr * W + c0);
+          float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (inj) i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
+          const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
+          const float tt[4] = {t4.x, t4.y, t4.z, t4.w}, ii[4] = {i4.x, i4.y, i4.z, i4.w};
+          float out[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const float ds = inj ? dsv[e] + ii[e] : dsv[e];
             out[e] = (vv[e] + ds * bb[e]) * tt[e];
           }
           *reinterpret_cast<float4*>(s_vn + rr * W + c0) = make_float4(out[0], out[1], out[2], out[3]);
@@ -425,6 +434,9 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
   // the next step may start its launch and prologue now
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
+#undef inv_dx
+#undef inv_dz
+#undef gdt
 
 // ---- point kernels ---------------------------------------------------------------
 // FP32 staggered derivatives of a field with row pitch `ld` (f, or f - g).
