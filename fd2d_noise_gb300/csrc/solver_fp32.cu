@@ -228,6 +228,9 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
       }
       return;
     }
+    // the tile is in shared memory: the next step may launch and run its
+    // prologue (its own wait orders it after this grid's stores)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int nbs = s_nsrc;
     const float* s_sxy = buf + T::O_SXY;
     const float* s_szy = buf + T::O_SZY;
@@ -431,8 +434,6 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
       }
     }
   }
-  // the next step may start its launch and prologue now
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 #undef inv_dx
 #undef inv_dz
