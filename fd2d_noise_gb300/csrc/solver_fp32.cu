@@ -78,8 +78,9 @@ struct Tile {
   // reserved, ~1 KB of static shared variables), at most 8
   static constexpr int CTAS = (228 * 1024) / (BYTES + 2048) < 8 ? (228 * 1024) / (BYTES + 2048) : 8;
   // CTAs per SM to ask of the register allocator: the shared-memory limit, but
-  // no fewer than 80 registers per thread (the kernel spills below that)
-  static constexpr int MINB = CTAS < 65536 / (NT * 80) ? CTAS : 65536 / (NT * 80);
+  // no fewer than 64 registers per thread (4 CTAs of 256 threads at order 8;
+  // the kernel spills below that)
+  static constexpr int MINB = CTAS < 65536 / (NT * 64) ? CTAS : 65536 / (NT * 64);
 };
 
 struct alignas(64) StepMaps {
@@ -245,9 +246,9 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
     // DS = div_s(sxy, szy) (+ sources) (+ injection); v = (v + DS*dt/rho)*taper.
     // Sums are formed in the same order as the scalar form (m = 1..R).
     {
-      // work item: a 4-wide block of NB1 = 2 rows (the szy rows of the z sum
-      // are shared by both rows); at most one item per thread
-      constexpr int NB1 = 2;
+      // work item: a 4-wide block of NB1 rows; NB1 = 1 keeps the kernel within
+      // 64 registers (4 resident CTAs per SM) without spills
+      constexpr int NB1 = 1;
       constexpr int NQ = W / 4, NRB = (T::BH + NB1 - 1) / NB1;
       for (int item = tid; item < NQ * NRB; item += NT) {
         const int q = item % NQ, r0 = NB1 * (item / NQ);
