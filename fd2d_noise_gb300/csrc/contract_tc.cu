@@ -135,16 +135,20 @@ __global__ __launch_bounds__(256) void k_image(const float* __restrict__ src, in
 //   warp 0   : one lane issues the bulk copies (STAGES-deep ring);
 //   warp 1   : allocates TMEM (two 128-column accumulators); one lane issues
 //              the MMAs (12 per K block) and commits stages and accumulators;
-//   warps 2-5: epilogue, TMEM lanes 32*(warp%4) .. +31 of the accumulator the
-//              MMAs are not writing -- it overlaps the next tile's main loop.
-constexpr int NTHREADS_P = 192;
+//   warps 2-9: epilogue, TMEM lanes 32*(warp%4) .. +31 of the accumulator the
+//              MMAs are not writing, columns 64*((warp-2)/4) .. +63 -- it
+//              overlaps the next tile's main loop.  Two warps per TMEM lane
+//              quarter keep enough stores in flight for the FP64 spectra.
+constexpr int EPI_WARPS = 8;
+constexpr int NTHREADS_P = 64 + 32 * EPI_WARPS;
+static_assert(EPI_WARPS % 4 == 0 && BN % (32 * (EPI_WARPS / 4)) == 0, "epilogue warps split the columns in 32s");
 
 __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, int ntn, int n_tiles, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];   // both blocks of the stage landed (tx)
   __shared__ __align__(8) uint64_t empty_bar[STAGES];  // MMAs done reading the stage
   __shared__ __align__(8) uint64_t accf_bar[2];        // accumulator complete
-  __shared__ __align__(8) uint64_t acce_bar[2];        // accumulator read out (4 epilogue warps)
+  __shared__ __align__(8) uint64_t acce_bar[2];        // accumulator read out (every epilogue warp)
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
 
@@ -164,7 +168,7 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf_bar[b], 1);
-      mbar_init(&acce_bar[b], 4);
+      mbar_init(&acce_bar[b], EPI_WARPS);
     }
     fail = 0;
     fence_mbar_init();
@@ -245,8 +249,10 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
     }
     __syncwarp();
   } else {
-    // ---------------- epilogue: warps 2-5 ----------------
+    // ---------------- epilogue: warps 2-9 ----------------
     const int quarter = warp & 3;  // TMEM lanes 32*quarter .. +31
+    constexpr int CW = BN / (EPI_WARPS / 4);   // columns per warp
+    const int cbeg = CW * ((warp - 2) / 4);    // this warp's first column
     int i = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++i) {
       const int acc = i & 1;
@@ -272,11 +278,11 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
         valid = ii < a.remap_nx && jj < a.remap_nz;
         q = lane_off + ii + (int64_t)a.remap_nx * jj;
       }
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = cbeg; c0 < cbeg + CW; c0 += 32) {
         float v[32];
         // all lanes of the warp take part in tcgen05.ld (sync.aligned)
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TMEM_COLS + c0), v);
-        if (c0 + 32 == BN) {
+        if (c0 + 32 == cbeg + CW) {
           // the accumulator is in registers: hand it back to the MMAs
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
@@ -292,6 +298,16 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
         }
         if (a.acc0) {
           // Column n of the tile goes to plane n (acc0) or n - nsplit (acc1).
+          const int nb = n0 + c0;
+          if (a.overwrite && nb + 32 <= a.N && (nb + 32 <= a.nsplit || nb >= a.nsplit)) {
+            // the 32 columns are whole and on one side of the split: plain
+            // stores along one plane stride (warp-uniform branch)
+            double* p = nb < a.nsplit ? a.acc0 + (int64_t)nb * a.ldacc + q
+                                      : a.acc1 + (int64_t)(nb - a.nsplit) * a.ldacc + q;
+#pragma unroll
+            for (int j = 0; j < 32; ++j, p += a.ldacc) *p = widen_exact(v[j]);
+            continue;
+          }
           // Overwrite: plain stores.  Accumulate: 8 loads in flight per group.
 #pragma unroll
           for (int gg = 0; gg < 32; gg += 8) {

@@ -4,9 +4,9 @@
 // the hardware conversion instructions run on it.  Kernels that convert every
 // element (the FP64 spectra written by the DFT, the FP32 injection planes made
 // from FP64 spectra) use these bit-level versions instead: exact widening and
-// round-to-nearest-even narrowing of normal numbers; zeros, subnormals,
+// round-to-nearest-even narrowing of normal numbers (zeros, subnormals,
 // infinities, NaNs and out-of-range values fall back to the hardware
-// conversion.  Host-compilable so the rounding can be checked on the CPU.
+// conversion there; the widening handles every class with integers).  Host-compilable so the rounding can be checked on the CPU.
 #pragma once
 
 #include <cstdint>
@@ -60,13 +60,35 @@ FD2D_HD double f64_from(uint64_t u) {
 #endif
 }
 
-// Exact FP32 -> FP64.
+FD2D_HD int clz32(uint32_t v) {
+#if defined(__CUDA_ARCH__)
+  return __clz((int)v);
+#else
+  return v ? __builtin_clz(v) : 32;
+#endif
+}
+
+// Exact FP32 -> FP64, integer operations only (every class: signed zeros,
+// subnormals normalised, infinities, NaNs quietened with their payload).
 FD2D_HD double widen_exact(float x) {
   const uint32_t u = f32_bits(x);
   const uint32_t e = (u >> 23) & 0xFFu;
-  if (e == 0 || e == 0xFFu) return (double)x;
-  return f64_from(((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
-                  ((uint64_t)(u & 0x7FFFFFu) << 29));
+  uint32_t m = u & 0x7FFFFFu;
+  uint64_t eb;
+  if (e == 0xFFu) {
+    eb = 0x7FFu;
+    if (m) m |= 0x400000u;  // quiet NaN
+  } else if (e != 0) {
+    eb = e + 896u;          // rebias 127 -> 1023
+  } else if (m == 0) {
+    eb = 0;                 // signed zero
+  } else {
+    // subnormal m * 2^-149 with its leading one at bit p: exponent p - 149
+    const int p = 31 - clz32(m);
+    eb = (uint64_t)(p + 874);
+    m = (m << (23 - p)) & 0x7FFFFFu;
+  }
+  return f64_from(((uint64_t)(u & 0x80000000u) << 32) | (eb << 52) | ((uint64_t)m << 29));
 }
 
 // FP64 -> FP32, round to nearest, ties to even (the C conversion).

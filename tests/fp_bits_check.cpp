@@ -49,6 +49,16 @@ int main() {
                             -1e300, std::numeric_limits<double>::infinity(), std::nan(""), 1.17549435e-38,
                             1.1754942e-38, 0.999999999, 1.0, 16777217.0, 16777219.0};
   for (double x : special) check_d(x);
+  const float fspecial[] = {0.0f, -0.0f, 1e-45f, -1e-45f, 1e-40f, 5.8774718e-39f, 1.1754942e-38f, 1.17549435e-38f,
+                            3.4028235e38f, std::numeric_limits<float>::infinity(),
+                            -std::numeric_limits<float>::infinity(), std::nanf("")};
+  for (float x : fspecial) check_f(x);
+  for (uint32_t m = 1; m < 0x800000u; m += 997) {  // subnormals across every leading-one position
+    float f;
+    std::memcpy(&f, &m, 4);
+    check_f(f);
+    check_f(-f);
+  }
   std::printf("%s %ld of %ld\n", bad ? "FAIL" : "ok", bad, n);
   return bad ? 1 : 0;
 }
