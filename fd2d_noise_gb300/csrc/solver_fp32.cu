@@ -34,6 +34,7 @@
 #include "tma.cuh"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace fd2d {
 namespace {
@@ -242,6 +243,11 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
     const float* s_mu = buf + T::O_MU;
     const float* s_u = buf + T::O_U;
 
+    // Interior tiles (the halo box inside the operator's range on every side)
+    // skip the edge selects and partial stores: one uniform branch per CTA.
+    const bool edge = !(x0 >= R + 4 && x0 + TX + 4 + R <= nx && z0 >= 2 * R - 1 && z0 + TZ + 2 * R <= nz);
+    auto compute = [&](auto edge_tag) {
+      constexpr bool EDGE = decltype(edge_tag)::value;
     // ---- new v on the box: 4-wide blocks of rows ---------------------------------------
     // DS = div_s(sxy, szy) (+ sources) (+ injection); v = (v + DS*dt/rho)*taper.
     // Sums are formed in the same order as the scalar form (m = 1..R).
@@ -289,21 +295,30 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
             float az = 0.f;
 #pragma unroll
             for (int m = 1; m <= R; ++m) az += cf[m - 1] * (zs[k + R + m - 1][e] - zs[k + R - m][e]);
-            float ds = (gx >= R && gx <= nx - R - 1) ? ax * inv_dx : 0.f;
-            ds = zin ? ds + az * inv_dz : ds;
-            if (nbs) {
-              const int idx = rr * W + c0 + e;
-              if (nbs <= MAX_BOX_SRC) {
-                for (int qq = 0; qq < nbs; ++qq)
-                  if (s_src[qq] == idx) ds += s_amp[qq];
-              } else {
-                for (int qq = 0; qq < S.nsrc; ++qq) {
-                  const int2 w = src_xy[qq];
-                  if (w.x == gx && w.y == gz) ds += amp ? (float)amp[qq] : S.amp_const;
-                }
+            float ds = (!EDGE || (gx >= R && gx <= nx - R - 1)) ? ax * inv_dx : 0.f;
+            ds = (!EDGE || zin) ? ds + az * inv_dz : ds;
+            dsv[e] = ds;
+          }
+          if (nbs) {
+            // point sources in this block (only tiles that hold one), added in
+            // list order after the stencil sums
+            const int idx0 = rr * W + c0;
+            if (nbs <= MAX_BOX_SRC) {
+              for (int qq = 0; qq < nbs; ++qq) {
+                const int d = s_src[qq] - idx0;
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                  if (d == e) dsv[e] += s_amp[qq];
+              }
+            } else {
+              for (int qq = 0; qq < S.nsrc; ++qq) {
+                const int2 w = src_xy[qq];
+                const int d = w.x - (vx0 + c0);
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                  if (w.y == gz && d == e) dsv[e] += amp ? (float)amp[qq] : S.amp_const;
               }
             }
-            dsv[e] = ds;
           }
           // the point-wise operands are read once the stencil sums are formed
           // (fewer live registers)
@@ -332,7 +347,7 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
       const int q = tid % NQ2, tz = tid / NQ2;
       const int j = z0 + tz;
       const int i0 = x0 + 4 * q;
-      if (tz < TZ && j < nz && i0 < nx) {
+      if (tz < TZ && (!EDGE || (j < nz && i0 < nx))) {
         const int rr = tz + R - 1;  // box row of output row j
         const int cv = 4 + 4 * q;   // box column of element 0
         // vx = box columns cv-4 .. cv+7: v(i) is vx[e + 4], v(i + m) is vx[e + m + 4],
@@ -370,22 +385,22 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
           for (int m = 1; m <= R; ++m) ax += cf[m - 1] * (vx[e + m + 4] - vx[e - m + 5]);
 #pragma unroll
           for (int m = 1; m <= R; ++m) az += cf[m - 1] * (vz[R - 1 + m][e] - vz[R - m][e]);
-          nsx[e] = (i >= R - 1 && i <= nx - R - 1) ? sxo[e] + mu[e] * (ax * inv_dx) : sxo[e];
-          nsz[e] = zin ? szo[e] + mu[e] * (az * inv_dz) : szo[e];
+          nsx[e] = (!EDGE || (i >= R - 1 && i <= nx - R - 1)) ? sxo[e] + mu[e] * (ax * inv_dx) : sxo[e];
+          nsz[e] = (!EDGE || zin) ? szo[e] + mu[e] * (az * inv_dz) : szo[e];
           nu[e] = HU ? uo[e] + vn[e] * gdt : vn[e];
         }
         const int64_t p = lo + i0 + (int64_t)P * j;
-        if (i0 + 3 < nx) {
+        if (!EDGE || i0 + 3 < nx) {
           // whole quad inside the grid: vector stores
           *reinterpret_cast<float4*>(S.vo + p) = make_float4(vn[0], vn[1], vn[2], vn[3]);
-          if (i0 + 3 <= nx - 2) {
+          if (!EDGE || i0 + 3 <= nx - 2) {
             *reinterpret_cast<float4*>(S.sxyo + p) = make_float4(nsx[0], nsx[1], nsx[2], nsx[3]);
           } else {
 #pragma unroll
             for (int e = 0; e < 4; ++e)
               if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
           }
-          if (j <= nz - 2) *reinterpret_cast<float4*>(S.szyo + p) = make_float4(nsz[0], nsz[1], nsz[2], nsz[3]);
+          if (!EDGE || j <= nz - 2) *reinterpret_cast<float4*>(S.szyo + p) = make_float4(nsz[0], nsz[1], nsz[2], nsz[3]);
           if (HU) *reinterpret_cast<float4*>(S.uo + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
           if (S.snap_dft) *reinterpret_cast<float4*>(S.snap_dft + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
         } else {
@@ -417,10 +432,15 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
           const float* old = S.snap_pre_u ? s_u + tz * TX + 4 * q : s_v + rr * W + cv;
 #pragma unroll
           for (int e = 0; e < 4; ++e)
-            if (i0 + e < nx) S.snap_pre[i0 + e + nx * j] = old[e];
+            if (!EDGE || i0 + e < nx) S.snap_pre[i0 + e + nx * j] = old[e];
         }
       }
     }
+    };
+    if (edge)
+      compute(std::true_type{});
+    else
+      compute(std::false_type{});
     if (S.nrec && s_nrec < 0) {
       // more receivers in this tile than the shared list holds: read them back
       __syncthreads();
