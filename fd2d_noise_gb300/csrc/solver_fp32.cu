@@ -74,6 +74,7 @@ struct Tile {
   static constexpr int O_U = O_MU + al(TZ * TX);
   static constexpr int O_VN = O_U + (HU ? al(TZ * TX) : 0);
   static constexpr int TOTAL = O_VN + al(BH * BWa);  // new v on the 40-wide box (x from x0-4)
+  static_assert(BH + 2 * R - 1 <= SZH, "the z sum of the last box row stays inside the szy rows");
   static constexpr int BYTES = TOTAL * 4 + 128;      // + alignment slack
   // resident CTAs per SM the shared memory allows (228 KB per SM, 1 KB per CTA
   // reserved, ~1 KB of static shared variables), at most 8
@@ -110,14 +111,12 @@ struct Step32 {
   int rec_u;
 };
 
-// One CTA per tile; tiles of all lanes form one list (blockIdx.x).
+// One CTA per tile: blockIdx = (tile column, tile row, lane).
 template <int R>
-__device__ __forceinline__ void tile_coords(const Grid32& G, int t, int& x0, int& z0, int& lane) {
-  const int per = G.ntx * G.ntz;
-  lane = t / per;
-  const int r = t - lane * per;
-  z0 = (r / G.ntx) * TZ;
-  x0 = (r - (r / G.ntx) * G.ntx) * TX;
+__device__ __forceinline__ void tile_coords(const Grid32&, int, int& x0, int& z0, int& lane) {
+  lane = blockIdx.z;
+  z0 = blockIdx.y * TZ;
+  x0 = blockIdx.x * TX;
 }
 
 template <int R, bool HU, bool HI>
@@ -173,7 +172,8 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
   float* s_vn = sm + T::O_VN;
   constexpr bool inj = HI;
 
-  const int t = blockIdx.x;
+  // tile number in the per-(lane, tile) tables
+  const int t = blockIdx.x + G.ntx * (blockIdx.y + G.ntz * blockIdx.z);
   if (t >= n_tiles) return;
   if (tid == 0) {
     s_nsrc = 0;
@@ -263,14 +263,15 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
 #pragma unroll
         for (int k = 0; k < 2 * R + NB1 - 1; ++k) {
           // szy row r0 + k holds szy(gz0 + k - R) for gz0 = global z of row r0
-          const int rr = min(r0 + k, T::SZH - 1);
+          // (one-row items never reach past the last szy row: no clamp)
+          const int rr = NB1 == 1 ? r0 + k : min(r0 + k, T::SZH - 1);
           const float4 f = *reinterpret_cast<const float4*>(s_szy + rr * W + c0);
           zs[k][0] = f.x; zs[k][1] = f.y; zs[k][2] = f.z; zs[k][3] = f.w;
         }
 #pragma unroll
         for (int k = 0; k < NB1; ++k) {
           const int rr = r0 + k;
-          if (rr >= T::BH) break;
+          if (NB1 > 1 && rr >= T::BH) break;
           const int gz = bz0 + rr;
           const bool zin = gz >= R && gz <= nz - R - 1;
           float xs[12];  // sxy columns c0 .. c0+11 (x from x0-8 = box column - 4)
@@ -836,7 +837,7 @@ fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S
   }
   r.G.ntx = (nx + TX - 1) / TX;
   r.G.ntz = (nz + TZ - 1) / TZ;
-  r.sgrid = dim3(r.G.ntx * r.G.ntz * S);
+  r.sgrid = dim3(r.G.ntx, r.G.ntz, S);
   r.pgrid = dim3((nx + 31) / 32, (nz + 7) / 8);
   FD2D_TRY(step_attributes(ctx));
   FD2D_TRY(contract_prepare(ctx));
@@ -1060,7 +1061,7 @@ void sig_run(Sig& sg, const Run& r) {
   sg.add(r.b); sg.add(r.taper); sg.add(r.dtmu);
   for (int q = 0; q < 2; ++q) { sg.add(r.v[q]); sg.add(r.sxy[q]); sg.add(r.szy[q]); sg.add(r.u[q]); }
   sg.bytes(r.maps, sizeof(r.maps));
-  sg.add(r.sgrid.x); sg.add(r.sgrid.y); sg.add(r.pgrid.x); sg.add(r.pgrid.y);
+  sg.add(r.sgrid.x); sg.add(r.sgrid.y); sg.add(r.sgrid.z); sg.add(r.pgrid.x); sg.add(r.pgrid.y);
   sg.add(r.R); sg.add(r.rec_xy); sg.add(r.src_xy); sg.add(r.np); sg.add(r.ps);
 }
 
@@ -1537,7 +1538,7 @@ extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg,
   }
   r.G.ntx = (nx + TX - 1) / TX;
   r.G.ntz = (nz + TZ - 1) / TZ;
-  r.sgrid = dim3(r.G.ntx * r.G.ntz);
+  r.sgrid = dim3(r.G.ntx, r.G.ntz, 1);
   r.pgrid = dim3((P + 31) / 32, (nz + 7) / 8);
   // The array keeps the previous call's contents: clear what must start at zero.
   FD2D_CUDA(nullptr, cudaMemsetAsync(d_err, 0, sizeof(int), stream));
