@@ -131,6 +131,19 @@ def cpu_sample(w, nt_cpu: int, threads: int):
     return gpt / dt / 1e9, dt, gpt, cfg
 
 
+def workload_config(w, world):
+    """The ``config`` object of both arms' lines for a single-grid workload."""
+    cfg = w.cfg
+    np_, K = cfg.npts, cfg.n_sample
+    return {"workload": w.name, "nx": cfg.nx, "nz": cfg.nz, "nt": cfg.nt, "ntc": cfg.ntc,
+            "order": cfg.order, "n_sample": K, "freq_samp": cfg.freq_samp,
+            "reference_stations": int(w.ref_stations.shape[0]), "receivers": int(w.receivers.shape[0]),
+            "gpt_per_step": int(w.ref_stations.shape[0] * w.gpt_per_station()),
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs > L2 per step (FP64 Green spectra %.2f GB, injection planes %.2f GB)"
+                  % (2 * np_ * K * 8 / 1e9, (cfg.ntc // cfg.freq_samp) * np_ * 4 / 1e9)}
+
+
 def run_reference(args, w, world, rank):
     if rank != 0:
         return
@@ -148,11 +161,12 @@ def run_reference(args, w, world, rank):
               f"Green {cfg.nt} + correlation {cfg.ntc} steps on {cfg.nx}x{cfg.nz}, K={cfg.n_sample}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpt-updates/s",
-        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": world, "gpus_used": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * statistics.median(dts), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": w.name, "nx": w.cfg.nx, "nz": w.cfg.nz, "nt": args.cpu_nt,
-                   "order": w.cfg.order, "n_sample": w.cfg.n_sample},
+        # the workload is the GPU arm's; each step times a bounded sample of it
+        # (cpu_baseline.sample) and reports the same per-update rate
+        "config": workload_config(w, world),
         "cpu_baseline": {"value": value, "unit": "Gpt-updates/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "Gpt-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -293,12 +307,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": w.name, "nx": cfg.nx, "nz": cfg.nz, "nt": cfg.nt, "ntc": cfg.ntc,
-                   "order": cfg.order, "n_sample": K, "freq_samp": cfg.freq_samp,
-                   "reference_stations": n_ref, "receivers": nr,
-                   "gpt_per_step": gpt_step, "parallelism": f"replicas x{world}",
-                   "l2": "inputs > L2 per step (FP64 Green spectra %.2f GB, injection planes %.2f GB)"
-                         % (2 * np_ * K * 8 / 1e9, (cfg.ntc // cfg.freq_samp) * np_ * 4 / 1e9)},
+        "config": workload_config(w, world),
         "roofline": roof, "gpu_launches": launches, "clocks": clk,
     }
     result["config"]["launch_groups"] = sess.ctx.last_batch()  # lanes per launch group
