@@ -191,6 +191,9 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=40,
                     help="requests of the serving measurement (0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="mean Poisson arrival rate [1/s]")
+    ap.add_argument("--no-hbm-probe", action="store_true",
+                    help="skip the stencil roofline on a grid whose fields exceed L2")
+    ap.add_argument("--probe-nt", type=int, default=200, help="nt of the large-grid stencil probe")
     ap.add_argument("--no-timing", action="store_true",
                     help="do not bracket kernels with CUDA events (no roofline)")
     args = ap.parse_args()
@@ -341,6 +344,9 @@ def main():
     if rank == 0 and args.serve_requests > 0:
         result["serving"] = serving_run(args, dev)
 
+    if rank == 0 and not args.no_hbm_probe:
+        result["roofline_large_grid"] = hbm_probe(args, dev)
+
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         v, dt, gpt, ccfg = cpu_sample(w, args.cpu_nt, threads)
@@ -353,6 +359,50 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def hbm_probe(args, dev):
+    """Stencil roofline where HBM is the bound: large_2048_o8 (4 stations as
+    lanes of 2048x2048, fields 4 x 11 x 16.8 MB > L2), one instrumented batch
+    call after one warm-up call; the library's CUDA events bracket each time
+    loop and each contraction, so stencil time = loop time - contractions."""
+    import numpy as np
+    import torch
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+    from fd2d_noise_gb300.workloads import large_2048_o8
+
+    w = large_2048_o8(nt=args.probe_nt)
+    cfg = w.cfg
+    nr = w.receivers.shape[0]
+    sess = DeviceSession(cfg, dev, "fp32")
+    mu, rho = to_device(w.mu, np.float64, dev), to_device(w.rho, np.float64, dev)
+    spec, sd = to_device(w.spectrum, np.float64, dev), to_device(w.source_dist, np.float64, dev)
+    rec = to_device(w.receivers, np.float64, dev)
+    n_ref = w.ref_stations.shape[0]
+    batch = [dict(cfg=cfg, mu=mu, rho=rho, spectrum=spec, source_dist=sd,
+                  src=to_device(w.ref_stations[i:i + 1], np.float64, dev), rec=rec, nr=nr,
+                  out=sess.zeros(nr * cfg.ntc, torch.float64)) for i in range(n_ref)]
+    sess.correlation_batch(batch)
+    torch.cuda.synchronize()
+    sess.ctx.timing()
+    sess.ctx.set_timing(True)
+    sess.correlation_batch(batch)
+    sess.ctx.set_timing(False)
+    (msV, nV, uV), (msVU, nVU, uVU), (msC, nC, uC) = sess.ctx.timing()
+    lanes = sess.ctx.last_batch()
+    sess.ctx.close()
+    del batch, mu, rho, spec, sd, rec
+    torch.cuda.empty_cache()
+    st_ms = msV + msVU - msC
+    peak, peak_kind = measured_peaks()
+    achieved = (B_STEP_V * uV + B_STEP_VU * uVU) / (st_ms / 1e3) / 1e9 if st_ms > 0 else None
+    return {"workload": w.name, "nx": cfg.nx, "nz": cfg.nz, "nt": cfg.nt, "ntc": cfg.ntc, "order": cfg.order,
+            "lanes": lanes, "bound": "hbm", "unit": "GB/s", "achieved": achieved, "peak": peak,
+            "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_kind} hbm_gbs (burst)",
+            "stencil_us_per_launch": 1e3 * st_ms / max(nV + nVU, 1), "launches": nV + nVU,
+            "gpt_per_s": (uV + uVU) / (st_ms / 1e3) / 1e9 if st_ms > 0 else None,
+            "traffic": profiled_traffic("k32_step", w.name),
+            "bytes_per_update": "36 (Green step) / 44 (correlation step), algorithmic"}
 
 
 def run_batch_workload(args, w, dev, world, rank):

@@ -9,6 +9,8 @@
                             (10 % std, 20 km correlation length), ring source.
 * ``structure_512``      -- 512x512, nt 2500, snapshots every 5 steps, 200
                             frequencies, 1 reference station, 20 receivers.
+* ``large_2048_o8``      -- 2048x2048, order 8, 4 stations, 8 frequencies, nt 200:
+                            fields larger than L2 (stencil HBM roofline).
 * ``batch_uneven``       -- 32 reference stations on grids of 256, 384, 512 or
                             800 points square, nt 1500-4000, order 4, 4
                             frequency bands (see :func:`batch_uneven`).
@@ -99,6 +101,25 @@ def structure_512(nt: int = 2500) -> Workload:
     return Workload("structure_512", cfg, mu, rho, ref, rec, spec, sd)
 
 
+def large_2048_o8(nt: int = 200, K: int = 8, n_ref: int = 4) -> Workload:
+    """Stencil-bandwidth case: 2048x2048, order 8, ``n_ref`` stations as lanes,
+    few frequencies, so the fields (11 planes x 16.8 MB per station) exceed L2
+    and the stencil streams them from HBM."""
+    nx = 2048
+    dx = L / (nx - 1)
+    cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.4 * dx / 4000.0, nt=nt, order=8, f_sample=_freqs(0.01, 0.2, K),
+                 freq_samp=5, fw_nth=1, absorb_width=20 * dx, source_type="ring")
+    mu, rho = random_media(cfg, std=0.10, corr_len=2.0e4, seed=7)
+    s = L / 2.0e6
+    sd, spec = make_noise_source("ring", 0, cfg,
+                                 spectrum_kw=dict(f_peak=[0.1], bandwidth=[0.03], strength=[1.0]),
+                                 x_r=1.0e6 * s, z_r=1.0e6 * s, radius=6.8e5 * s, thickness=1e5 * s,
+                                 radial_scale=9e8 * s * s)
+    rec = interior_points(cfg, 40, seed=3, margin_frac=0.2)
+    ref = interior_points(cfg, n_ref, seed=17, margin_frac=0.3)
+    return Workload("large_2048_o8", cfg, mu, rho, ref, rec, spec, sd)
+
+
 @dataclasses.dataclass
 class BatchWorkload:
     """Reference stations on grids of different sizes (one Workload per station)."""
@@ -140,5 +161,6 @@ WORKLOADS: Dict[str, Callable[..., Workload]] = {
     "plain_cpu_300": plain_cpu_300,
     "single_600_o8": single_600_o8,
     "structure_512": structure_512,
+    "large_2048_o8": large_2048_o8,
     "batch_uneven": batch_uneven,
 }
