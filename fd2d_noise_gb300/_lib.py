@@ -33,8 +33,10 @@ EXPORTED = [
     "fd2d_ctx_set_timing", "fd2d_ctx_timing", "fd2d_contract_f32",
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
     "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch", "fd2d_ctx_release", "fd2d_ctx_workspace_bytes",
-    "fd2d_gaussblur2d", "fd2d_ctx_set_chunks",
+    "fd2d_gaussblur2d", "fd2d_ctx_set_chunks", "fd2d_ctx_set_tile_rows", "fd2d_ctx_last_tile_rows",
 ]
+TILE_ROWS_AUTO = 0
+TILE_ROWS_RULE = -1
 MEAS_WAVEFORM_DIFFERENCE = 0
 MEAS_LOG_AMPLITUDE_RATIO = 1
 
@@ -89,6 +91,8 @@ def load(path: str = LIB_PATH):
         L.fd2d_ctx_kernel_launches.restype = _i64
         L.fd2d_ctx_last_batch.argtypes = [_vp, ctypes.POINTER(ctypes.c_int32), _i32]
         L.fd2d_ctx_last_batch.restype = _i32
+        L.fd2d_ctx_set_tile_rows.argtypes = [_vp, _i32]
+        L.fd2d_ctx_last_tile_rows.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.restype = _i64
         L.fd2d_ctx_release.argtypes = [_vp, ctypes.POINTER(_i64)]
@@ -113,7 +117,7 @@ def load(path: str = LIB_PATH):
             _vp, _i32, _vp, _i32, _vp, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp]
         for name in EXPORTED:
             if name not in ("fd2d_abi_version", "fd2d_ctx_kernel_launches", "fd2d_last_error",
-                            "fd2d_ctx_last_batch", "fd2d_ctx_workspace_bytes"):
+                            "fd2d_ctx_last_batch", "fd2d_ctx_workspace_bytes", "fd2d_ctx_last_tile_rows"):
                 getattr(L, name).restype = _i32
         _lib = L
         return L
@@ -178,6 +182,14 @@ class Context:
     @property
     def workspace_bytes(self) -> int:
         return int(self.L.fd2d_ctx_workspace_bytes(self.h))
+
+    def set_tile_rows(self, rows: int):
+        """Step-kernel tile rows: 16 or 32 forced, TILE_ROWS_AUTO (0) timed per
+        grid when the stream is idle, TILE_ROWS_RULE (-1) by grid size only."""
+        check(self.L.fd2d_ctx_set_tile_rows(self.h, int(rows)), self.h)
+
+    def last_tile_rows(self) -> int:
+        return int(self.L.fd2d_ctx_last_tile_rows(self.h))
 
     def last_batch(self):
         """Lane counts of the launch groups of the last batch."""

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <functional>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -119,6 +120,10 @@ struct fd2d_ctx {
   int32_t max_dft_chunk = 0;  // snapshots per DFT contraction (0: 1024, within 2 GiB)
   int32_t max_inj_chunk = 0;  // resident injection planes (0: within 4 GiB)
   std::vector<int32_t> last_lanes;  // lanes of each launch group of the last batch
+  int32_t tile_rows = 0;       // step-kernel tile rows: 0 timed per grid, -1 size rule, 16 or 32 forced
+  int32_t last_tile_rows = 0;  // tile rows of the last FP32 time loop set up
+  std::map<uint64_t, int> tile_choice;  // tuned tile rows by (grid, order, lanes)
+  int32_t concurrent_groups = 0;        // lane groups a batch runs side by side (set while planning)
   std::vector<cudaStream_t> side_streams;
   std::vector<cudaEvent_t> fork_events;
 };

@@ -838,6 +838,16 @@ extern "C" fd2d_status fd2d_ctx_set_chunks(fd2d_ctx* ctx, int32_t max_snapshots,
   return FD2D_OK;
 }
 
+extern "C" fd2d_status fd2d_ctx_set_tile_rows(fd2d_ctx* ctx, int32_t rows) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  if (rows != FD2D_TILE_ROWS_AUTO && rows != FD2D_TILE_ROWS_RULE && rows != 16 && rows != 32)
+    return set_error(ctx, FD2D_ERR_ARG, "tile rows must be 16, 32, FD2D_TILE_ROWS_AUTO or FD2D_TILE_ROWS_RULE");
+  ctx->tile_rows = rows;
+  return FD2D_OK;
+}
+
+extern "C" int32_t fd2d_ctx_last_tile_rows(const fd2d_ctx* ctx) { return ctx ? ctx->last_tile_rows : 0; }
+
 extern "C" fd2d_status fd2d_ctx_set_memory_budget(fd2d_ctx* ctx, int64_t bytes) {
   if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
   if (bytes < 0) return set_error(ctx, FD2D_ERR_ARG, "negative memory budget");
@@ -984,6 +994,7 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
     } else {
       // one plan per lane group; the groups' loops run as parallel graph branches
       std::vector<LoopPlan> plans(lanes.size());
+      ctx->concurrent_groups = (int32_t)lanes.size();
       std::vector<SolveArgs> la;
       for (size_t q = 0; q < lanes.size() && st == FD2D_OK; ++q) {
         ctx->ws_prefix = "L" + std::to_string(q) + ":";
@@ -1000,6 +1011,7 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
         st = fp32_correlation_plan(ctx, B[lanes[q][0]].g, la.data(), (int)la.size(), plans[q]);
       }
       ctx->ws_prefix.clear();
+      ctx->concurrent_groups = 0;
       if (st == FD2D_OK) st = run_parallel(ctx, "batch_corr", 0x2u, plans);
     }
     for (int j = j0; j < j1 && st == FD2D_OK; ++j) {
@@ -1020,6 +1032,7 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
     j0 = j1;
   }
   ctx->ws_prefix.clear();
+  ctx->concurrent_groups = 0;
   if (st != FD2D_OK) return st;
   return finish_call(ctx);
 }

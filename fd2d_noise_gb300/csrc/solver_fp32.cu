@@ -34,12 +34,16 @@
 #include "tma.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 
 namespace fd2d {
 namespace {
 
-constexpr int TX = 32, TZ = 32, NT = 256;
+// Tiles are TX = 32 points wide and TZ rows high; TZ is 16 or 32 (chosen per
+// grid and lane count by tune_tile_rows), with TX/4 * TZ threads per CTA.
+constexpr int TX = 32;
+constexpr int TILE_ROWS[2] = {16, 32};
 constexpr int MAX_BOX_SRC = 64;
 constexpr int MAX_TILE_REC = 32;  // receivers of one tile kept in shared memory
 
@@ -56,8 +60,10 @@ struct Grid32 {
 // Shared-memory layout of one tile (floats, regions 128-byte aligned); the
 // displacement (HU) and injection (HI) regions exist only in the variants
 // that load them.
-template <int R, bool HU = true, bool HI = true>
+template <int R, bool HU = true, bool HI = true, int TZ_ = 32>
 struct Tile {
+  static constexpr int TZ = TZ_;
+  static constexpr int NT = (TX / 4) * TZ;    // one 4-wide row segment per thread in phase 2
   static constexpr int BWc = TX + 2 * R - 1;  // computed v box width (x from x0-R+1)
   static constexpr int BH = TZ + 2 * R - 1;   // box rows (z from z0-R+1)
   static constexpr int SZH = TZ + 4 * R - 2;  // szy rows (z from z0-2R+1)
@@ -112,19 +118,19 @@ struct Step32 {
 };
 
 // One CTA per tile: blockIdx = (tile column, tile row, lane).
-template <int R>
+template <int R, int TZ>
 __device__ __forceinline__ void tile_coords(const Grid32&, int, int& x0, int& z0, int& lane) {
   lane = blockIdx.z;
   z0 = blockIdx.y * TZ;
   x0 = blockIdx.x * TX;
 }
 
-template <int R, bool HU, bool HI>
+template <int R, bool HU, bool HI, int TZ>
 __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, const Step32& S, float* buf,
                                            uint64_t* bar, int t, bool coeffs, bool fields) {
-  using T = Tile<R, HU, HI>;
+  using T = Tile<R, HU, HI, TZ>;
   int x0, z0, lane;
-  tile_coords<R>(G, t, x0, z0, lane);
+  tile_coords<R, TZ>(G, t, x0, z0, lane);
   const int bz0 = z0 - R + 1;
   if (coeffs) {
     uint32_t bytes = 4u * (T::BH * T::SXWa + T::SZH * T::BWa + 3 * T::BH * T::BWa + TZ * TX);
@@ -144,10 +150,11 @@ __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, c
   }
 }
 
-template <int R, bool HU, bool HI>
-__global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
+template <int R, bool HU, bool HI, int TZ>
+__global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB) void k32_step(
     Grid32 G, const __grid_constant__ StepMaps M, Step32 S) {
-  using T = Tile<R, HU, HI>;
+  using T = Tile<R, HU, HI, TZ>;
+  constexpr int NT = T::NT;
   extern __shared__ __align__(128) unsigned char sm_raw[];
   // TMA destinations: 128-byte aligned regardless of the static smem in front
   // (offset arithmetic on the shared array keeps the pointer in the shared
@@ -182,18 +189,18 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
     fence_mbar_init();
     // coefficient planes are not written by the time loop: their loads may
     // overlap the end of the previous step (programmatic dependent launch)
-    issue_tile<R, HU, HI>(G, M, S, sm, &bar, t, true, false);
+    issue_tile<R, HU, HI, TZ>(G, M, S, sm, &bar, t, true, false);
     // The fields are what the previous launch wrote (or will write what it
     // read: ping-pong buffers): wait for it to complete, then load them.  The
     // other threads touch those buffers only after this tile's loads land, so
     // this thread's wait orders the whole CTA after the previous step.
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    issue_tile<R, HU, HI>(G, M, S, sm, &bar, t, false, true);
+    issue_tile<R, HU, HI, TZ>(G, M, S, sm, &bar, t, false, true);
   }
   {
     const float* buf = sm;
     int x0, z0, lane;
-    tile_coords<R>(G, t, x0, z0, lane);
+    tile_coords<R, TZ>(G, t, x0, z0, lane);
     const int bz0 = z0 - R + 1, vx0 = x0 - 4;
     const int64_t lo = (int64_t)lane * G.ps;
     const int2* src_xy = S.src_xy + (int64_t)lane * S.nsrc;
@@ -248,6 +255,9 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
     const bool edge = !(x0 >= R + 4 && x0 + TX + 4 + R <= nx && z0 >= 2 * R - 1 && z0 + TZ + 2 * R <= nz);
     auto compute = [&](auto edge_tag) {
       constexpr bool EDGE = decltype(edge_tag)::value;
+    // Every rounding below is spelled out (__fmaf_rn / __fmul_rn / __fadd_rn), so
+    // the result of a point does not depend on which kernel instantiation (tile
+    // shape, edge or interior path) computes it.
     // ---- new v on the box: 4-wide blocks of rows ---------------------------------------
     // DS = div_s(sxy, szy) (+ sources) (+ injection); v = (v + DS*dt/rho)*taper.
     // Sums are formed in the same order as the scalar form (m = 1..R).
@@ -291,13 +301,13 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
             // sxy(gx + m - 1) is xs[e + 3 + m], sxy(gx - m) is xs[e + 4 - m]
             float ax = 0.f;
 #pragma unroll
-            for (int m = 1; m <= R; ++m) ax += cf[m - 1] * (xs[e + 3 + m] - xs[e + 4 - m]);
+            for (int m = 1; m <= R; ++m) ax = __fmaf_rn(cf[m - 1], __fsub_rn(xs[e + 3 + m], xs[e + 4 - m]), ax);
             // szy(gz + m - 1) is zs[k + R + m - 1], szy(gz - m) is zs[k + R - m]
             float az = 0.f;
 #pragma unroll
-            for (int m = 1; m <= R; ++m) az += cf[m - 1] * (zs[k + R + m - 1][e] - zs[k + R - m][e]);
-            float ds = (!EDGE || (gx >= R && gx <= nx - R - 1)) ? ax * inv_dx : 0.f;
-            ds = (!EDGE || zin) ? ds + az * inv_dz : ds;
+            for (int m = 1; m <= R; ++m) az = __fmaf_rn(cf[m - 1], __fsub_rn(zs[k + R + m - 1][e], zs[k + R - m][e]), az);
+            float ds = (!EDGE || (gx >= R && gx <= nx - R - 1)) ? __fmul_rn(ax, inv_dx) : 0.f;
+            ds = (!EDGE || zin) ? __fmaf_rn(az, inv_dz, ds) : ds;
             dsv[e] = ds;
           }
           if (nbs) {
@@ -309,7 +319,7 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
                 const int d = s_src[qq] - idx0;
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
-                  if (d == e) dsv[e] += s_amp[qq];
+                  if (d == e) dsv[e] = __fadd_rn(dsv[e], s_amp[qq]);
               }
             } else {
               for (int qq = 0; qq < S.nsrc; ++qq) {
@@ -317,7 +327,7 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
                 const int d = w.x - (vx0 + c0);
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
-                  if (w.y == gz && d == e) dsv[e] += amp ? (float)amp[qq] : S.amp_const;
+                  if (w.y == gz && d == e) dsv[e] = __fadd_rn(dsv[e], amp ? (float)amp[qq] : S.amp_const);
               }
             }
           }
@@ -333,8 +343,8 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
           float out[4];
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            const float ds = inj ? dsv[e] + ii[e] : dsv[e];
-            out[e] = (vv[e] + ds * bb[e]) * tt[e];
+            const float ds = inj ? __fadd_rn(dsv[e], ii[e]) : dsv[e];
+            out[e] = __fmul_rn(__fmaf_rn(ds, bb[e], vv[e]), tt[e]);
           }
           *reinterpret_cast<float4*>(s_vn + rr * W + c0) = make_float4(out[0], out[1], out[2], out[3]);
         }
@@ -383,12 +393,13 @@ __global__ __launch_bounds__(NT, Tile<R, HU, HI>::MINB) void k32_step(
           vn[e] = vx[e + 4];
           float ax = 0.f, az = 0.f;
 #pragma unroll
-          for (int m = 1; m <= R; ++m) ax += cf[m - 1] * (vx[e + m + 4] - vx[e - m + 5]);
+          for (int m = 1; m <= R; ++m) ax = __fmaf_rn(cf[m - 1], __fsub_rn(vx[e + m + 4], vx[e - m + 5]), ax);
 #pragma unroll
-          for (int m = 1; m <= R; ++m) az += cf[m - 1] * (vz[R - 1 + m][e] - vz[R - m][e]);
-          nsx[e] = (!EDGE || (i >= R - 1 && i <= nx - R - 1)) ? sxo[e] + mu[e] * (ax * inv_dx) : sxo[e];
-          nsz[e] = (!EDGE || zin) ? szo[e] + mu[e] * (az * inv_dz) : szo[e];
-          nu[e] = HU ? uo[e] + vn[e] * gdt : vn[e];
+          for (int m = 1; m <= R; ++m) az = __fmaf_rn(cf[m - 1], __fsub_rn(vz[R - 1 + m][e], vz[R - m][e]), az);
+          nsx[e] = (!EDGE || (i >= R - 1 && i <= nx - R - 1)) ? __fmaf_rn(mu[e], __fmul_rn(ax, inv_dx), sxo[e])
+                                                              : sxo[e];
+          nsz[e] = (!EDGE || zin) ? __fmaf_rn(mu[e], __fmul_rn(az, inv_dz), szo[e]) : szo[e];
+          nu[e] = HU ? __fmaf_rn(vn[e], gdt, uo[e]) : vn[e];
         }
         const int64_t p = lo + i0 + (int64_t)P * j;
         if (!EDGE || i0 + 3 < nx) {
@@ -620,6 +631,7 @@ struct Run {
   StepMaps maps[2];  // read buffers 0 / 1
   dim3 sgrid, pgrid, pblock{32, 8};
   int R = 2;
+  int tz = 32;  // tile rows of the step kernel (16 or 32)
   int2* rec_xy = nullptr;
   int2* src_xy = nullptr;
   int2* tile_rec = nullptr;  // per (lane, tile): {first entry, count}
@@ -633,19 +645,26 @@ struct Run {
 // Step launches carry the programmatic-stream-serialization attribute: a step
 // may be scheduled while the previous one drains; k32_step waits for it with
 // griddepcontrol.wait before touching the fields.
-template <int R, bool HU, bool HI>
-void launch_step_v(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
+template <int R, bool HU, bool HI, int TZ>
+void launch_step_t(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
+  using T = Tile<R, HU, HI, TZ>;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = r.sgrid;
-  cfg.blockDim = dim3(NT);
-  cfg.dynamicSmemBytes = Tile<R, HU, HI>::BYTES;
+  cfg.blockDim = dim3(T::NT);
+  cfg.dynamicSmemBytes = T::BYTES;
   cfg.stream = ctx->stream;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k32_step<R, HU, HI>, r.G, r.maps[par], s);
+  cudaLaunchKernelEx(&cfg, k32_step<R, HU, HI, TZ>, r.G, r.maps[par], s);
+}
+
+template <int R, bool HU, bool HI>
+void launch_step_v(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
+  if (r.tz == 16) launch_step_t<R, HU, HI, 16>(ctx, r, par, s);
+  else launch_step_t<R, HU, HI, 32>(ctx, r, par, s);
 }
 
 template <int R>
@@ -660,17 +679,23 @@ void launch_step_r(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
   }
 }
 
+template <int R, int TZ>
+fd2d_status step_attributes_t(fd2d_ctx* ctx) {
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, false, false, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, false, false, TZ>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, false, true, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, false, true, TZ>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, true, false, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, true, false, TZ>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, true, true, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, true, true, TZ>::BYTES));
+  return FD2D_OK;
+}
+
 template <int R>
 fd2d_status step_attributes_r(fd2d_ctx* ctx) {
-  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      Tile<R, false, false>::BYTES));
-  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      Tile<R, false, true>::BYTES));
-  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      Tile<R, true, false>::BYTES));
-  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step<R, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      Tile<R, true, true>::BYTES));
-  return FD2D_OK;
+  FD2D_TRY((step_attributes_t<R, 16>(ctx)));
+  return step_attributes_t<R, 32>(ctx);
 }
 
 // Opt the step kernels in to their dynamic shared memory (once, before any capture).
@@ -710,7 +735,7 @@ fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, int par, Step32 s) {
   }
 
 fd2d_status make_maps(fd2d_ctx* ctx, Run& r) {
-  const int nx = r.G.nx, nz = r.G.nz, P = r.G.P, R = r.R;
+  const int nx = r.G.nx, nz = r.G.nz, P = r.G.P, R = r.R, TZ = r.tz;
   const int BH = TZ + 2 * R - 1, SZH = TZ + 4 * R - 2, BWa = TX + 8, SXWa = TX + 16;
   for (int q = 0; q < 2; ++q) {
     StepMaps& m = r.maps[q];
@@ -731,15 +756,15 @@ fd2d_status make_maps(fd2d_ctx* ctx, Run& r) {
 
 // Injection planes are [event][lane] planes of stride ps: lane l of event j is plane j*S + l.
 fd2d_status set_inj_map(fd2d_ctx* ctx, Run& r, const float* planes, int n_planes) {
-  const int BH = TZ + 2 * r.R - 1, BWa = TX + 8;
+  const int BH = r.tz + 2 * r.R - 1, BWa = TX + 8;
   for (int q = 0; q < 2; ++q)
     FD2D_TRY(make_tmap_f32(ctx, &r.maps[q].inj, planes, r.G.nx, r.G.nz, r.G.P, BWa, BH, n_planes, r.ps));
   return FD2D_OK;
 }
 
 // CSR of receivers by (lane, tile) of the step grid: table[(l*ntz + tz)*ntx + tx]
-// = {first, count} into ent = {k, (z - tz*TZ)*TX + (x - tx*TX)}.
-void build_tile_receivers_idx(int nx, int nz, const std::vector<const std::vector<int>*>& lanes,
+// = {first, count} into ent = {k, (z - tz*TZ)*TX + (x - tx*TX)}; TZ = tile rows.
+void build_tile_receivers_idx(int nx, int nz, int TZ, const std::vector<const std::vector<int>*>& lanes,
                               std::vector<int2>& table, std::vector<int2>& ent) {
   const int ntx = (nx + TX - 1) / TX, ntz = (nz + TZ - 1) / TZ;
   const int S = (int)lanes.size();
@@ -761,11 +786,104 @@ void build_tile_receivers_idx(int nx, int nz, const std::vector<const std::vecto
   if (ent.empty()) ent.push_back(make_int2(0, 0));
 }
 
-void build_tile_receivers(int nx, int nz, const SolveArgs* a, int S, std::vector<int2>& table,
+void build_tile_receivers(int nx, int nz, int TZ, const SolveArgs* a, int S, std::vector<int2>& table,
                           std::vector<int2>& ent) {
   std::vector<const std::vector<int>*> lanes;
   for (int l = 0; l < S; ++l) lanes.push_back(&a[l].rec_idx);
-  build_tile_receivers_idx(nx, nz, lanes, table, ent);
+  build_tile_receivers_idx(nx, nz, TZ, lanes, table, ent);
+}
+
+// Step grid and tensor maps of the run's tile rows r.tz.
+fd2d_status set_tiling(fd2d_ctx* ctx, Run& r) {
+  r.G.ntx = (r.G.nx + TX - 1) / TX;
+  r.G.ntz = (r.G.nz + r.tz - 1) / r.tz;
+  r.sgrid = dim3(r.G.ntx, r.G.ntz, r.S);
+  return make_maps(ctx, r);
+}
+
+// Tile rows of the step kernel for this grid and lane count.  Forced by
+// fd2d_ctx_set_tile_rows (or FD2D_TILE_ROWS).  Otherwise, when the context's
+// stream is idle and no other lane group of a batch runs beside this one, both
+// shapes are timed once per context on this run's freshly zeroed fields --
+// Green-function steps with no sources, receivers or snapshots -- and the
+// faster (by more than 1 %, else the size rule's shape) is kept for later runs
+// of the same grid, order and lane count.  When timing would stall queued or
+// concurrent work, or during a stream capture, the size rule decides: 32 rows
+// when the grid has at least four CTAs of 32 rows per SM, else 16 (measured on
+// GB300: 600x600 with two lanes runs 2 % faster with 32 rows, one lane 2 %
+// faster with 16; concurrent lane groups of 256-800 point grids favour 16).
+fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
+  int forced = ctx->tile_rows;
+  if (forced == FD2D_TILE_ROWS_AUTO) {
+    const char* e = std::getenv("FD2D_TILE_ROWS");
+    if (e) forced = std::atoi(e);
+  }
+  if (forced == 16 || forced == 32) {
+    r.tz = forced;
+    return FD2D_OK;
+  }
+  Sig key;
+  key.add(r.G.nx); key.add(r.G.nz); key.add(r.R); key.add(r.S);
+  auto it = ctx->tile_choice.find(key.h);
+  if (it != ctx->tile_choice.end()) {
+    r.tz = it->second;
+    return FD2D_OK;
+  }
+  const int64_t tiles32 = (int64_t)((r.G.nx + TX - 1) / TX) * ((r.G.nz + 31) / 32) * r.S;
+  const int rule = tiles32 >= 4 * std::max(ctx->sm_count, 1) ? 32 : 16;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  FD2D_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
+  bool idle = cs == cudaStreamCaptureStatusNone && ctx->concurrent_groups <= 1 && forced != FD2D_TILE_ROWS_RULE;
+  if (idle) {
+    idle = cudaStreamQuery(ctx->stream) == cudaSuccess;
+    cudaGetLastError();  // a busy stream answers cudaErrorNotReady
+  }
+  if (!idle) {
+    r.tz = rule;
+    return FD2D_OK;
+  }
+  constexpr int WARM = 3, TIMED = 24;
+  cudaEvent_t e0, e1;
+  FD2D_CUDA(ctx, cudaEventCreate(&e0));
+  FD2D_CUDA(ctx, cudaEventCreate(&e1));
+  float ms_of[2] = {0.f, 0.f};
+  fd2d_status st = FD2D_OK;
+  for (int c = 0; c < 2; ++c) {
+    const int tz = TILE_ROWS[c];
+    r.tz = tz;
+    if ((st = set_tiling(ctx, r)) != FD2D_OK) break;
+    Step32 s{};
+    s.inj_plane = -1;
+    s.src_xy = r.src_xy;
+    s.rec_xy = r.rec_xy;
+    for (int n = 0; n < WARM && st == FD2D_OK; ++n) st = launch_step(ctx, r, n & 1, s);
+    cudaEventRecord(e0, ctx->stream);
+    for (int n = 0; n < TIMED && st == FD2D_OK; ++n) st = launch_step(ctx, r, n & 1, s);
+    cudaEventRecord(e1, ctx->stream);
+    if (st != FD2D_OK) break;
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      st = set_error(ctx, FD2D_ERR_CUDA, "tile-row timing failed");
+      break;
+    }
+    ms_of[c] = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != FD2D_OK) return st;
+  // the timed steps ran on the zeroed fields: zero them again
+  const size_t bytes = (size_t)r.lanes_ps() * 4;
+  for (int q = 0; q < 2; ++q) {
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.v[q], 0, bytes, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.sxy[q], 0, bytes, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.szy[q], 0, bytes, ctx->stream));
+  }
+  // the other shape must win by more than 1 % to override the rule
+  const int other = rule == TILE_ROWS[0] ? 1 : 0;
+  const float rule_ms = ms_of[1 - other];
+  r.tz = ms_of[other] < 0.99f * rule_ms ? TILE_ROWS[other] : rule;
+  ctx->tile_choice[key.h] = r.tz;
+  return FD2D_OK;
 }
 
 // Buffers, coefficient planes and tensor maps of S lanes a[0..S-1] (solves of
@@ -828,20 +946,19 @@ fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S
   };
   FD2D_TRY(upload(ctx, "f32.rec", xy(true), &r.rec_xy));
   FD2D_TRY(upload(ctx, "f32.src", xy(false), &r.src_xy));
-  {
-    // receivers grouped by step tile, so each CTA finds its own in one read
-    std::vector<int2> table, ent;
-    build_tile_receivers(nx, nz, a, S, table, ent);
-    FD2D_TRY(upload(ctx, "f32.tile_rec", table, &r.tile_rec));
-    FD2D_TRY(upload(ctx, "f32.rec_ent", ent, &r.rec_ent));
-  }
-  r.G.ntx = (nx + TX - 1) / TX;
-  r.G.ntz = (nz + TZ - 1) / TZ;
-  r.sgrid = dim3(r.G.ntx, r.G.ntz, S);
   r.pgrid = dim3((nx + 31) / 32, (nz + 7) / 8);
   FD2D_TRY(step_attributes(ctx));
   FD2D_TRY(contract_prepare(ctx));
-  return make_maps(ctx, r);
+  FD2D_TRY(tune_tile_rows(ctx, r));
+  ctx->last_tile_rows = r.tz;
+  {
+    // receivers grouped by step tile, so each CTA finds its own in one read
+    std::vector<int2> table, ent;
+    build_tile_receivers(nx, nz, r.tz, a, S, table, ent);
+    FD2D_TRY(upload(ctx, "f32.tile_rec", table, &r.tile_rec));
+    FD2D_TRY(upload(ctx, "f32.rec_ent", ent, &r.rec_ent));
+  }
+  return set_tiling(ctx, r);
 }
 
 // Frequency-band weights (interpol_matrix) on the device.
@@ -1062,7 +1179,7 @@ void sig_run(Sig& sg, const Run& r) {
   for (int q = 0; q < 2; ++q) { sg.add(r.v[q]); sg.add(r.sxy[q]); sg.add(r.szy[q]); sg.add(r.u[q]); }
   sg.bytes(r.maps, sizeof(r.maps));
   sg.add(r.sgrid.x); sg.add(r.sgrid.y); sg.add(r.sgrid.z); sg.add(r.pgrid.x); sg.add(r.pgrid.y);
-  sg.add(r.R); sg.add(r.rec_xy); sg.add(r.src_xy); sg.add(r.np); sg.add(r.ps);
+  sg.add(r.R); sg.add(r.tz); sg.add(r.rec_xy); sg.add(r.src_xy); sg.add(r.np); sg.add(r.ps);
 }
 
 void sig_args(Sig& sg, const Geometry& g, const SolveArgs& a) {
@@ -1536,8 +1653,9 @@ extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg,
     r.szy[q] = planes + (7 + q) * ps;
     r.u[q] = nullptr;
   }
+  r.tz = 32;  // no timing here: the allocation-free path keeps one shape
   r.G.ntx = (nx + TX - 1) / TX;
-  r.G.ntz = (nz + TZ - 1) / TZ;
+  r.G.ntz = (nz + r.tz - 1) / r.tz;
   r.sgrid = dim3(r.G.ntx, r.G.ntz, 1);
   r.pgrid = dim3((P + 31) / 32, (nz + 7) / 8);
   // The array keeps the previous call's contents: clear what must start at zero.
@@ -1570,12 +1688,16 @@ extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg,
     s.sxyo = r.sxy[1 - par];
     s.szyo = r.szy[1 - par];
     s.uo = nullptr;
+#define FD2D_NOALLOC_STEP(R_)                                                                            \
+  k32_step<R_, false, false, 32><<<r.sgrid, Tile<R_, false, false, 32>::NT, Tile<R_, false, false, 32>::BYTES, \
+                                   stream>>>(r.G, r.maps[par], s)
     switch (r.R) {
-      case 1: k32_step<1, false, false><<<r.sgrid, NT, Tile<1, false, false>::BYTES, stream>>>(r.G, r.maps[par], s); break;
-      case 2: k32_step<2, false, false><<<r.sgrid, NT, Tile<2, false, false>::BYTES, stream>>>(r.G, r.maps[par], s); break;
-      case 3: k32_step<3, false, false><<<r.sgrid, NT, Tile<3, false, false>::BYTES, stream>>>(r.G, r.maps[par], s); break;
-      default: k32_step<4, false, false><<<r.sgrid, NT, Tile<4, false, false>::BYTES, stream>>>(r.G, r.maps[par], s); break;
+      case 1: FD2D_NOALLOC_STEP(1); break;
+      case 2: FD2D_NOALLOC_STEP(2); break;
+      case 3: FD2D_NOALLOC_STEP(3); break;
+      default: FD2D_NOALLOC_STEP(4); break;
     }
+#undef FD2D_NOALLOC_STEP
     FD2D_CUDA(nullptr, cudaGetLastError());
   }
   int herr = 0;

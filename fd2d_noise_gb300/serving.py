@@ -233,6 +233,9 @@ class Server:
             from . import _lib, solvers
             from .solvers import _prec
             ctx = _lib.Context(self.device, _prec(self.precision))
+            # slots share the GPU: pick tile shapes by the size rule rather than
+            # by timing trial steps, which would wait for this slot's queue
+            ctx.set_tile_rows(_lib.TILE_ROWS_RULE)
             bind = solvers.bound_context(ctx)
             bind.__enter__()
         try:
