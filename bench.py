@@ -185,6 +185,7 @@ def main():
     ap.add_argument("--cpu-nt", type=int, default=120)
     ap.add_argument("--nt", type=int, default=0, help="override the workload's nt (profiling runs)")
     ap.add_argument("--stations", type=int, default=0, help="override the number of reference stations")
+    ap.add_argument("--grid", type=int, default=0, help="square grid size of single_600_o8 (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -203,6 +204,8 @@ def main():
     kw = {"nt": args.nt} if args.nt else {}
     if args.stations:
         kw["n_ref"] = args.stations
+    if args.grid:
+        kw["nx"] = args.grid
     w = WORKLOADS[args.workload](**kw)
     if args.impl == "reference":
         run_reference(args, w, world, rank)

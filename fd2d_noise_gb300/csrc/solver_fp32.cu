@@ -43,7 +43,8 @@ namespace {
 // Tiles are TX = 32 points wide and TZ rows high; TZ is 16 or 32 (chosen per
 // grid and lane count by tune_tile_rows), with TX/4 * TZ threads per CTA.
 constexpr int TX = 32;
-constexpr int TILE_ROWS[2] = {16, 32};
+constexpr int N_TILE_ROWS = 3;
+constexpr int TILE_ROWS[N_TILE_ROWS] = {16, 32, 40};
 constexpr int MAX_BOX_SRC = 64;
 constexpr int MAX_TILE_REC = 32;  // receivers of one tile kept in shared memory
 
@@ -59,11 +60,15 @@ struct Grid32 {
 
 // Shared-memory layout of one tile (floats, regions 128-byte aligned); the
 // displacement (HU) and injection (HI) regions exist only in the variants
-// that load them.
+// that load them.  The new v is written over the old one in place.  Tiles
+// taller than 32 rows read the injection plane straight from L2 (it is only
+// needed point-wise), which keeps four of them resident per SM.
 template <int R, bool HU = true, bool HI = true, int TZ_ = 32>
 struct Tile {
   static constexpr int TZ = TZ_;
-  static constexpr int NT = (TX / 4) * TZ;    // one 4-wide row segment per thread in phase 2
+  // one 4-wide row segment per thread in phase 2, at most 256 threads
+  static constexpr int NT = (TX / 4) * TZ < 256 ? (TX / 4) * TZ : 256;
+  static constexpr bool INJ_SMEM = HI && TZ <= 32;
   static constexpr int BWc = TX + 2 * R - 1;  // computed v box width (x from x0-R+1)
   static constexpr int BH = TZ + 2 * R - 1;   // box rows (z from z0-R+1)
   static constexpr int SZH = TZ + 4 * R - 2;  // szy rows (z from z0-2R+1)
@@ -76,10 +81,9 @@ struct Tile {
   static constexpr int O_B = O_V + al(BH * BWa);
   static constexpr int O_T = O_B + al(BH * BWa);
   static constexpr int O_I = O_T + al(BH * BWa);
-  static constexpr int O_MU = O_I + (HI ? al(BH * BWa) : 0);
+  static constexpr int O_MU = O_I + (INJ_SMEM ? al(BH * BWa) : 0);
   static constexpr int O_U = O_MU + al(TZ * TX);
-  static constexpr int O_VN = O_U + (HU ? al(TZ * TX) : 0);
-  static constexpr int TOTAL = O_VN + al(BH * BWa);  // new v on the 40-wide box (x from x0-4)
+  static constexpr int TOTAL = O_U + (HU ? al(TZ * TX) : 0);
   static_assert(BH + 2 * R - 1 <= SZH, "the z sum of the last box row stays inside the szy rows");
   static constexpr int BYTES = TOTAL * 4 + 128;      // + alignment slack
   // resident CTAs per SM the shared memory allows (228 KB per SM, 1 KB per CTA
@@ -107,6 +111,7 @@ struct Step32 {
   float amp_const;
   float* snap_pre;               // single(old field) in MATLAB layout, or nullptr (one lane only)
   int snap_pre_u;
+  const float* inj_base;         // injection planes ([plane][lane] of stride ps), read when not staged
   float* snap_dft;               // new field (v or u) into the DFT snapshot plane (pitched); per lane + l*ps
   const int2* rec_xy;            // per lane + l*nrec
   int nrec;
@@ -135,7 +140,7 @@ __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, c
   if (coeffs) {
     uint32_t bytes = 4u * (T::BH * T::SXWa + T::SZH * T::BWa + 3 * T::BH * T::BWa + TZ * TX);
     if (HU) bytes += 4u * TZ * TX;
-    if (HI) bytes += 4u * T::BH * T::BWa;
+    if (T::INJ_SMEM) bytes += 4u * T::BH * T::BWa;
     mbar_expect_tx(bar, bytes);
     tma_load_3d(buf + T::O_B, &M.b, x0 - 4, bz0, lane, bar);
     tma_load_3d(buf + T::O_T, &M.taper, x0 - 4, bz0, lane, bar);
@@ -146,7 +151,7 @@ __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, c
     tma_load_3d(buf + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, lane, bar);
     tma_load_3d(buf + T::O_V, &M.v, x0 - 4, bz0, lane, bar);
     if (HU) tma_load_3d(buf + T::O_U, &M.u, x0, z0, lane, bar);
-    if (HI) tma_load_3d(buf + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, bar);
+    if (T::INJ_SMEM) tma_load_3d(buf + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, bar);
   }
 }
 
@@ -176,7 +181,7 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
   const int nx = G.nx, nz = G.nz, P = G.P;
   const int n_tiles = G.ntx * G.ntz * G.S;
   constexpr int W = T::BWa;  // 40: row stride of the box regions
-  float* s_vn = sm + T::O_VN;
+  float* s_vn = sm + T::O_V;  // new v, written over the old v of the same point
   constexpr bool inj = HI;
 
   // tile number in the per-(lane, tile) tables
@@ -337,7 +342,24 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
           const float4 b4 = *reinterpret_cast<const float4*>(s_b + rr * W + c0);
           const float4 t4 = *reinterpret_cast<const float4*>(s_t + rr * W + c0);
           float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (inj) i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
+          if (T::INJ_SMEM) {
+            i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
+          } else if (inj) {
+            // from L2; outside the grid the plane is zero (as the TMA fill)
+            const int gx0 = vx0 + c0;
+            if (gx0 >= 0 && gx0 < P && gz >= 0 && gz < nz)
+              i4 = __ldg(reinterpret_cast<const float4*>(
+                  S.inj_base + ((int64_t)S.inj_plane * G.S + lane) * G.ps + (int64_t)P * gz + gx0));
+          }
+          if (S.snap_pre && !S.snap_pre_u && rr >= R - 1 && rr < R - 1 + TZ && c0 >= 4 && c0 < 4 + TX) {
+            // single(v) before the update at the tile's own points, taken here
+            // because the new v replaces the old one in shared memory
+            const int gx0 = vx0 + c0;
+            const float vo[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if (!EDGE || (gx0 + e < nx && gz < nz)) S.snap_pre[gx0 + e + (int64_t)nx * gz] = vo[e];
+          }
           const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
           const float tt[4] = {t4.x, t4.y, t4.z, t4.w}, ii[4] = {i4.x, i4.y, i4.z, i4.w};
           float out[4];
@@ -352,10 +374,10 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
     }
     __syncthreads();
 
-    // ---- stress, displacement and outputs: each thread a 4-wide row segment ---------
-    {
-      constexpr int NQ2 = TX / 4;  // 8 quads per row, TZ rows: NQ2 * TZ == NT
-      const int q = tid % NQ2, tz = tid / NQ2;
+    // ---- stress, displacement and outputs: each thread 4-wide row segments -----------
+    constexpr int NQ2 = TX / 4;  // 8 quads per row
+    for (int it = tid; it < NQ2 * TZ; it += NT) {
+      const int q = it % NQ2, tz = it / NQ2;
       const int j = z0 + tz;
       const int i0 = x0 + 4 * q;
       if (tz < TZ && (!EDGE || (j < nz && i0 < nx))) {
@@ -440,11 +462,11 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
             }
           }
         }
-        if (S.snap_pre) {
-          const float* old = S.snap_pre_u ? s_u + tz * TX + 4 * q : s_v + rr * W + cv;
+        if (HU && S.snap_pre && S.snap_pre_u) {
+          const float* old = s_u + tz * TX + 4 * q;
 #pragma unroll
           for (int e = 0; e < 4; ++e)
-            if (!EDGE || i0 + e < nx) S.snap_pre[i0 + e + nx * j] = old[e];
+            if (!EDGE || i0 + e < nx) S.snap_pre[i0 + e + (int64_t)nx * j] = old[e];
         }
       }
     }
@@ -631,7 +653,8 @@ struct Run {
   StepMaps maps[2];  // read buffers 0 / 1
   dim3 sgrid, pgrid, pblock{32, 8};
   int R = 2;
-  int tz = 32;  // tile rows of the step kernel (16 or 32)
+  int tz = 32;  // tile rows of the step kernel (TILE_ROWS)
+  const float* inj_planes = nullptr;  // injection planes (set_inj_map)
   int2* rec_xy = nullptr;
   int2* src_xy = nullptr;
   int2* tile_rec = nullptr;  // per (lane, tile): {first entry, count}
@@ -664,6 +687,7 @@ void launch_step_t(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
 template <int R, bool HU, bool HI>
 void launch_step_v(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
   if (r.tz == 16) launch_step_t<R, HU, HI, 16>(ctx, r, par, s);
+  else if (r.tz == 40) launch_step_t<R, HU, HI, 40>(ctx, r, par, s);
   else launch_step_t<R, HU, HI, 32>(ctx, r, par, s);
 }
 
@@ -695,6 +719,7 @@ fd2d_status step_attributes_t(fd2d_ctx* ctx) {
 template <int R>
 fd2d_status step_attributes_r(fd2d_ctx* ctx) {
   FD2D_TRY((step_attributes_t<R, 16>(ctx)));
+  FD2D_TRY((step_attributes_t<R, 40>(ctx)));
   return step_attributes_t<R, 32>(ctx);
 }
 
@@ -711,6 +736,7 @@ fd2d_status step_attributes(fd2d_ctx* ctx) {
 }
 
 fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, int par, Step32 s) {
+  s.inj_base = r.inj_planes;
   s.tile_rec = r.tile_rec;
   s.rec_ent = r.rec_ent;
   s.vo = r.v[1 - par];
@@ -757,6 +783,7 @@ fd2d_status make_maps(fd2d_ctx* ctx, Run& r) {
 // Injection planes are [event][lane] planes of stride ps: lane l of event j is plane j*S + l.
 fd2d_status set_inj_map(fd2d_ctx* ctx, Run& r, const float* planes, int n_planes) {
   const int BH = r.tz + 2 * r.R - 1, BWa = TX + 8;
+  r.inj_planes = planes;
   for (int q = 0; q < 2; ++q)
     FD2D_TRY(make_tmap_f32(ctx, &r.maps[q].inj, planes, r.G.nx, r.G.nz, r.G.P, BWa, BH, n_planes, r.ps));
   return FD2D_OK;
@@ -801,27 +828,55 @@ fd2d_status set_tiling(fd2d_ctx* ctx, Run& r) {
   return make_maps(ctx, r);
 }
 
-// Tile rows of the step kernel for this grid and lane count.  Forced by
-// fd2d_ctx_set_tile_rows (or FD2D_TILE_ROWS).  Otherwise, when the context's
-// stream is idle and no other lane group of a batch runs beside this one, both
-// shapes are timed once per context on this run's freshly zeroed fields --
-// Green-function steps with no sources, receivers or snapshots -- and the
-// faster (by more than 1 %, else the size rule's shape) is kept for later runs
-// of the same grid, order and lane count.  When timing would stall queued or
-// concurrent work, or during a stream capture, the size rule decides: 32 rows
-// when the grid has at least four CTAs of 32 rows per SM, else 16 (measured on
-// GB300: 600x600 with two lanes runs 2 % faster with 32 rows, one lane 2 %
-// faster with 16; concurrent lane groups of 256-800 point grids favour 16).
+// Resident CTAs per SM of the (largest, displacement) step kernel with TZ rows.
+template <int R, int TZ>
+int step_ctas_t() {
+  using T = Tile<R, true, false, TZ>;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k32_step<R, true, false, TZ>, T::NT, T::BYTES) != cudaSuccess) {
+    cudaGetLastError();
+    n = 1;
+  }
+  return std::max(n, 1);
+}
+
+template <int R>
+int step_ctas_r(int tz) {
+  return tz == 16 ? step_ctas_t<R, 16>() : tz == 40 ? step_ctas_t<R, 40>() : step_ctas_t<R, 32>();
+}
+
+int step_ctas(int R, int tz) {
+  switch (R) {
+    case 1: return step_ctas_r<1>(tz);
+    case 2: return step_ctas_r<2>(tz);
+    case 3: return step_ctas_r<3>(tz);
+    default: return step_ctas_r<4>(tz);
+  }
+}
+
+// Tile rows of the step kernel for this grid and lane count (TILE_ROWS).
+// Forced by fd2d_ctx_set_tile_rows (or FD2D_TILE_ROWS).  Otherwise, when the
+// context's stream is idle and no other lane group of a batch runs beside this
+// one, every shape is timed once per context on this run's freshly zeroed
+// fields -- Green-function steps with no sources, receivers or snapshots --
+// and the fastest is kept for later runs of the same grid, order and lane
+// count if it beats the size rule's shape by more than 1 %.  When timing would
+// stall queued or concurrent work, or during a stream capture, the size rule
+// decides: the fewest waves of CTAs (tiles over resident CTAs per SM x SMs),
+// the shortest tiles among equals.  The step time is set by the waves: on
+// GB300 a 600x600 Green step takes ~5.5 us for any tile count up to one wave
+// and ~7.7 us just past it.
 fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
   int forced = ctx->tile_rows;
   if (forced == FD2D_TILE_ROWS_AUTO) {
     const char* e = std::getenv("FD2D_TILE_ROWS");
     if (e) forced = std::atoi(e);
   }
-  if (forced == 16 || forced == 32) {
-    r.tz = forced;
-    return FD2D_OK;
-  }
+  for (int tz : TILE_ROWS)
+    if (forced == tz) {
+      r.tz = forced;
+      return FD2D_OK;
+    }
   Sig key;
   key.add(r.G.nx); key.add(r.G.nz); key.add(r.R); key.add(r.S);
   auto it = ctx->tile_choice.find(key.h);
@@ -829,8 +884,17 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
     r.tz = it->second;
     return FD2D_OK;
   }
-  const int64_t tiles32 = (int64_t)((r.G.nx + TX - 1) / TX) * ((r.G.nz + 31) / 32) * r.S;
-  const int rule = tiles32 >= 4 * std::max(ctx->sm_count, 1) ? 32 : 16;
+  int rule = TILE_ROWS[0];
+  int64_t rule_waves = -1;
+  for (int tz : TILE_ROWS) {
+    const int64_t tiles = (int64_t)((r.G.nx + TX - 1) / TX) * ((r.G.nz + tz - 1) / tz) * r.S;
+    const int64_t slots = (int64_t)step_ctas(r.R, tz) * std::max(ctx->sm_count, 1);
+    const int64_t waves = (tiles + slots - 1) / slots;
+    if (rule_waves < 0 || waves < rule_waves) {
+      rule = tz;
+      rule_waves = waves;
+    }
+  }
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   FD2D_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
   bool idle = cs == cudaStreamCaptureStatusNone && ctx->concurrent_groups <= 1 && forced != FD2D_TILE_ROWS_RULE;
@@ -846,11 +910,10 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
   cudaEvent_t e0, e1;
   FD2D_CUDA(ctx, cudaEventCreate(&e0));
   FD2D_CUDA(ctx, cudaEventCreate(&e1));
-  float ms_of[2] = {0.f, 0.f};
+  float ms_of[N_TILE_ROWS] = {};
   fd2d_status st = FD2D_OK;
-  for (int c = 0; c < 2; ++c) {
-    const int tz = TILE_ROWS[c];
-    r.tz = tz;
+  for (int c = 0; c < N_TILE_ROWS; ++c) {
+    r.tz = TILE_ROWS[c];
     if ((st = set_tiling(ctx, r)) != FD2D_OK) break;
     Step32 s{};
     s.inj_plane = -1;
@@ -861,12 +924,10 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
     for (int n = 0; n < TIMED && st == FD2D_OK; ++n) st = launch_step(ctx, r, n & 1, s);
     cudaEventRecord(e1, ctx->stream);
     if (st != FD2D_OK) break;
-    float ms = 0.f;
-    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms_of[c], e0, e1) != cudaSuccess) {
       st = set_error(ctx, FD2D_ERR_CUDA, "tile-row timing failed");
       break;
     }
-    ms_of[c] = ms;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -878,10 +939,12 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
     FD2D_CUDA(ctx, cudaMemsetAsync(r.sxy[q], 0, bytes, ctx->stream));
     FD2D_CUDA(ctx, cudaMemsetAsync(r.szy[q], 0, bytes, ctx->stream));
   }
-  // the other shape must win by more than 1 % to override the rule
-  const int other = rule == TILE_ROWS[0] ? 1 : 0;
-  const float rule_ms = ms_of[1 - other];
-  r.tz = ms_of[other] < 0.99f * rule_ms ? TILE_ROWS[other] : rule;
+  int best = 0, ri = 0;
+  for (int c = 0; c < N_TILE_ROWS; ++c) {
+    if (ms_of[c] < ms_of[best]) best = c;
+    if (TILE_ROWS[c] == rule) ri = c;
+  }
+  r.tz = ms_of[best] < 0.99f * ms_of[ri] ? TILE_ROWS[best] : rule;
   ctx->tile_choice[key.h] = r.tz;
   return FD2D_OK;
 }
@@ -1179,7 +1242,7 @@ void sig_run(Sig& sg, const Run& r) {
   for (int q = 0; q < 2; ++q) { sg.add(r.v[q]); sg.add(r.sxy[q]); sg.add(r.szy[q]); sg.add(r.u[q]); }
   sg.bytes(r.maps, sizeof(r.maps));
   sg.add(r.sgrid.x); sg.add(r.sgrid.y); sg.add(r.sgrid.z); sg.add(r.pgrid.x); sg.add(r.pgrid.y);
-  sg.add(r.R); sg.add(r.tz); sg.add(r.rec_xy); sg.add(r.src_xy); sg.add(r.np); sg.add(r.ps);
+  sg.add(r.R); sg.add(r.tz); sg.add(r.inj_planes); sg.add(r.rec_xy); sg.add(r.src_xy); sg.add(r.np); sg.add(r.ps);
 }
 
 void sig_args(Sig& sg, const Geometry& g, const SolveArgs& a) {

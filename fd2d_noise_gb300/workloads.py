@@ -70,8 +70,9 @@ def plain_cpu_300(nt: int = 1200) -> Workload:
     return Workload("plain_cpu_300", cfg, mu, rho, ref, rec, spec, sd)
 
 
-def single_600_o8(nt: int = 3000, K: int = 300, n_ref: int = 2) -> Workload:
-    nx = 600
+def single_600_o8(nt: int = 3000, K: int = 300, n_ref: int = 2, nx: int = 600) -> Workload:
+    """``nx`` (square grid) other than 600 is for profiling the step kernel
+    across grid sizes; the workload is named for its grid."""
     dx = L / (nx - 1)
     cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.05, nt=nt, order=8, f_sample=_freqs(0.01, 0.2, K),
                  freq_samp=5, fw_nth=1, absorb_width=20 * dx, source_type="ring")
@@ -83,7 +84,7 @@ def single_600_o8(nt: int = 3000, K: int = 300, n_ref: int = 2) -> Workload:
                                  radial_scale=9e8 * s * s)
     rec = interior_points(cfg, 40, seed=3, margin_frac=0.2)
     ref = interior_points(cfg, n_ref, seed=13, margin_frac=0.3)
-    return Workload("single_600_o8", cfg, mu, rho, ref, rec, spec, sd)
+    return Workload("single_600_o8" if nx == 600 else f"single_{nx}_o8", cfg, mu, rho, ref, rec, spec, sd)
 
 
 def structure_512(nt: int = 2500) -> Workload:

@@ -118,12 +118,12 @@ fd2d_status fd2d_ctx_synchronize(fd2d_ctx* ctx);
  * multiple of 128; 0 = as many as fit in 4 GiB).  Smaller chunks use less
  * memory at the cost of more, smaller contractions. */
 fd2d_status fd2d_ctx_set_chunks(fd2d_ctx* ctx, int32_t max_snapshots, int32_t max_injection_planes);
-/* Tile rows of the FP32 step kernel (tiles are 32 points wide): 16 or 32 to
- * force a shape; FD2D_TILE_ROWS_AUTO (0, default) to time both once per
- * context for each grid, FD order and lane count when the stream is idle and
- * keep the faster (the size rule otherwise); FD2D_TILE_ROWS_RULE (-1) for the
- * size rule only (32 rows when the grid has at least four 32-row tiles per SM,
- * else 16).  The environment variable FD2D_TILE_ROWS forces a shape for
+/* Tile rows of the FP32 step kernel (tiles are 32 points wide): 16, 32 or 40
+ * to force a shape; FD2D_TILE_ROWS_AUTO (0, default) to time every shape once
+ * per context for each grid, FD order and lane count when the stream is idle
+ * and keep the fastest (the size rule otherwise); FD2D_TILE_ROWS_RULE (-1) for
+ * the size rule only (fewest waves of resident CTAs, the shortest tiles among
+ * equals).  The environment variable FD2D_TILE_ROWS forces a shape for
  * contexts left at 0. */
 #define FD2D_TILE_ROWS_AUTO 0
 #define FD2D_TILE_ROWS_RULE (-1)
