@@ -858,9 +858,10 @@ int step_ctas(int R, int tz) {
 // Forced by fd2d_ctx_set_tile_rows (or FD2D_TILE_ROWS).  Otherwise, when the
 // context's stream is idle and no other lane group of a batch runs beside this
 // one, every shape is timed once per context on this run's freshly zeroed
-// fields -- Green-function steps with no sources, receivers or snapshots --
-// and the fastest is kept for later runs of the same grid, order and lane
-// count if it beats the size rule's shape by more than 1 %.  When timing would
+// fields -- steps of the run's kind (with or without the displacement u) with
+// no sources, receivers or snapshots -- and the fastest is kept for later runs
+// of the same grid, order, lane count and kind if it beats the size rule's
+// shape by more than 1 %.  When timing would
 // stall queued or concurrent work, or during a stream capture, the size rule
 // decides: the fewest waves of CTAs (tiles over resident CTAs per SM x SMs),
 // the shortest tiles among equals.  The step time is set by the waves: on
@@ -877,8 +878,9 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
       r.tz = forced;
       return FD2D_OK;
     }
+  const bool with_u = r.u[0] != nullptr;
   Sig key;
-  key.add(r.G.nx); key.add(r.G.nz); key.add(r.R); key.add(r.S);
+  key.add(r.G.nx); key.add(r.G.nz); key.add(r.R); key.add(r.S); key.add((int)with_u);
   auto it = ctx->tile_choice.find(key.h);
   if (it != ctx->tile_choice.end()) {
     r.tz = it->second;
@@ -917,6 +919,7 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
     if ((st = set_tiling(ctx, r)) != FD2D_OK) break;
     Step32 s{};
     s.inj_plane = -1;
+    s.has_u = with_u;
     s.src_xy = r.src_xy;
     s.rec_xy = r.rec_xy;
     for (int n = 0; n < WARM && st == FD2D_OK; ++n) st = launch_step(ctx, r, n & 1, s);
@@ -938,6 +941,7 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
     FD2D_CUDA(ctx, cudaMemsetAsync(r.v[q], 0, bytes, ctx->stream));
     FD2D_CUDA(ctx, cudaMemsetAsync(r.sxy[q], 0, bytes, ctx->stream));
     FD2D_CUDA(ctx, cudaMemsetAsync(r.szy[q], 0, bytes, ctx->stream));
+    if (with_u) FD2D_CUDA(ctx, cudaMemsetAsync(r.u[q], 0, bytes, ctx->stream));
   }
   int best = 0, ri = 0;
   for (int c = 0; c < N_TILE_ROWS; ++c) {
