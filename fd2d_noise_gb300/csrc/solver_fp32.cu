@@ -56,7 +56,16 @@ struct Grid32 {
   float c[4];
   float inv_dx, inv_dz, dt;
   int* err;       // device error flag (bounded waits)
+  // tiles blockIdx.x in [t1x0, t1x1], blockIdx.y in [t1z0, t1z1] have taper == 1
+  // exactly on their whole halo box: they skip its load and the multiply
+  int t1x0, t1x1, t1z0, t1z1;
 };
+
+// blockIdx (x, y) in the all-ones taper rectangle of G
+__device__ __forceinline__ bool taper_is_one(const Grid32& G) {
+  return (int)blockIdx.x >= G.t1x0 && (int)blockIdx.x <= G.t1x1 && (int)blockIdx.y >= G.t1z0 &&
+         (int)blockIdx.y <= G.t1z1;
+}
 
 // Shared-memory layout of one tile (floats, regions 128-byte aligned); the
 // displacement (HU) and injection (HI) regions exist only in the variants
@@ -138,12 +147,13 @@ __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, c
   tile_coords<R, TZ>(G, t, x0, z0, lane);
   const int bz0 = z0 - R + 1;
   if (coeffs) {
-    uint32_t bytes = 4u * (T::BH * T::SXWa + T::SZH * T::BWa + 3 * T::BH * T::BWa + TZ * TX);
+    const bool t1 = taper_is_one(G);
+    uint32_t bytes = 4u * (T::BH * T::SXWa + T::SZH * T::BWa + (t1 ? 2 : 3) * T::BH * T::BWa + TZ * TX);
     if (HU) bytes += 4u * TZ * TX;
     if (T::INJ_SMEM) bytes += 4u * T::BH * T::BWa;
     mbar_expect_tx(bar, bytes);
     tma_load_3d(buf + T::O_B, &M.b, x0 - 4, bz0, lane, bar);
-    tma_load_3d(buf + T::O_T, &M.taper, x0 - 4, bz0, lane, bar);
+    if (!t1) tma_load_3d(buf + T::O_T, &M.taper, x0 - 4, bz0, lane, bar);
     tma_load_3d(buf + T::O_MU, &M.dtmu, x0, z0, lane, bar);
   }
   if (fields) {
@@ -251,6 +261,7 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
     const float* s_v = buf + T::O_V;
     const float* s_b = buf + T::O_B;
     const float* s_t = buf + T::O_T;
+    const bool t1 = taper_is_one(G);
     const float* s_i = buf + T::O_I;
     const float* s_mu = buf + T::O_MU;
     const float* s_u = buf + T::O_U;
@@ -340,7 +351,8 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
           // (fewer live registers)
           const float4 v4 = *reinterpret_cast<const float4*>(s_v + rr * W + c0);
           const float4 b4 = *reinterpret_cast<const float4*>(s_b + rr * W + c0);
-          const float4 t4 = *reinterpret_cast<const float4*>(s_t + rr * W + c0);
+          const float4 t4 = t1 ? make_float4(1.f, 1.f, 1.f, 1.f)
+                               : *reinterpret_cast<const float4*>(s_t + rr * W + c0);
           float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
           if (T::INJ_SMEM) {
             i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
@@ -366,7 +378,8 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             const float ds = inj ? __fadd_rn(dsv[e], ii[e]) : dsv[e];
-            out[e] = __fmul_rn(__fmaf_rn(ds, bb[e], vv[e]), tt[e]);
+            // (a taper of exactly 1 leaves the product unchanged: skipped)
+            out[e] = t1 ? __fmaf_rn(ds, bb[e], vv[e]) : __fmul_rn(__fmaf_rn(ds, bb[e], vv[e]), tt[e]);
           }
           *reinterpret_cast<float4*>(s_vn + rr * W + c0) = make_float4(out[0], out[1], out[2], out[3]);
         }
@@ -654,6 +667,7 @@ struct Run {
   dim3 sgrid, pgrid, pblock{32, 8};
   int R = 2;
   int tz = 32;  // tile rows of the step kernel (TILE_ROWS)
+  int t1[N_TILE_ROWS][4] = {};  // per tile shape: all-ones taper tile range (Grid32::t1x0..)
   const float* inj_planes = nullptr;  // injection planes (set_inj_map)
   int2* rec_xy = nullptr;
   int2* src_xy = nullptr;
@@ -820,11 +834,51 @@ void build_tile_receivers(int nx, int nz, int TZ, const SolveArgs* a, int S, std
   build_tile_receivers_idx(nx, nz, TZ, lanes, table, ent);
 }
 
+// Per tile shape, the range of tiles whose halo box (the 40-wide, BH-row box
+// of the dt/rho and taper loads) lies inside the grid with an FP32 taper of
+// exactly 1; the taper is separable, so these tiles form a rectangle (an empty
+// range if not).
+void taper_ones(const std::vector<double>& ab, int nx, int nz, int R, int out[N_TILE_ROWS][4]) {
+  const size_t W = (size_t)nx + 1;
+  std::vector<int> pre(W * (nz + 1), 0);  // prefix counts of taper != 1
+  for (int j = 0; j < nz; ++j)
+    for (int i = 0; i < nx; ++i)
+      pre[(j + 1) * W + i + 1] = ((float)ab[i + (size_t)nx * j] != 1.0f) + pre[j * W + i + 1] +
+                                 pre[(j + 1) * W + i] - pre[j * W + i];
+  auto bad = [&](int x0, int x1, int z0, int z1) {  // inclusive ranges
+    return pre[(z1 + 1) * W + x1 + 1] - pre[z0 * W + x1 + 1] - pre[(z1 + 1) * W + x0] + pre[z0 * W + x0];
+  };
+  for (int c = 0; c < N_TILE_ROWS; ++c) {
+    const int tz = TILE_ROWS[c], BH = tz + 2 * R - 1;
+    const int ntx = (nx + TX - 1) / TX, ntz = (nz + tz - 1) / tz;
+    std::vector<char> one((size_t)ntx * ntz, 0);
+    int bx0 = ntx, bx1 = -1, bz0 = ntz, bz1 = -1;
+    for (int b = 0; b < ntz; ++b)
+      for (int a = 0; a < ntx; ++a) {
+        const int x0 = a * TX - 4, x1 = a * TX + TX + 3, z0 = b * tz - R + 1, z1 = z0 + BH - 1;
+        if (x0 < 0 || x1 > nx - 1 || z0 < 0 || z1 > nz - 1 || bad(x0, x1, z0, z1)) continue;
+        one[(size_t)b * ntx + a] = 1;
+        bx0 = std::min(bx0, a); bx1 = std::max(bx1, a);
+        bz0 = std::min(bz0, b); bz1 = std::max(bz1, b);
+      }
+    bool rect = bx1 >= bx0;
+    for (int b = bz0; rect && b <= bz1; ++b)
+      for (int a = bx0; rect && a <= bx1; ++a) rect = one[(size_t)b * ntx + a];
+    const int e[4] = {1, 0, 1, 0};
+    const int f[4] = {bx0, bx1, bz0, bz1};
+    for (int k = 0; k < 4; ++k) out[c][k] = rect ? f[k] : e[k];
+  }
+}
+
 // Step grid and tensor maps of the run's tile rows r.tz.
 fd2d_status set_tiling(fd2d_ctx* ctx, Run& r) {
   r.G.ntx = (r.G.nx + TX - 1) / TX;
   r.G.ntz = (r.G.nz + r.tz - 1) / r.tz;
   r.sgrid = dim3(r.G.ntx, r.G.ntz, r.S);
+  for (int c = 0; c < N_TILE_ROWS; ++c)
+    if (TILE_ROWS[c] == r.tz) {
+      r.G.t1x0 = r.t1[c][0]; r.G.t1x1 = r.t1[c][1]; r.G.t1z0 = r.t1[c][2]; r.G.t1z1 = r.t1[c][3];
+    }
   return make_maps(ctx, r);
 }
 
@@ -1014,6 +1068,7 @@ fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S
   FD2D_TRY(upload(ctx, "f32.rec", xy(true), &r.rec_xy));
   FD2D_TRY(upload(ctx, "f32.src", xy(false), &r.src_xy));
   r.pgrid = dim3((nx + 31) / 32, (nz + 7) / 8);
+  taper_ones(*g.absbound, nx, nz, r.R, r.t1);
   FD2D_TRY(step_attributes(ctx));
   FD2D_TRY(contract_prepare(ctx));
   FD2D_TRY(tune_tile_rows(ctx, r));
@@ -1721,6 +1776,7 @@ extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg,
     r.u[q] = nullptr;
   }
   r.tz = 32;  // no timing here: the allocation-free path keeps one shape
+  r.G.t1x0 = 1; r.G.t1x1 = 0; r.G.t1z0 = 1; r.G.t1z1 = 0;  // taper loaded on every tile
   r.G.ntx = (nx + TX - 1) / TX;
   r.G.ntz = (nz + r.tz - 1) / r.tz;
   r.sgrid = dim3(r.G.ntx, r.G.ntz, 1);
