@@ -34,6 +34,7 @@ EXPORTED = [
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
     "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch", "fd2d_ctx_release", "fd2d_ctx_workspace_bytes",
     "fd2d_gaussblur2d", "fd2d_ctx_set_chunks", "fd2d_ctx_set_tile_rows", "fd2d_ctx_last_tile_rows",
+    "fd2d_ctx_set_shared_gpu",
 ]
 TILE_ROWS_AUTO = 0
 TILE_ROWS_RULE = -1
@@ -92,6 +93,7 @@ def load(path: str = LIB_PATH):
         L.fd2d_ctx_last_batch.argtypes = [_vp, ctypes.POINTER(ctypes.c_int32), _i32]
         L.fd2d_ctx_last_batch.restype = _i32
         L.fd2d_ctx_set_tile_rows.argtypes = [_vp, _i32]
+        L.fd2d_ctx_set_shared_gpu.argtypes = [_vp, _i32]
         L.fd2d_ctx_last_tile_rows.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.restype = _i64
@@ -187,6 +189,11 @@ class Context:
         """Step-kernel tile rows: 16 or 32 forced, TILE_ROWS_AUTO (0) timed per
         grid when the stream is idle, TILE_ROWS_RULE (-1) by grid size only."""
         check(self.L.fd2d_ctx_set_tile_rows(self.h, int(rows)), self.h)
+
+    def set_shared_gpu(self, shared: bool):
+        """Other work shares the GPU: no programmatic early launch of steps,
+        tile shapes by the size rule."""
+        check(self.L.fd2d_ctx_set_shared_gpu(self.h, 1 if shared else 0), self.h)
 
     def last_tile_rows(self) -> int:
         return int(self.L.fd2d_ctx_last_tile_rows(self.h))

@@ -124,6 +124,7 @@ struct fd2d_ctx {
   int32_t last_tile_rows = 0;  // tile rows of the last FP32 time loop set up
   std::map<uint64_t, int> tile_choice;  // tuned tile rows by (grid, order, lanes)
   int32_t concurrent_groups = 0;        // lane groups a batch runs side by side (set while planning)
+  int32_t shared_gpu = 0;               // other work shares the GPU (fd2d_ctx_set_shared_gpu)
   std::vector<cudaStream_t> side_streams;
   std::vector<cudaEvent_t> fork_events;
 };

@@ -848,6 +848,12 @@ extern "C" fd2d_status fd2d_ctx_set_tile_rows(fd2d_ctx* ctx, int32_t rows) {
 
 extern "C" int32_t fd2d_ctx_last_tile_rows(const fd2d_ctx* ctx) { return ctx ? ctx->last_tile_rows : 0; }
 
+extern "C" fd2d_status fd2d_ctx_set_shared_gpu(fd2d_ctx* ctx, int32_t shared) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  ctx->shared_gpu = shared ? 1 : 0;
+  return FD2D_OK;
+}
+
 extern "C" fd2d_status fd2d_ctx_set_memory_budget(fd2d_ctx* ctx, int64_t bytes) {
   if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
   if (bytes < 0) return set_error(ctx, FD2D_ERR_ARG, "negative memory budget");

@@ -667,6 +667,11 @@ struct Run {
   dim3 sgrid, pgrid, pblock{32, 8};
   int R = 2;
   int tz = 32;  // tile rows of the step kernel (TILE_ROWS)
+  // Programmatic dependent launch of the steps: on when the solve has the GPU
+  // to itself.  Beside other work (lane groups of a batch in parallel graph
+  // branches, serving slots) an early-launched step would park CTAs that wait
+  // for their predecessor in SM slots the other solves could use.
+  bool pdl = true;
   int t1[N_TILE_ROWS][4] = {};  // per tile shape: all-ones taper tile range (Grid32::t1x0..)
   const float* inj_planes = nullptr;  // injection planes (set_inj_map)
   int2* rec_xy = nullptr;
@@ -694,7 +699,7 @@ void launch_step_t(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = r.pdl ? 1 : 0;
   cudaLaunchKernelEx(&cfg, k32_step<R, HU, HI, TZ>, r.G, r.maps[par], s);
 }
 
@@ -953,7 +958,8 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
   }
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   FD2D_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
-  bool idle = cs == cudaStreamCaptureStatusNone && ctx->concurrent_groups <= 1 && forced != FD2D_TILE_ROWS_RULE;
+  bool idle = cs == cudaStreamCaptureStatusNone && ctx->concurrent_groups <= 1 && !ctx->shared_gpu &&
+              forced != FD2D_TILE_ROWS_RULE;
   if (idle) {
     idle = cudaStreamQuery(ctx->stream) == cudaSuccess;
     cudaGetLastError();  // a busy stream answers cudaErrorNotReady
@@ -1068,6 +1074,7 @@ fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S
   FD2D_TRY(upload(ctx, "f32.rec", xy(true), &r.rec_xy));
   FD2D_TRY(upload(ctx, "f32.src", xy(false), &r.src_xy));
   r.pgrid = dim3((nx + 31) / 32, (nz + 7) / 8);
+  r.pdl = ctx->concurrent_groups <= 1 && !ctx->shared_gpu;
   taper_ones(*g.absbound, nx, nz, r.R, r.t1);
   FD2D_TRY(step_attributes(ctx));
   FD2D_TRY(contract_prepare(ctx));
@@ -1301,7 +1308,7 @@ void sig_run(Sig& sg, const Run& r) {
   for (int q = 0; q < 2; ++q) { sg.add(r.v[q]); sg.add(r.sxy[q]); sg.add(r.szy[q]); sg.add(r.u[q]); }
   sg.bytes(r.maps, sizeof(r.maps));
   sg.add(r.sgrid.x); sg.add(r.sgrid.y); sg.add(r.sgrid.z); sg.add(r.pgrid.x); sg.add(r.pgrid.y);
-  sg.add(r.R); sg.add(r.tz); sg.add(r.inj_planes); sg.add(r.rec_xy); sg.add(r.src_xy); sg.add(r.np); sg.add(r.ps);
+  sg.add(r.R); sg.add(r.tz); sg.add((int)r.pdl); sg.add(r.inj_planes); sg.add(r.rec_xy); sg.add(r.src_xy); sg.add(r.np); sg.add(r.ps);
 }
 
 void sig_args(Sig& sg, const Geometry& g, const SolveArgs& a) {

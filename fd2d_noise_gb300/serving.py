@@ -233,9 +233,9 @@ class Server:
             from . import _lib, solvers
             from .solvers import _prec
             ctx = _lib.Context(self.device, _prec(self.precision))
-            # slots share the GPU: pick tile shapes by the size rule rather than
-            # by timing trial steps, which would wait for this slot's queue
-            ctx.set_tile_rows(_lib.TILE_ROWS_RULE)
+            # slots share the GPU: steps without programmatic early launch and
+            # tile shapes by the size rule (no timed trials on a busy queue)
+            ctx.set_shared_gpu(True)
             bind = solvers.bound_context(ctx)
             bind.__enter__()
         try:

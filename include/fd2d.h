@@ -130,6 +130,13 @@ fd2d_status fd2d_ctx_set_chunks(fd2d_ctx* ctx, int32_t max_snapshots, int32_t ma
 fd2d_status fd2d_ctx_set_tile_rows(fd2d_ctx* ctx, int32_t rows);
 /* Tile rows used by the last FP32 time loop this context set up (0: none yet). */
 int32_t fd2d_ctx_last_tile_rows(const fd2d_ctx* ctx);
+/* Declare that other work (other contexts, processes or streams) runs on the
+ * GPU beside this context's solves (1) or not (0, default).  Shared: time steps
+ * are launched without programmatic early launch (a waiting step would hold
+ * SM slots the other work could use) and tile shapes follow the size rule
+ * (no timed trials).  Lane groups of one fd2d_correlation_batch call are
+ * treated as shared among themselves automatically. */
+fd2d_status fd2d_ctx_set_shared_gpu(fd2d_ctx* ctx, int32_t shared);
 /* Device memory the context keeps between calls (workspace buffers). */
 int64_t fd2d_ctx_workspace_bytes(const fd2d_ctx* ctx);
 /* Wait for the stream, then free the workspace and the cached CUDA graphs;
