@@ -373,7 +373,22 @@ fd2d_status contract(fd2d_ctx* ctx, cudaStream_t stream, const ContractArgs& a) 
   if (tiles > 0x7fffffff) return set_error(ctx, FD2D_ERR_SHAPE, "contraction too large for one launch");
   const int grid = (int)std::min<int64_t>(tiles, std::max(ctx->sm_count, 1));
   const int t0 = timer_begin(ctx, stream);
-  k_contract_tc<<<grid, NTHREADS_P, SMEM_BYTES, stream>>>(a, ntn, (int)tiles, ctx->d_err);
+  // Highest scheduling priority: the persistent grid needs a whole SM per CTA,
+  // and beside other solves' step kernels (parallel branches of a batch) an SM
+  // only frees up if its CTAs are preferred when slots drain.
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(NTHREADS_P);
+  cfg.dynamicSmemBytes = SMEM_BYTES;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = prio_greatest;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_contract_tc, a, ntn, (int)tiles, ctx->d_err);
   timer_end(ctx, stream, t0, FD2D_TIMER_CONTRACT, (int64_t)a.M * a.N * a.Kd);
   return after_launch(ctx, "k_contract_tc");
 }
