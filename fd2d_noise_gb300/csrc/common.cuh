@@ -107,6 +107,7 @@ struct fd2d_ctx {
   std::vector<TimerRec> cap_recs;
   struct GraphEntry {
     uint64_t key = 0;
+    uint64_t seen = 0;  // key of the last run launched eagerly (not captured)
     cudaGraphExec_t exec = nullptr;
     std::vector<cudaEvent_t> ev;
     std::vector<TimerRec> recs;
@@ -172,15 +173,16 @@ struct Sig {
 // captured again and the executable graph updated or re-instantiated.
 template <typename F>
 fd2d_status run_captured(fd2d_ctx* ctx, const char* name, uint64_t key, F&& body);
-fd2d_status graph_begin(fd2d_ctx* ctx, const char* name, uint64_t key, bool* replayed);
+fd2d_status graph_begin(fd2d_ctx* ctx, const char* name, uint64_t key, bool* replayed, bool* eager);
 fd2d_status graph_end(fd2d_ctx* ctx, const char* name, uint64_t key, fd2d_status body_status);
 
 template <typename F>
 fd2d_status run_captured(fd2d_ctx* ctx, const char* name, uint64_t key, F&& body) {
-  bool replayed = false;
-  FD2D_TRY(graph_begin(ctx, name, key, &replayed));
+  bool replayed = false, eager = false;
+  FD2D_TRY(graph_begin(ctx, name, key, &replayed, &eager));
   if (replayed) return FD2D_OK;
   fd2d_status s = body();
+  if (eager) return s;
   return graph_end(ctx, name, key, s);
 }
 

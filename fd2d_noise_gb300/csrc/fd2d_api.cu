@@ -166,13 +166,27 @@ static fd2d_status launch_graph(fd2d_ctx* ctx, fd2d_ctx::GraphEntry& g) {
 
 static thread_local int64_t g_launches_at_capture = 0;
 
-fd2d_status graph_begin(fd2d_ctx* ctx, const char* name, uint64_t key, bool* replayed) {
+fd2d_status graph_begin(fd2d_ctx* ctx, const char* name, uint64_t key, bool* replayed, bool* eager) {
   *replayed = false;
+  *eager = false;
   key ^= ctx->timing ? 0x9e3779b97f4a7c15ull : 0;
   fd2d_ctx::GraphEntry* g = find_graph(ctx, name);
   if (g && g->exec && g->key == key) {
     *replayed = true;
     return launch_graph(ctx, *g);
+  }
+  // A loop seen for the first time is launched eagerly: capture and
+  // instantiation cost more host time than one run (serving requests of ever
+  // new shapes run once each).  The second run with the same key captures the
+  // graph, later ones replay it.
+  if (!g) {
+    ctx->graphs.emplace_back(name, fd2d_ctx::GraphEntry());
+    g = &ctx->graphs.back().second;
+  }
+  if (g->seen != key) {
+    g->seen = key;
+    *eager = true;
+    return FD2D_OK;
   }
   ctx->cap_ev.clear();
   ctx->cap_recs.clear();
@@ -262,8 +276,8 @@ fd2d_status run_parallel(fd2d_ctx* ctx, const char* name, uint64_t key, std::vec
     FD2D_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     ctx->fork_events.push_back(e);
   }
-  bool replayed = false;
-  FD2D_TRY(graph_begin(ctx, name, sg.h, &replayed));
+  bool replayed = false, eager = false;
+  FD2D_TRY(graph_begin(ctx, name, sg.h, &replayed, &eager));
   if (replayed) return FD2D_OK;
   cudaStream_t main = ctx->stream;
   fd2d_status st = FD2D_OK;
@@ -278,6 +292,7 @@ fd2d_status run_parallel(fd2d_ctx* ctx, const char* name, uint64_t key, std::vec
     cudaStreamWaitEvent(main, ctx->fork_events[j + 1], 0);
   }
   ctx->stream = main;
+  if (eager) return st;
   return graph_end(ctx, name, sg.h, st);
 }
 

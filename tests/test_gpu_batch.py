@@ -56,7 +56,7 @@ def test_batch_matches_single_solves(fd2d_lib, prec, budget):
                        src=to_device(j["src"], np.float64), rec=to_device(j["rec"], np.float64),
                        nr=j["rec"].shape[0],
                        out=torch.zeros(j["rec"].shape[0] * c.ntc, dtype=torch.float64, device="cuda")))
-    for rep in range(2):  # the second call replays the cached graphs
+    for rep in range(3):  # launched eagerly, then captured, then replayed
         sess.correlation_batch(dj)
         sess.ctx.synchronize()
         groups = sess.ctx.last_batch()
