@@ -192,6 +192,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=40,
                     help="requests of the serving measurement (0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="mean Poisson arrival rate [1/s]")
+    ap.add_argument("--serve-slots", type=int, default=8, help="concurrent solves of the serving loop")
     ap.add_argument("--no-hbm-probe", action="store_true",
                     help="skip the stencil roofline on a grid whose fields exceed L2")
     ap.add_argument("--probe-nt", type=int, default=200, help="nt of the large-grid stencil probe")
@@ -486,7 +487,7 @@ def serving_run(args, dev):
     reqs = [make_request(kind, nx, nt, n_ref=n_ref, seed=sd) for (_, kind, nx, nt, n_ref, sd) in mix]
     free, _ = torch.cuda.mem_get_info(dev)
     budget = int(free * 0.6)
-    with Server(budget_bytes=budget, slots=4, device=dev) as srv:
+    with Server(budget_bytes=budget, slots=args.serve_slots, device=dev) as srv:
         # warm-up: one request of each kind alone (graph capture, tables)
         seen = set()
         for r in reqs:
@@ -509,7 +510,7 @@ def serving_run(args, dev):
     kinds = {}
     for (kind, *_rest) in srv.log:
         kinds[kind] = kinds.get(kind, 0) + 1
-    st.update({"offered_rate_req_s": args.serve_rate, "slots": 4, "budget_bytes": budget, "mix": kinds,
+    st.update({"offered_rate_req_s": args.serve_rate, "slots": args.serve_slots, "budget_bytes": budget, "mix": kinds,
                "workload": "synthetic Poisson stream, grids 256-384, nt 800-1600, 1-4 stations, FP32 form"})
     return st
 
