@@ -182,7 +182,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="single_600_o8")
-    ap.add_argument("--cpu-nt", type=int, default=120)
+    ap.add_argument("--cpu-nt", type=int, default=400,
+                    help="nt of the CPU oracle sample (one station; about 10 s on 16 cores)")
     ap.add_argument("--nt", type=int, default=0, help="override the workload's nt (profiling runs)")
     ap.add_argument("--stations", type=int, default=0, help="override the number of reference stations")
     ap.add_argument("--grid", type=int, default=0, help="square grid size of single_600_o8 (profiling runs)")
