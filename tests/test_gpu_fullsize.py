@@ -1,0 +1,126 @@
+"""Full-size checks on the benchmark workload: 600x600, order 8, dt 0.05 s,
+nt 3000 (5999 correlation steps), 300 frequencies, two reference stations,
+40 receivers, random media, ring noise source.
+
+The oracle needs minutes per station at this size, so these tests use
+properties that hold at any size:
+
+* the batched FP32 / split-TF32 correlations agree with the plain FP64 GPU
+  form of each station to <= 1e-4 relative L2 (the FP32 bound); the FP64 form
+  itself is pinned to the oracle at <= 1e-10 by the parity tests;
+* snapshots and receiver traces are consistent bit for bit: snapshot i, taken
+  before the update of step n, holds single(seismograms(:, n-1)) at the
+  receiver nodes that the oracle's nearest-node rule picks (the relation is
+  pinned on the oracle in test_schedules.py), in both precisions;
+* the correlations are linear in the noise-source distribution:
+  C(a) + C(b) = C(a + b) to <= 1e-4 relative L2 in FP32.
+"""
+import numpy as np
+import pytest
+
+from tests.test_schedules import (assert_snapshots_match_traces, correlation_snapshot_steps,
+                                  green_snapshot_steps)
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def W():
+    from fd2d_noise_gb300.workloads import single_600_o8
+    w = single_600_o8()
+    # 50-step snapshot spacing: 60 Green and 119 correlation snapshots
+    w.cfg = w.cfg.replace(fw_nth=50)
+    return w
+
+
+@pytest.fixture(scope="module")
+def dev_inputs(fd2d_lib, W):
+    from fd2d_noise_gb300.device import to_device
+    d = {k: to_device(getattr(W, k), np.float64) for k in ("mu", "rho", "spectrum", "source_dist", "receivers")}
+    d["refs"] = [to_device(W.ref_stations[i:i + 1], np.float64) for i in range(W.ref_stations.shape[0])]
+    return d
+
+
+def _batch(sess, W, d, source_dists):
+    """One fd2d_correlation_batch call: station i with source_dists[i]."""
+    nr = W.receivers.shape[0]
+    outs = [sess.zeros(nr * W.cfg.ntc, sess.torch.float64) for _ in source_dists]
+    jobs = [dict(cfg=W.cfg, mu=d["mu"], rho=d["rho"], spectrum=d["spectrum"], source_dist=sd,
+                 src=src, rec=d["receivers"], nr=nr, out=o) for (src, sd), o in zip(source_dists, outs)]
+    sess.correlation_batch(jobs)
+    sess.torch.cuda.synchronize()
+    return [o.cpu().numpy().reshape(nr, W.cfg.ntc, order="F") for o in outs]
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_batched_fp32_matches_plain_fp64(W, dev_inputs):
+    from fd2d_noise_gb300.device import DeviceSession
+    d = dev_inputs
+    cfg, nr = W.cfg, W.receivers.shape[0]
+    s32 = DeviceSession(cfg, 0, "fp32")
+    c32 = _batch(s32, W, d, [(src, d["source_dist"]) for src in d["refs"]])
+    s32.ctx.close()
+    s64 = DeviceSession(cfg, 0, "fp64")
+    G_re, G_im, _, seis = s64.green_outputs(nr)
+    for i, src in enumerate(d["refs"]):
+        out = s64.zeros(nr * cfg.ntc, s64.torch.float64)
+        s64.forward1_green(d["mu"], d["rho"], src, 1, d["receivers"], nr, G_re, G_im, seis)
+        s64.forward2_correlation(d["mu"], d["rho"], G_re, G_im, d["spectrum"], 1, d["source_dist"], 1,
+                                 d["receivers"], nr, out)
+        s64.torch.cuda.synchronize()
+        c64 = out.cpu().numpy().reshape(nr, cfg.ntc, order="F")
+        assert np.abs(c64).max() > 0
+        err = _rel(c32[i], c64)
+        assert err <= FP32_TOL, (i, err)
+    s64.ctx.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_snapshots_hold_receiver_traces(W, dev_inputs, oracle, prec):
+    from fd2d_noise_gb300.config import n_fw_corr
+    from fd2d_noise_gb300.device import DeviceSession
+    d = dev_inputs
+    cfg, nr = W.cfg, W.receivers.shape[0]
+    ix, iz = oracle.nearest_indices(cfg, W.receivers)
+    sess = DeviceSession(cfg, 0, prec)
+    t = sess.torch
+    G_re, G_im, G_out, seis = sess.green_outputs(nr, mode=1)
+    sess.forward1_green(d["mu"], d["rho"], d["refs"][0], 1, d["receivers"], nr, G_re, G_im, seis,
+                        mode=1, G_out=G_out)
+    C_out = sess.zeros(cfg.npts * n_fw_corr(cfg), t.float32)
+    corr = sess.zeros(nr * cfg.ntc, t.float64)
+    sess.forward2_correlation(d["mu"], d["rho"], G_re, G_im, d["spectrum"], 1, d["source_dist"], 1,
+                              d["receivers"], nr, corr, mode=1, C_out=C_out)
+    t.cuda.synchronize()
+    shape = lambda n: (cfg.nx, cfg.nz, n)  # noqa: E731
+    g_steps, c_steps = green_snapshot_steps(cfg), correlation_snapshot_steps(cfg)
+    G_snap = G_out.cpu().numpy().reshape(shape(len(g_steps)), order="F")
+    C_snap = C_out.cpu().numpy().reshape(shape(len(c_steps)), order="F")
+    seis_h = seis.cpu().numpy().reshape(nr, cfg.nt, order="F")
+    corr_h = corr.cpu().numpy().reshape(nr, cfg.ntc, order="F")
+    assert np.abs(seis_h).max() > 0 and np.abs(corr_h).max() > 0
+    assert_snapshots_match_traces(G_snap, seis_h, ix, iz, g_steps)
+    assert_snapshots_match_traces(C_snap, corr_h, ix, iz, c_steps)
+    sess.ctx.close()
+
+
+def test_correlations_linear_in_source_distribution(W, dev_inputs):
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+    d = dev_inputs
+    sd = W.source_dist
+    x = np.arange(W.cfg.nx)[:, None, None]
+    sd_a = np.asfortranarray(np.where(x < W.cfg.nx // 2, sd, 0.0))
+    sd_b = np.asfortranarray(sd - sd_a)
+    src = d["refs"][0]
+    sess = DeviceSession(W.cfg, 0, "fp32")
+    ca, cb, cab = _batch(sess, W, d, [(src, to_device(sd_a, np.float64)), (src, to_device(sd_b, np.float64)),
+                                      (src, d["source_dist"])])
+    sess.ctx.close()
+    assert np.abs(ca).max() > 0 and np.abs(cb).max() > 0
+    err = _rel(ca + cb, cab)
+    assert err <= FP32_TOL, err
