@@ -118,7 +118,7 @@ struct fd2d_ctx {
   // fork the jobs' loops into parallel branches of one captured graph
   std::string ws_prefix;
   int64_t mem_budget = 0;  // batch device-memory budget (0: 80 % of free memory)
-  int32_t max_dft_chunk = 0;  // snapshots per DFT contraction (0: 1024, within 2 GiB)
+  int32_t max_dft_chunk = 0;  // snapshots per DFT contraction (0: DFT_CHUNK_DEFAULT, within 2 GiB)
   int32_t max_inj_chunk = 0;  // resident injection planes (0: within 4 GiB)
   std::vector<int32_t> last_lanes;  // lanes of each launch group of the last batch
   int32_t tile_rows = 0;       // step-kernel tile rows: 0 timed per grid, -1 size rule, 16 or 32 forced
@@ -131,6 +131,13 @@ struct fd2d_ctx {
 };
 
 namespace fd2d {
+
+// Snapshots per DFT contraction unless fd2d_ctx_set_chunks says otherwise.  A
+// chunk is summed in two halves, each in FP32 in tensor memory, and the chunks
+// in FP64, so every FP32 sum covers at most 256 snapshots: the FP32 mu kernel
+// of a 512x512, nt 2500 structure-kernel run is then within 1e-4 of the FP64
+// form (1.4e-4 with one FP32 sum over all 500 snapshots).
+constexpr int DFT_CHUNK_DEFAULT = 512;
 
 // Returns a device buffer of at least `bytes` under `name` (grown when needed).
 fd2d_status workspace(fd2d_ctx* ctx, const char* name, size_t bytes, void** out);

@@ -50,6 +50,11 @@ struct ContractArgs {
   // FP32 store: out32[n*ldo + m]
   float* out32 = nullptr;
   int64_t ldo = 0;
+  // 2: the K blocks are summed in two halves, each in its own FP32 tensor-memory
+  // accumulator, and the halves added once in the epilogue (a long DFT loses
+  // less to FP32 rounding of small late terms against a large running sum);
+  // 1: one accumulator.
+  int k_partials = 1;
 };
 
 fd2d_status contract(fd2d_ctx* ctx, cudaStream_t stream, const ContractArgs& a);

@@ -17,6 +17,9 @@
 // k_contract_tc is persistent (one CTA per SM) over 128 x 128 output tiles,
 // with a 3-stage ring of 64 KB stages (A and B blocks, hi and lo) and two TMEM
 // accumulators, so the epilogue of one tile overlaps the main loop of the next.
+// Each accumulator has two halves (all 512 TMEM columns): with k_partials = 2
+// the first half of the K blocks sums into one and the rest into the other,
+// and the epilogue adds the two FP32 partial sums.
 // Every mbarrier wait is bounded in time; a wait that gives up sets the
 // context's error flag, the CTA lets its own copies land (bounded) and frees
 // its TMEM.
@@ -34,7 +37,8 @@ constexpr int A_BYTES = BM * BK * 4;        // 16 KB per split half
 constexpr int B_BYTES = BN * BK * 4;        // 16 KB per split half
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;  // + 1024-byte alignment slack
-constexpr uint32_t TMEM_COLS = BN;
+constexpr uint32_t TMEM_COLS = BN;          // one partial accumulator
+constexpr uint32_t TMEM_ALLOC = 4 * TMEM_COLS;  // 2 accumulators x 2 partials = 512 columns
 
 // Instruction descriptor, kind::tf32: D = F32 (bits 4-5 = 1), A = B = TF32
 // (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
@@ -154,6 +158,9 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nkb = (a.Kd + BK - 1) / BK;
+  // K blocks [0, kb_half) go to partial 0, [kb_half, nkb) to partial 1
+  const bool two = a.k_partials == 2 && nkb > 1;
+  const int kb_half = two ? (nkb + 1) / 2 : nkb;
   unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sbase = smem_u32(smem);
   auto a_hi = [&](int s) { return sbase + s * STAGE_BYTES; };
@@ -175,7 +182,7 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(2 * TMEM_COLS)
+                 "r"(TMEM_ALLOC)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -220,7 +227,7 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
       bool ok = true;
       for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++i) {
         const int acc = i & 1;
-        const uint32_t d = tmem + (uint32_t)(acc * TMEM_COLS);
+        const uint32_t d0 = tmem + (uint32_t)(2 * acc * TMEM_COLS);
         if (!mbar_wait_bounded(&acce_bar[acc], ((i >> 1) & 1) ^ 1)) {
           ok = false;
           break;
@@ -233,11 +240,14 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const bool second = kb >= kb_half;
+          const uint32_t d = second ? d0 + TMEM_COLS : d0;
+          const int kb_first = second ? kb_half : 0;  // first K block of this partial
 #pragma unroll
           for (int kk = 0; kk < BK / 8; ++kk) {
             const uint64_t ah = smem_desc(a_hi(s) + kk * 32), al = smem_desc(a_lo(s) + kk * 32);
             const uint64_t bh = smem_desc(b_hi(s) + kk * 32), bl = smem_desc(b_lo(s) + kk * 32);
-            mma_tf32(d, ah, bh, (kb > 0 || kk > 0) ? 1u : 0u);
+            mma_tf32(d, ah, bh, (kb > kb_first || kk > 0) ? 1u : 0u);
             mma_tf32(d, ah, bl, 1u);
             mma_tf32(d, al, bh, 1u);
           }
@@ -281,7 +291,14 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
       for (int c0 = cbeg; c0 < cbeg + CW; c0 += 32) {
         float v[32];
         // all lanes of the warp take part in tcgen05.ld (sync.aligned)
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TMEM_COLS + c0), v);
+        const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(2 * acc * TMEM_COLS + c0);
+        tmem_ld32(ta, v);
+        if (two) {
+          float w[32];
+          tmem_ld32(ta + TMEM_COLS, w);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = __fadd_rn(v[j], w[j]);
+        }
         if (c0 + 32 == cbeg + CW) {
           // the accumulator is in registers: hand it back to the MMAs
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -308,13 +325,15 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
             for (int j = 0; j < 32; ++j, p += a.ldacc) *p = widen_exact(v[j]);
             continue;
           }
-          // Overwrite: plain stores.  Accumulate: 8 loads in flight per group.
+          // Overwrite: plain stores.  Accumulate: 16 loads in flight per group,
+          // then the stores (the pass is bound by the latency of these loads).
+          constexpr int G = 16;
 #pragma unroll
-          for (int gg = 0; gg < 32; gg += 8) {
-            double* p[8];
-            double old[8];
+          for (int gg = 0; gg < 32; gg += G) {
+            double* p[G];
+            double old[G];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
+            for (int j = 0; j < G; ++j) {
               const int n = n0 + c0 + gg + j;
               p[j] = n >= a.N ? nullptr
                               : (n < a.nsplit ? a.acc0 + (int64_t)n * a.ldacc + q
@@ -322,7 +341,7 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
               old[j] = (p[j] && !a.overwrite) ? *p[j] : 0.0;
             }
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
+            for (int j = 0; j < G; ++j)
               if (p[j]) *p[j] = a.overwrite ? widen_exact(v[gg + j]) : old[j] + widen_exact(v[gg + j]);
           }
         }
@@ -333,7 +352,7 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
   __syncthreads();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TMEM_COLS)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_ALLOC)
                  : "memory");
   }
   if (tid == 0 && fail) set_error_flag(err, 2);

@@ -837,7 +837,7 @@ size_t job_footprint(const Geometry& g, int nr, int n_dist, bool host_inputs) {
   const size_t plane = ps * 4;
   size_t n_dft = 0;
   for (int n = 1; n <= g.nt; ++n) n_dft += ((n + g.nt - 1) % g.fs == 0);
-  const size_t T = std::min<size_t>({n_dft, 1024, ((size_t)2 << 30) / plane});
+  const size_t T = std::min<size_t>({n_dft, (size_t)DFT_CHUNK_DEFAULT, ((size_t)2 << 30) / plane});
   const size_t n_inj = g.ntc / g.fs;
   const size_t chunk = std::min<size_t>(n_inj, ((size_t)4 << 30) / plane);
   // fields and coefficients, snapshot chunk and its split image (x2), FP64

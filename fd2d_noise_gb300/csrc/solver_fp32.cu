@@ -1233,7 +1233,7 @@ fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
   if (n_events == 0) return FD2D_OK;
   const size_t cap = (size_t)2 << 30;  // snapshot chunk <= 2 GiB
   const int64_t sps = r.lanes_ps();
-  const int64_t lim = ctx->max_dft_chunk > 0 ? ctx->max_dft_chunk : 1024;
+  const int64_t lim = ctx->max_dft_chunk > 0 ? ctx->max_dft_chunk : DFT_CHUNK_DEFAULT;
   d.T = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)n_events, lim, (int64_t)(cap / (sps * 4))}));
   // chunks start on K blocks of the coefficient image
   if (d.T < n_events) d.T = std::max(CONTRACT_BK, d.T / CONTRACT_BK * CONTRACT_BK);
@@ -1288,6 +1288,7 @@ fd2d_status dft_flush(fd2d_ctx* ctx, const Run& r, const Geometry& g, Dft& d) {
     c.remap_nx = g.nx;
     c.remap_nz = g.nz;
     c.overwrite = d.done == 0;  // the first chunk defines the spectra
+    c.k_partials = 2;
     FD2D_TRY(contract(ctx, ctx->stream, c));
   }
   d.done += d.filled;

@@ -14,6 +14,10 @@ properties that hold at any size:
   pinned on the oracle in test_schedules.py), in both precisions;
 * the correlations are linear in the noise-source distribution:
   C(a) + C(b) = C(a + b) to <= 1e-4 relative L2 in FP32.
+
+The structure-kernel path is checked the same way at its own full size
+(512x512, nt 2500, snapshots every 5 steps, 200 frequencies, 20 receivers):
+FP32 misfit and mu kernel against the plain FP64 GPU form.
 """
 import numpy as np
 import pytest
@@ -124,3 +128,51 @@ def test_correlations_linear_in_source_distribution(W, dev_inputs):
     assert np.abs(ca).max() > 0 and np.abs(cb).max() > 0
     err = _rel(ca + cb, cab)
     assert err <= FP32_TOL, err
+
+
+def _structure_problem():
+    """512x512, nt 2500, snapshots every 5 steps, 200 frequencies, one reference
+    station in the centre and 20 receivers on a 450 km ring: the surface waves
+    arrive at ~110 s, inside the 100-200 s window of the log-amplitude-ratio
+    measurement (tools/measurement/make_adjoint_sources.m:85-86)."""
+    from fd2d_noise_gb300.config import Config
+    L, nx = 1.0e6, 512
+    dx = L / (nx - 1)
+    cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.2, nt=2500, order=4, n_basis_fct=0, fw_nth=5,
+                 f_sample=np.linspace(0.006, 0.028, 200), freq_samp=5, absorb_width=20 * dx)
+    X, Z = np.meshgrid(np.linspace(0, L, nx), np.linspace(0, L, nx), indexing="ij")
+    mu0 = 4.8e10 * np.ones((nx, nx))
+    ang = np.linspace(0, 2 * np.pi, 20, endpoint=False)
+    arr = np.concatenate([[[0.5e6, 0.5e6]], np.stack([0.5e6 + 0.45e6 * np.cos(ang),
+                                                      0.5e6 + 0.45e6 * np.sin(ang)], axis=1)])
+    p = dict(mu0=mu0, rho=3000.0 * np.ones((nx, nx)),
+             mu_true=mu0 * (1 + 0.05 * np.exp(-((X - 0.7e6) ** 2 + (Z - 0.55e6) ** 2) / 1.0e5 ** 2)),
+             spec=np.exp(-(cfg.f_sample - 0.017) ** 2 / 0.008 ** 2).reshape(-1, 1),
+             sd=np.asfortranarray((1 + 5 * np.exp(-((X - 0.3e6) ** 2 + (Z - 0.7e6) ** 2) / 1.5e5 ** 2))[:, :, None]),
+             ref=arr[:1], arr=arr, t=(-(cfg.nt - 1) + np.arange(cfg.ntc)) * cfg.dt)
+    return cfg, p
+
+
+def test_structure_kernel_fp32_matches_fp64(fd2d_lib):
+    """The structure-kernel workload at full size through
+    eval_objective_and_gradient (Green and correlation with stored wavefields,
+    log-amplitude-ratio adjoint sources, adjoint modes 1 and 0): the FP32
+    correlations, misfit and mu kernel agree with the plain FP64 GPU form to
+    <= 1e-4 relative L2."""
+    from fd2d_noise_gb300.objective import eval_objective_and_gradient
+    cfg, p = _structure_problem()
+
+    def run(mu, c_data, precision, only=False):
+        return eval_objective_and_gradient(mu, p["rho"], p["spec"], p["sd"], p["ref"], p["arr"], c_data, p["t"],
+                                           cfg=cfg, precision=precision, weighting=1.0, only_objective=only,
+                                           type="structure")
+
+    _, _, c_data = run(p["mu_true"], np.zeros((20, cfg.ntc)), "fp64", only=True)
+    j64, g64, c64 = run(p["mu0"], c_data, "fp64")
+    j32, g32, c32 = run(p["mu0"], c_data, "fp32")
+    assert j64 > 0 and np.linalg.norm(g64[:, :, -1]) > 0
+    print(f"structure kernel FP32 vs FP64: correlations {_rel(c32, c64):.3e}, misfit "
+          f"{abs(j32 - j64) / abs(j64):.3e}, mu kernel {_rel(g32[:, :, -1], g64[:, :, -1]):.3e}")
+    assert _rel(c32, c64) <= FP32_TOL
+    assert abs(j32 - j64) <= FP32_TOL * abs(j64), (j32, j64)
+    assert _rel(g32[:, :, -1], g64[:, :, -1]) <= FP32_TOL
