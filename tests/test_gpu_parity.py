@@ -2,7 +2,7 @@
 
 Every call goes through libfd2d's C ABI (host buffers).  Bars: the plain FP64
 form agrees with the oracle to <= 1e-10 relative L2 on every output; the FP32
-form to <= 1e-4 on correlations, kernels and spectra (the benchmark spec's bound) --
+form to <= 1e-4 on correlations, kernels and spectra (the FP32 bound) --
 FP32 wavefield snapshots get 1e-4 as well.  Receiver indices and snapshot
 schedules are exact: the snapshot stacks of the FP64 form equal the oracle's
 single() values except for rare one-ulp rounding-boundary cases.
