@@ -104,7 +104,12 @@ def make_noise_source(source_type: str = "homogeneous", n_basis_fct: int = 0,
     nx, nz = cfg.nx, cfg.nz
     dist = np.ones((nx, nz, n_noise_sources), order="F")
     if source_type == "gaussian":
-        kw = dict(x_c=[1.0e5], z_c=[1.6e5], width=[4e4], magnitude=[6.0])
+        # the reference's two parameter sets, chosen by domain size (make_noise_source.m:13-17,47-60)
+        if cfg.Lx == 2.0e6 or cfg.Lz == 2.0e6:
+            kw = dict(x_c=[0.6e6, 0.5e6, 1.3e6], z_c=[0.8e6, 1.5e6, 1.6e6], width=[1.5e5, 1.5e5, 1.8e5],
+                      magnitude=[6.5, 5.0, 3.0])
+        else:
+            kw = dict(x_c=[1.0e5], z_c=[1.6e5], width=[4e4], magnitude=[6.0])
         kw.update(dist_kw)
         for ns in range(n_noise_sources):
             dist[:, :, ns] = gaussian_blobs(cfg, kw["x_c"][ns:ns + 1], kw["z_c"][ns:ns + 1],

@@ -407,6 +407,11 @@ class Parser:
             elif tok.kind == "op" and tok.val in ("'", ".'"):
                 self.next()
                 e = ("transpose", tok.val, e)
+            elif tok.kind == "op" and tok.val == "." and self.peek(1).kind == "id":
+                # struct field: parsed so that files holding struct code (in
+                # branches the solvers do not take) load; evaluating it fails
+                self.next()
+                e = ("field", e, self.next().val)
             else:
                 return e
 
@@ -881,6 +886,8 @@ BUILTINS: Dict[str, Callable] = {
     "eps": lambda: A(np.finfo(np.float64).eps),
     "log": lambda x: np.asfortranarray(np.log(to_float(A(x)))),
     "cos": lambda x: np.asfortranarray(np.cos(to_float(A(x)))),
+    "atan": lambda x: np.asfortranarray(np.arctan(to_float(A(x)))),
+    "isnan": lambda x: np.asfortranarray(np.isnan(A(x))),
     "fliplr": lambda x: np.asfortranarray(A(x)[:, ::-1]),
     "strcmp": lambda a, b: A(isinstance(a, str) and isinstance(b, str) and a == b),
     "fprintf": lambda *a: [],
@@ -936,6 +943,13 @@ class Interpreter:
                 sh.append(1)
             out = sh[:nargout - 1] + [int(np.prod(sh[nargout - 1:]))]
             return [A(float(d)) for d in out]
+        if name == "find" and nargout == 2 and len(args) == 1:
+            # [row, col] = find(A): 1-based subscripts of the nonzeros, column-major order
+            a = A(args[0])
+            a = a.reshape(a.shape[0], -1, order="F")
+            lin = np.nonzero(a.reshape(-1, order="F") != 0)[0]
+            r, c = lin % a.shape[0] + 1.0, lin // a.shape[0] + 1.0
+            return [r.reshape(-1, 1), c.reshape(-1, 1)]
         if name in BUILTINS:
             r = BUILTINS[name](*args)
             return r if isinstance(r, list) else [r]
@@ -943,7 +957,7 @@ class Interpreter:
 
     def run_function(self, fn, args, nargout):
         _, name, params, outs, body = fn
-        env: Dict[str, Any] = {}
+        env: Dict[str, Any] = {"nargin": A(float(len(args)))}
         for p, a in zip(params, args):
             if p != "~":
                 env[p] = a
