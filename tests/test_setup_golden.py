@@ -44,5 +44,5 @@ def test_host_grid_matches_reference(name):
     cfg = _cfg(name)
     X, Z, x, z, dx, dz = define_computational_domain(cfg.Lx, cfg.Lz, cfg.nx, cfg.nz)
     assert np.array_equal(x, GOLDEN[f"{name}/x"].ravel()) and np.array_equal(z, GOLDEN[f"{name}/z"].ravel())
-    assert dx == float(GOLDEN[f"{name}/dx"]) and dz == float(GOLDEN[f"{name}/dz"])
+    assert dx == GOLDEN[f"{name}/dx"].ravel()[0] and dz == GOLDEN[f"{name}/dz"].ravel()[0]
     assert X.shape == (cfg.nz, cfg.nx)
