@@ -239,6 +239,12 @@ class Parser:
                 body = self.parse_block(())
                 self.expect("kw", "end")
                 return ("for", var, rng, body)
+            if tok.val == "while":
+                self.next()
+                cond = self.parse_expr()
+                body = self.parse_block(())
+                self.expect("kw", "end")
+                return ("while", cond, body)
             if tok.val == "if":
                 self.next()
                 clauses = []
@@ -408,8 +414,7 @@ class Parser:
                 self.next()
                 e = ("transpose", tok.val, e)
             elif tok.kind == "op" and tok.val == "." and self.peek(1).kind == "id":
-                # struct field: parsed so that files holding struct code (in
-                # branches the solvers do not take) load; evaluating it fails
+                # struct field (scalar structs are dicts)
                 self.next()
                 e = ("field", e, self.next().val)
             else:
@@ -883,6 +888,8 @@ BUILTINS: Dict[str, Callable] = {
     "all": lambda x: A(bool(np.all(A(x) != 0))),
     "numel": lambda x: A(float(A(x).size)),
     "pi": lambda: A(np.pi),
+    "true": lambda: A(1.0),
+    "false": lambda: A(0.0),
     "eps": lambda: A(np.finfo(np.float64).eps),
     "log": lambda x: np.asfortranarray(np.log(to_float(A(x)))),
     "cos": lambda x: np.asfortranarray(np.cos(to_float(A(x)))),
@@ -1003,6 +1010,12 @@ class Interpreter:
                     self.exec_block(s[3], env)
                 except _Break:
                     break
+        elif kind == "while":
+            while truth(self.eval(s[1], env)):
+                try:
+                    self.exec_block(s[2], env)
+                except _Break:
+                    break
         elif kind == "if":
             for cond, body in s[1]:
                 if truth(self.eval(cond, env)):
@@ -1026,6 +1039,23 @@ class Interpreter:
             base = env.get(name)
             subs = [self.eval_sub(a, env, base, d, len(target[2])) for d, a in enumerate(target[2])]
             env[name] = massign_into(base, subs, value)
+            return
+        if target[0] == "field":
+            # s.a.b = v on scalar structs (dicts), created as needed
+            path, t = [], target
+            while t[0] == "field":
+                path.append(t[2])
+                t = t[1]
+            if t[0] != "id":
+                raise MatlabError("unsupported struct assignment target")
+            node = env.get(t[1])
+            if not isinstance(node, dict):
+                node = env[t[1]] = {}
+            for name in reversed(path[1:]):
+                if not isinstance(node.get(name), dict):
+                    node[name] = {}
+                node = node[name]
+            node[path[0]] = value
             return
         raise MatlabError("unsupported assignment target")
 
@@ -1058,6 +1088,11 @@ class Interpreter:
                 return env[name]
             r = self.call(name, [], nargout=max(nargout, 1))
             return r[0] if r else None
+        if kind == "field":
+            v = self.eval(e[1], env)
+            if not isinstance(v, dict) or e[2] not in v:
+                raise MatlabError(f"reference to non-existent field {e[2]}")
+            return v[e[2]]
         if kind == "end":
             base, d, k = self._end_stack[-1]
             a = A(base)

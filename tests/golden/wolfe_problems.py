@@ -1,0 +1,41 @@
+"""Line-search test problems shared by make_golden_wolfe.py and the tests.
+
+TEST INFRASTRUCTURE.  Each case: objective and gradient (numpy, FP64), start
+point, search direction rule and the optlib_wolfe arguments.
+"""
+import numpy as np
+
+
+def rosenbrock(x):
+    x = np.asarray(x, dtype=np.float64).ravel()
+    f = 100.0 * (x[1] - x[0] ** 2) ** 2 + (1.0 - x[0]) ** 2
+    g = np.array([-400.0 * x[0] * (x[1] - x[0] ** 2) - 2.0 * (1.0 - x[0]), 200.0 * (x[1] - x[0] ** 2)])
+    return f, g
+
+
+DIAG = np.array([1.0, 3.0, 10.0, 30.0, 100.0])
+
+
+def quadratic(x):
+    x = np.asarray(x, dtype=np.float64).ravel()
+    return 0.5 * float(np.sum(DIAG * x * x)), DIAG * x
+
+
+# name, function, start, direction ('gradient' or 'newton'), sig0, try_larger_steps
+CASES = [
+    ("rosen_far", rosenbrock, [-1.2, 1.0], "gradient", 1.0, 1),
+    ("rosen_small_step", rosenbrock, [0.5, 0.2], "gradient", 1e-3, 1),
+    ("rosen_no_expand", rosenbrock, [0.5, 0.2], "gradient", 1e-3, 0),
+    ("quad_gradient", quadratic, [1.0, -1.0, 1.0, -1.0, 1.0], "gradient", 0.05, 0),
+    ("quad_gradient_long", quadratic, [1.0, 1.0, 1.0, 1.0, 1.0], "gradient", 0.002, 1),
+    ("quad_newton", quadratic, [1.0, 2.0, 3.0, 4.0, 5.0], "newton", 1.0, 1),
+    ("rosen_bisect", rosenbrock, [-0.2125, -0.4], "gradient", 0.0557, 1),
+    ("rosen_halve_bisect", rosenbrock, [-1.4323, 1.317], "gradient", 0.0125, 1),
+]
+DELTA, THETA = 0.001, 0.6  # optlib_init_default_parameters_lbfgs defaults (wolfe_delta, wolfe_theta)
+
+
+def direction(fun, x, rule):
+    f, g = fun(x)
+    s = g.copy() if rule == "gradient" else g / DIAG
+    return f, g, s
