@@ -790,9 +790,11 @@ def b_find_n(x, k=None, direction=None):
 
 
 def b_max(x, *rest):
-    """max of a vector: [value, first index of the maximum]."""
+    """max of a vector: [value, first index of the maximum]; max(a, b) elementwise."""
+    if len(rest) == 1:
+        return elementwise(np.fmax, A(x), A(rest[0]))
     if rest:
-        raise MatlabError("max with more than one argument")
+        raise MatlabError("max with more than two arguments")
     v = A(x).reshape(-1, order="F")
     i = int(np.argmax(v))
     return [A(v[i]), A(float(i + 1))]
@@ -834,8 +836,10 @@ def b_hann(n):
 
 
 def b_min(x, *rest):
+    if len(rest) == 1:  # min(a, b): elementwise, NaN ignored as in MATLAB
+        return elementwise(np.fmin, A(x), A(rest[0]))
     if rest:
-        raise MatlabError("min with more than one argument")
+        raise MatlabError("min with more than two arguments")
     a = A(x)
     v = a.reshape(-1, order="F")
     if a.ndim == 2 and (a.shape[0] == 1 or a.shape[1] == 1):
@@ -890,6 +894,11 @@ BUILTINS: Dict[str, Callable] = {
     "pi": lambda: A(np.pi),
     "true": lambda: A(1.0),
     "false": lambda: A(0.0),
+    "isfield": lambda st, name: A(isinstance(st, dict) and str(name) in st),
+    "norm": lambda x: A(float(np.linalg.norm(A(x).ravel()))),
+    "fopen": lambda *a: A(1.0),
+    "fclose": lambda *a: A(0.0),
+    "disp": lambda *a: [],
     "eps": lambda: A(np.finfo(np.float64).eps),
     "log": lambda x: np.asfortranarray(np.log(to_float(A(x)))),
     "cos": lambda x: np.asfortranarray(np.cos(to_float(A(x)))),
@@ -1142,6 +1151,10 @@ class Interpreter:
                 base = env[f[1]]
                 subs = [self.eval_sub(a, env, base, d, len(e[2])) for d, a in enumerate(e[2])]
                 return mread(base, subs)
+            if f[0] == "field":
+                base = self.eval(f, env)
+                if isinstance(base, list):  # struct array (list of dicts), one 1-based index
+                    return base[int(scalar(self.eval(e[2][0], env))) - 1]
             if f[0] == "id":
                 args = [self.eval(a, env) for a in e[2]]
                 r = self.call(f[1], args, nargout=max(nargout, 1))

@@ -39,3 +39,15 @@ def direction(fun, x, rule):
     f, g = fun(x)
     s = g.copy() if rule == "gradient" else g / DIAG
     return f, g, s
+
+# L-BFGS driver cases: name, function, start, options given to optlib_lbfgs
+# (the rest take the defaults of optlib_init_default_parameters_lbfgs)
+LBFGS_CASES = [
+    ("rosen_converge", rosenbrock, [-1.2, 1.0],
+     dict(verbose=0, tolerance=1e-8, max_iterations=200, successive_change=0.0)),
+    ("rosen_stagnation", rosenbrock, [-1.2, 1.0], dict(verbose=0)),
+    ("rosen_capped", rosenbrock, [-1.2, 1.0], dict(verbose=0, max_iterations=7, successive_change=0.0)),
+    ("quad_defaults", quadratic, [1.0, 1.0, 1.0, 1.0, 1.0], dict(verbose=0)),
+    ("quad_tight", quadratic, [1.0, -2.0, 3.0, -4.0, 5.0],
+     dict(verbose=0, tolerance=1e-10, successive_change=0.0, init_step_length=0.01)),
+]
