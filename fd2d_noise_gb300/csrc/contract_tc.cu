@@ -325,8 +325,21 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
             for (int j = 0; j < 32; ++j, p += a.ldacc) *p = widen_exact(v[j]);
             continue;
           }
-          // Overwrite: plain stores.  Accumulate: 16 loads in flight per group,
-          // then the stores (the pass is bound by the latency of these loads).
+          if (!a.overwrite) {
+            // Accumulate: FP64 reductions performed in L2.  Each element has
+            // one writer per pass, so this is the same IEEE addition as a
+            // load, add and store, without the load's round trip.
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const int n = nb + j;
+              if (n < a.N)
+                atomicAdd(n < a.nsplit ? a.acc0 + (int64_t)n * a.ldacc + q
+                                       : a.acc1 + (int64_t)(n - a.nsplit) * a.ldacc + q,
+                          widen_exact(v[j]));
+            }
+            continue;
+          }
+          // Overwrite with a partial or split group of columns: plain stores.
           constexpr int G = 16;
 #pragma unroll
           for (int gg = 0; gg < 32; gg += G) {
