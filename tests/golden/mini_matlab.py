@@ -35,7 +35,7 @@ TOKEN_RE = re.compile(r"""
   | (?P<ws>[ \t\r]+)
 """, re.VERBOSE)
 
-KEYWORDS = {"function", "for", "end", "if", "elseif", "else", "while", "return", "break"}
+KEYWORDS = {"function", "for", "parfor", "end", "if", "elseif", "else", "while", "return", "break"}
 
 
 class Tok:
@@ -228,7 +228,7 @@ class Parser:
     def parse_statement(self):
         tok = self.peek()
         if tok.kind == "kw":
-            if tok.val == "for":
+            if tok.val in ("for", "parfor"):
                 self.next()
                 paren = self.accept("op", "(")
                 var = self.expect("id").val
@@ -762,7 +762,14 @@ def b_size(x, dim=None):
 
 def b_reshape(x, *dims):
     a = A(x)
-    d = [int(scalar(v)) for v in dims] if len(dims) > 1 else [int(v) for v in A(dims[0]).reshape(-1)]
+    if len(dims) > 1:
+        # one dimension may be [] (computed from the others)
+        d = [None if A(v).size == 0 else int(scalar(v)) for v in dims]
+        if None in d:
+            known = int(np.prod([v for v in d if v is not None]))
+            d[d.index(None)] = a.size // known if known else 0
+    else:
+        d = [int(v) for v in A(dims[0]).reshape(-1)]
     if int(np.prod(d)) != a.size:
         raise MatlabError("reshape: number of elements must not change")
     return np.asfortranarray(trim(a.reshape(d, order="F")))
@@ -875,6 +882,17 @@ def b_length(x):
     return A(float(max(a.shape)) if a.size else 0.0)
 
 
+def b_ismember(a, b, mode=None):
+    """ismember(A, B, 'rows'): which rows of A occur among the rows of B."""
+    if mode is None or str(mode) != "rows":
+        raise MatlabError("ismember: only the 'rows' form is supported")
+    a2, b2 = A(a), A(b)
+    a2 = a2.reshape(a2.shape[0], -1, order="F")
+    b2 = b2.reshape(b2.shape[0], -1, order="F")
+    hit = np.array([[float(any(np.array_equal(r, q) for q in b2))] for r in a2])
+    return np.asfortranarray(hit.reshape(-1, 1))
+
+
 BUILTINS: Dict[str, Callable] = {
     "zeros": b_zeros, "ones": b_ones, "size": b_size, "length": lambda x: b_length(x),
     "reshape": b_reshape, "min": b_min, "mod": b_mod, "squeeze": b_squeeze,
@@ -892,6 +910,9 @@ BUILTINS: Dict[str, Callable] = {
     "all": lambda x: A(bool(np.all(A(x) != 0))),
     "numel": lambda x: A(float(A(x).size)),
     "pi": lambda: A(np.pi),
+    "complex": lambda x, y=None: np.asfortranarray(A(x).astype(np.complex128) + (0 if y is None else 1j * A(y))),
+    "num2str": lambda x: str(int(scalar(x))) if float(scalar(x)).is_integer() else repr(float(scalar(x))),
+    "ismember": b_ismember,
     "true": lambda: A(1.0),
     "false": lambda: A(0.0),
     "isfield": lambda st, name: A(isinstance(st, dict) and str(name) in st),
@@ -1001,8 +1022,13 @@ class Interpreter:
             self.assign(s[1], self.eval(s[2], env), env)
         elif kind == "massign":
             targets, rhs = s[1], s[2]
+            if len(targets) == 1 and (rhs[0] != "call" or rhs[1][0] != "id" or rhs[1][1] in env):
+                # [a] = expression
+                if targets[0] is not None:
+                    self.assign(targets[0], self.eval(rhs, env), env)
+                return
             if rhs[0] != "call" or rhs[1][0] != "id":
-                raise MatlabError("multiple assignment needs a function call")
+                raise MatlabError(f"multiple assignment needs a function call: {rhs!r:.200}")
             args = [self.eval_arg(a, env) for a in rhs[2]]
             vals = self.call(rhs[1][1], args, nargout=len(targets))
             for t, v in zip(targets, vals):
@@ -1136,6 +1162,10 @@ class Interpreter:
         if kind == "colon_all":
             return COLON_ALL
         if kind == "matrix":
+            if len(e[1]) == 1:
+                parts = [self.eval(x, env) for x in e[1][0]]
+                if parts and all(isinstance(p, str) for p in parts):
+                    return "".join(parts)  # ['abc' num2str(i) '.mat']
             rows = []
             for r in e[1]:
                 vals = [A(self.eval(x, env)) for x in r]

@@ -1,0 +1,45 @@
+"""The misfit/gradient orchestration against the reference's own
+inversion/optlib_callback_fct/eval_objective_and_gradient.m.
+
+tests/golden/objective_cases.npz holds what that file returns when the
+MATLAB-subset interpreter runs it (tests/golden/make_golden_objective.py) with
+the solvers answered by the FP64 oracle, the reference's own measurement code
+(make_adjoint_sources.m), and the model map, gradient map and regularisation
+as identities -- the part fd2d_noise_gb300.objective restates.  Two reference
+stations, a waveform-difference source measurement and a log-amplitude-ratio
+structure measurement mixed 0.7 / 0.3, for the 'source', 'structure' and
+'joint' inversion types.  With the same oracle behind it, our orchestration
+must call the solvers with the same arguments in the same order: misfit,
+gradient and correlations agree to rounding of the measurement sums.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from fd2d_noise_gb300.objective import eval_objective_and_gradient
+from tests.test_objective import cfg4, oracle_backend, problem
+
+GOLDEN = np.load(os.path.join(os.path.dirname(__file__), "golden", "objective_cases.npz"))
+
+
+@pytest.mark.parametrize("typ", ["source", "structure", "joint"])
+def test_orchestration_matches_reference(typ):
+    cfg = cfg4()
+    p = problem(cfg)
+    j, g, c = eval_objective_and_gradient(p["mu0"], p["rho"], p["spec"], p["sd"], GOLDEN["ref_stat"], GOLDEN["array"],
+                                          GOLDEN["c_data"], GOLDEN["t"], cfg=cfg, type=typ, veldis="dis",
+                                          measurement_source="waveform_difference",
+                                          measurement_structure="log_amplitude_ratio",
+                                          weighting=float(GOLDEN["weighting"]), backend=oracle_backend(cfg))
+    jr, gr, cr = GOLDEN[f"{typ}/j"][0], GOLDEN[f"{typ}/g"], GOLDEN[f"{typ}/c_all"]
+    assert abs(j - jr) <= 1e-13 * abs(jr)
+    assert np.array_equal(c, cr)
+    assert g.shape == gr.shape
+    for q in range(g.shape[2]):
+        n = np.linalg.norm(gr[:, :, q])
+        if n == 0:
+            assert not np.any(g[:, :, q])
+        else:
+            assert np.linalg.norm(g[:, :, q] - gr[:, :, q]) <= 1e-12 * n, q
