@@ -12,7 +12,9 @@ spectrum and the density return the test problem; G_fft files are never
 found, so every station computes its Green function.  Cases: the 'source',
 'structure' and 'joint' inversion types with two reference stations, a
 waveform-difference source measurement and a log-amplitude-ratio structure
-measurement mixed by the weighting.  Outputs go to
+measurement mixed by the weighting; and eval_hessian_vector_product.m for the
+'structure' and 'joint' types (its model-space regularisation term set to
+zero, its Hessian map an identity).  Outputs go to
 tests/golden/objective_cases.npz.
 
     python tests/golden/make_golden_objective.py [path-to-reference-checkout]
@@ -114,6 +116,29 @@ def main():
         out[f"{typ}/g"] = np.asarray(g, dtype=np.float64)
         out[f"{typ}/c_all"] = np.asarray(c_all, dtype=np.float64)
         print(f"  {typ}: j = {float(np.ravel(j)[0]):.10g}, |g| = {np.linalg.norm(g):.4g}", flush=True)
+    # Hessian-vector products (stored fields every step: fw_nth = 1), regularisation weights zero
+    from tests.test_objective import cfg4
+    cfg = cfg4(fw=1)
+    hpaths = paths + [os.path.join(ref, "code", "propagation")]
+    ds = np.asfortranarray(0.1 * p["sd"])
+    out["hvp/ds"] = ds
+    out["hvp/dmu"] = np.asfortranarray(p["dmu"])
+    for typ in ("structure", "joint"):
+        dm = np.asfortranarray(np.concatenate([ds if typ == "joint" else 0 * ds, p["dmu"][:, :, None]], axis=2))
+        usr_par = {"config": {"nx": A(float(cfg.nx)), "nz": A(float(cfg.nz))},
+                   "data": {"t": np.asfortranarray(p["t"].reshape(1, -1)), "c_data": c_data},
+                   "network": {"ref_stat": np.asfortranarray(p["ref"]), "array": np.asfortranarray(p["arr"])},
+                   "type": typ, "veldis": "dis", "verbose": "no",
+                   "measurement": {"source": "waveform_difference", "structure": "log_amplitude_ratio"},
+                   "kernel": {"weighting": A(WEIGHTING)},
+                   "regularization": {"alpha": A(0.0), "beta": A(0.0), "weighting": A(1.0)}}
+        hov = dict(ov)
+        hov["map_Hparameters_to_Hm"] = lambda H, *_: [np.asfortranarray(np.asarray(H).reshape(-1, 1, order="F"))]
+        hov["absorb_specs"] = lambda *_: [A(cfg.absorb_width), A(1.0), A(1.0), A(1.0), A(1.0)]
+        I = Interpreter(hpaths, hov)
+        Hm = I.call("eval_hessian_vector_product", [m, dm, "abcdefgh", usr_par], nargout=1)[0]
+        out[f"hvp/{typ}/H"] = np.asarray(Hm, dtype=np.float64).reshape(m.shape, order="F")
+        print(f"  hvp {typ}: |H| = {np.linalg.norm(Hm):.4g}", flush=True)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({os.path.getsize(OUT) / 1e3:.1f} kB, {len(out)} arrays)")
 

@@ -913,6 +913,7 @@ BUILTINS: Dict[str, Callable] = {
     "complex": lambda x, y=None: np.asfortranarray(A(x).astype(np.complex128) + (0 if y is None else 1j * A(y))),
     "num2str": lambda x: str(int(scalar(x))) if float(scalar(x)).is_integer() else repr(float(scalar(x))),
     "ismember": b_ismember,
+    "repmat": lambda x, m, n=None: np.asfortranarray(np.tile(A(x), (int(scalar(m)), int(scalar(m if n is None else n))))),
     "true": lambda: A(1.0),
     "false": lambda: A(0.0),
     "isfield": lambda st, name: A(isinstance(st, dict) and str(name) in st),

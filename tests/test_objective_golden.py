@@ -1,5 +1,6 @@
-"""The misfit/gradient orchestration against the reference's own
-inversion/optlib_callback_fct/eval_objective_and_gradient.m.
+"""The misfit/gradient and Hessian-vector orchestration against the
+reference's own inversion/optlib_callback_fct/eval_objective_and_gradient.m
+and eval_hessian_vector_product.m.
 
 tests/golden/objective_cases.npz holds what that file returns when the
 MATLAB-subset interpreter runs it (tests/golden/make_golden_objective.py) with
@@ -13,7 +14,6 @@ must call the solvers with the same arguments in the same order: misfit,
 gradient and correlations agree to rounding of the measurement sums.
 """
 import os
-import sys
 
 import numpy as np
 import pytest
@@ -43,3 +43,27 @@ def test_orchestration_matches_reference(typ):
             assert not np.any(g[:, :, q])
         else:
             assert np.linalg.norm(g[:, :, q] - gr[:, :, q]) <= 1e-12 * n, q
+
+
+@pytest.mark.parametrize("typ", ["structure", "joint"])
+def test_hessian_vector_product_matches_reference(typ):
+    """eval_hessian_vector_product.m (Green, Born Green, correlation, Born
+    correlations, first- and second-order adjoint sources, adjoint modes 13,
+    11, 12 and 10) with its regularisation term set to zero."""
+    from fd2d_noise_gb300.objective import eval_hessian_vector_product
+    cfg = cfg4(fw=1)
+    p = problem(cfg)
+    H = eval_hessian_vector_product(p["mu0"], p["rho"], p["spec"], p["sd"], GOLDEN["ref_stat"], GOLDEN["array"],
+                                    GOLDEN["c_data"], GOLDEN["t"], GOLDEN["hvp/dmu"],
+                                    GOLDEN["hvp/ds"] if typ == "joint" else None, cfg=cfg, type=typ, veldis="dis",
+                                    measurement_source="waveform_difference",
+                                    measurement_structure="log_amplitude_ratio",
+                                    weighting=float(GOLDEN["weighting"]), backend=oracle_backend(cfg))
+    Hr = GOLDEN[f"hvp/{typ}/H"]
+    assert H.shape == Hr.shape
+    for q in range(H.shape[2]):
+        n = np.linalg.norm(Hr[:, :, q])
+        if n == 0:
+            assert not np.any(H[:, :, q])
+        else:
+            assert np.linalg.norm(H[:, :, q] - Hr[:, :, q]) <= 1e-12 * n, q
