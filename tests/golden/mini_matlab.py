@@ -1,12 +1,19 @@
 """A small MATLAB-subset interpreter (test infrastructure).
 
-It executes the reference's own solver sources (code/run_*.m and
-code/propagation/*.m) as written, so that golden vectors can be produced here
-without MATLAB.  It implements the subset those files use: function files with
-multiple outputs, for / if-elseif-else, indexed reads and writes with ``:``
-and ``end``, column-major linear indexing, implicit expansion, complex values,
-``single`` arithmetic (an operation with a single operand is carried out in
-single precision, as MATLAB does) and the builtins listed in ``BUILTINS``.
+It executes the reference's own sources as written -- the solvers
+(code/run_*.m, code/propagation/*.m), the noise-source model, the
+measurements, the model maps, the optimiser (inversion/optlib) and the
+misfit / gradient / Hessian orchestration -- so that golden vectors can be
+produced here without MATLAB.  It implements the subset those files use:
+function files with multiple outputs and ``nargin``, for / parfor / while /
+if-elseif-else, indexed reads and writes with ``:`` and ``end``, column-major
+linear indexing, implicit expansion, complex values, ``single`` arithmetic (an
+operation with a single operand is carried out in single precision, as MATLAB
+does), scalar structs (Python dicts) and struct arrays (lists of dicts),
+string concatenation, and the builtins listed in ``BUILTINS``.  Functions
+outside the reference checkout (solver MEX calls in the orchestration cases,
+user callbacks of the optimiser, configuration getters) are supplied by the
+caller as overrides.
 
 Values are numpy arrays with at least two dimensions in Fortran order; strings
 are Python ``str``.  Anything outside the subset raises ``MatlabError``.
