@@ -1083,6 +1083,12 @@ class Interpreter:
             subs = [self.eval_sub(a, env, base, d, len(target[2])) for d, a in enumerate(target[2])]
             env[name] = massign_into(base, subs, value)
             return
+        if target[0] == "call" and target[1][0] == "field":
+            # s.a(i) = v: assign into the field's value, then store it back
+            base = self.eval(target[1], env)
+            subs = [self.eval_sub(a, env, base, d, len(target[2])) for d, a in enumerate(target[2])]
+            self.assign(target[1], massign_into(base, subs, value), env)
+            return
         if target[0] == "field":
             # s.a.b = v on scalar structs (dicts), created as needed
             path, t = [], target
