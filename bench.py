@@ -131,6 +131,15 @@ def cpu_sample(w, nt_cpu: int, threads: int):
     return gpt / dt / 1e9, dt, gpt, cfg
 
 
+def one_thread_sample(w, nt_cpu: int) -> dict:
+    """The CPU oracle on one thread, on an eighth of the all-core sample's
+    steps (at least 4): the single-core figure beside the all-core one."""
+    nt1 = max(4, nt_cpu // 8)
+    v, dt, gpt, cfg = cpu_sample(w, nt1, 1)
+    return {"value_1thread": v,
+            "sample_1thread": f"one station, nt truncated to {cfg.nt} ({gpt:.3g} updates, {dt:.1f} s), 1 thread"}
+
+
 def workload_config(w, world):
     """The ``config`` object of both arms' lines for a single-grid workload."""
     cfg = w.cfg
@@ -168,7 +177,7 @@ def run_reference(args, w, world, rank):
         # (cpu_baseline.sample) and reports the same per-update rate
         "config": workload_config(w, world),
         "cpu_baseline": {"value": value, "unit": "Gpt-updates/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, **one_thread_sample(w, args.cpu_nt)},
         "e2e": {"value": value, "unit": "Gpt-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU restatement of the reference's MATLAB solvers (MATLAB unavailable), OpenMP over grid points",
     }
@@ -358,7 +367,8 @@ def main():
         result["cpu_baseline"] = {
             "value": v, "unit": "Gpt-updates/s", "cores": threads, "kind": "port",
             "sample": f"one station, nt truncated to {ccfg.nt} ({gpt:.3g} updates, {dt:.1f} s): "
-                      "FP64 C++ restatement of the reference solvers, MATLAB unavailable"}
+                      "FP64 C++ restatement of the reference solvers, MATLAB unavailable",
+            **one_thread_sample(w, args.cpu_nt)}
     if rank == 0:
         print(json.dumps(result), flush=True)
     if world > 1:

@@ -33,6 +33,7 @@ def test_reference_arm_prints_one_contract_line():
     assert d["config"]["workload"] == "single_600_o8" and d["config"]["nx"] == 600
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and "nt truncated to 4" in cb["sample"]
+    assert cb["value_1thread"] > 0 and "1 thread" in cb["sample_1thread"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 
