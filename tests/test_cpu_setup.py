@@ -1,12 +1,11 @@
 """CPU-only checks: host-side setup, oracle helpers, library load and symbols."""
-import ctypes
 import os
 import re
 
 import numpy as np
 import pytest
 
-from fd2d_noise_gb300.config import Config, matlab_colon, n_fw_green, n_fw_corr
+from fd2d_noise_gb300.config import matlab_colon, n_fw_green, n_fw_corr
 from tests.problems import small_cfg
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

@@ -1,6 +1,5 @@
 """GPU solvers against the reference's own outputs (tests/golden): the plain
 FP64 form to <= 1e-10 relative L2, the FP32 form to <= 1e-4."""
-import numpy as np
 import pytest
 
 from tests.golden_cases import cfg, group, rel
