@@ -8,6 +8,7 @@ launch counts, which need a GPU.
 """
 import json
 import os
+import socket
 import subprocess
 import sys
 
@@ -37,9 +38,15 @@ def test_reference_arm_prints_one_contract_line():
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 
+def _free_port() -> int:
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
 def test_reference_arm_under_two_ranks_prints_from_rank_zero_only():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
-           "--master-addr", "127.0.0.1", "--master-port", "29517", *ARGS, "--gpus", "2"]
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), *ARGS, "--gpus", "2"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600,
                        env={**os.environ, "OMP_NUM_THREADS": "2"})
     assert r.returncode == 0, r.stderr[-2000:]
