@@ -340,22 +340,12 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
             continue;
           }
           // Overwrite with a partial or split group of columns: plain stores.
-          constexpr int G = 16;
 #pragma unroll
-          for (int gg = 0; gg < 32; gg += G) {
-            double* p[G];
-            double old[G];
-#pragma unroll
-            for (int j = 0; j < G; ++j) {
-              const int n = n0 + c0 + gg + j;
-              p[j] = n >= a.N ? nullptr
-                              : (n < a.nsplit ? a.acc0 + (int64_t)n * a.ldacc + q
-                                              : a.acc1 + (int64_t)(n - a.nsplit) * a.ldacc + q);
-              old[j] = (p[j] && !a.overwrite) ? *p[j] : 0.0;
-            }
-#pragma unroll
-            for (int j = 0; j < G; ++j)
-              if (p[j]) *p[j] = a.overwrite ? widen_exact(v[gg + j]) : old[j] + widen_exact(v[gg + j]);
+          for (int j = 0; j < 32; ++j) {
+            const int n = nb + j;
+            if (n < a.N)
+              *(n < a.nsplit ? a.acc0 + (int64_t)n * a.ldacc + q
+                             : a.acc1 + (int64_t)(n - a.nsplit) * a.ldacc + q) = widen_exact(v[j]);
           }
         }
       }
