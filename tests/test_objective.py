@@ -74,6 +74,28 @@ def test_oracle_gradient_matches_finite_differences():
     assert max(errs) < 1e-2, errs
 
 
+def test_oracle_source_gradient_matches_finite_differences():
+    """The source kernel (run_noise_adjoint.m:302-320, plane 1 of the 'source'
+    gradient) against finite differences of the misfit along a perturbation of
+    the noise distribution; the error falls with h (first-order differences
+    of the nonlinear log-amplitude misfit)."""
+    cfg = cfg4()
+    p = problem(cfg)
+    backend = oracle_backend(cfg)
+    _, _, c_data = run(cfg, p, p["mu_true"], np.zeros((3, cfg.ntc)), backend, None, only=True)
+    j0, g, _ = run(cfg, p, p["mu0"], c_data, backend, None, type="source")
+    X, Z = np.meshgrid(np.linspace(0, cfg.Lx, cfg.nx), np.linspace(0, cfg.Lz, cfg.nx), indexing="ij")
+    dsd = 0.5 * np.exp(-((X - 0.5e6) ** 2 + (Z - 0.4e6) ** 2) / 1.5e5 ** 2)
+    pred = float(np.sum(g[:, :, 0] * dsd))
+    errs = []
+    for h in (1e-2, 1e-4):
+        q = dict(p, sd=np.asfortranarray(p["sd"] + h * dsd[:, :, None]))
+        j1, _, _ = run(cfg, q, p["mu0"], c_data, backend, None, only=True, type="source")
+        fd = (j1 - j0) / h
+        errs.append(abs(fd - pred) / abs(fd))
+    assert errs[1] < 1e-3 and errs[1] < errs[0] / 20, errs
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("memspace", ["device", "host"])
 @pytest.mark.parametrize("type", ["structure", "joint", "source"])
