@@ -128,6 +128,31 @@ def test_gpu_gradient_matches_finite_differences(fd2d_lib):
     assert max(errs32) < 2e-2, errs32
 
 
+def test_oracle_born_correlations_match_finite_differences():
+    """inversion/optlib/optlib_check_du.m on the oracle: the Born correlations
+    of the Hessian chain (Born Green, mode 5 with dmu, then the Born
+    correlation with dmu and the stored correlation field,
+    eval_hessian_vector_product.m:58-104) against finite differences of the
+    correlations along dmu; the error falls linearly with h."""
+    from oracle import pyoracle
+    pyoracle.build()
+    cfg = cfg4(fw=1)
+    p = problem(cfg)
+    src, rec = p["ref"], p["arr"][1:]
+    mu, rho, dmu, spec, sd = p["mu0"], p["rho"], p["dmu"], p["spec"], p["sd"]
+
+    def corr(m):
+        G_fft, G, _ = pyoracle.forward1_green(cfg, m, rho, src, rec, 1, None, None)
+        c, C = pyoracle.forward2_correlation(cfg, m, rho, G_fft, spec, sd, rec, 1, None, None)
+        return G, C, np.asarray(c)
+
+    G, C, c0 = corr(mu)
+    dG_fft, _, _ = pyoracle.forward1_green(cfg, mu, rho, src, rec, 5, dmu, G)
+    du = np.asarray(pyoracle.forward2_correlation(cfg, mu, rho, dG_fft, spec, sd, rec, 1, dmu, C)[0])
+    errs = [np.linalg.norm((corr(mu + h * dmu)[2] - c0) / h - du) / np.linalg.norm(du) for h in (1e-2, 1e-3)]
+    assert errs[1] < 1e-4 and errs[1] < errs[0] / 5, errs
+
+
 def hvp(cfg, p, c_data, backend=None, precision="fp64", type="structure", ds=None):
     from fd2d_noise_gb300.objective import eval_hessian_vector_product
     return eval_hessian_vector_product(p["mu0"], p["rho"], p["spec"], p["sd"], p["ref"], p["arr"], c_data, p["t"],
