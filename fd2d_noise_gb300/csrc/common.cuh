@@ -12,6 +12,7 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -42,6 +43,29 @@ fd2d_status set_error(fd2d_ctx* ctx, fd2d_status s, const std::string& msg);
                                                                       : FD2D_ERR_CUDA, \
                                std::string(#expr) + ": " + cudaGetErrorString(_e)); \
   } while (0)
+
+// Work done once per CUDA device, the first time a caller reaches it with that
+// device current: kernel attributes such as the dynamic shared-memory opt-in
+// belong to a device, not to the process.  Callers on several host threads are
+// serialised; a failed attempt is retried by the next caller.
+class PerDeviceOnce {
+ public:
+  template <typename F>
+  fd2d_status run(fd2d_ctx* ctx, F&& work) {
+    int dev = 0;
+    FD2D_CUDA(ctx, cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu_);
+    if ((size_t)dev < done_.size() && done_[dev]) return FD2D_OK;
+    FD2D_TRY(work());
+    if ((size_t)dev >= done_.size()) done_.resize((size_t)dev + 1, 0);
+    done_[dev] = 1;
+    return FD2D_OK;
+  }
+
+ private:
+  std::mutex mu_;
+  std::vector<char> done_;
+};
 
 // ---- host problem setup ---------------------------------------------------------
 // Everything a solver needs from fd2d_config, derived once on the host.

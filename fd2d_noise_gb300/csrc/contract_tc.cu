@@ -376,13 +376,12 @@ fd2d_status contract_image(fd2d_ctx* ctx, cudaStream_t stream, const float* src,
   return after_launch(ctx, "k_image");
 }
 
+PerDeviceOnce g_contract_attributes;
 fd2d_status contract_prepare(fd2d_ctx* ctx) {
-  static bool attr = false;
-  if (!attr) {
+  return g_contract_attributes.run(ctx, [ctx]() -> fd2d_status {
     FD2D_CUDA(ctx, cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr = true;
-  }
-  return FD2D_OK;
+    return FD2D_OK;
+  });
 }
 
 fd2d_status contract(fd2d_ctx* ctx, cudaStream_t stream, const ContractArgs& a) {

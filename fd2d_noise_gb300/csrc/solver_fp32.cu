@@ -742,16 +742,16 @@ fd2d_status step_attributes_r(fd2d_ctx* ctx) {
   return step_attributes_t<R, 32>(ctx);
 }
 
-// Opt the step kernels in to their dynamic shared memory (once, before any capture).
+// Opt the step kernels in to their dynamic shared memory (once per device,
+// before any capture on it).
+PerDeviceOnce g_step_attributes;
 fd2d_status step_attributes(fd2d_ctx* ctx) {
-  static bool done = false;
-  if (done) return FD2D_OK;
-  FD2D_TRY(step_attributes_r<1>(ctx));
-  FD2D_TRY(step_attributes_r<2>(ctx));
-  FD2D_TRY(step_attributes_r<3>(ctx));
-  FD2D_TRY(step_attributes_r<4>(ctx));
-  done = true;
-  return FD2D_OK;
+  return g_step_attributes.run(ctx, [ctx]() -> fd2d_status {
+    FD2D_TRY(step_attributes_r<1>(ctx));
+    FD2D_TRY(step_attributes_r<2>(ctx));
+    FD2D_TRY(step_attributes_r<3>(ctx));
+    return step_attributes_r<4>(ctx);
+  });
 }
 
 fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, int par, Step32 s) {
@@ -1746,7 +1746,7 @@ extern "C" fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg,
   const int nx = g.nx, nz = g.nz, P = (nx + 31) / 32 * 32;
   const int64_t ps = ((int64_t)P * nz + 127) / 128 * 128;
   const size_t plane = (size_t)ps * 4;
-  const size_t head = 256 + (((size_t)(ns + nr) * 8 + 255) / 256) * 256;
+  const size_t head = 256 + ((((size_t)ns + (size_t)nr) * sizeof(int2) + 255) / 256) * 256;
   const size_t need = head + 9 * plane;
   if (need > FD2D_NOALLOC_SCRATCH_BYTES)
     return set_error(nullptr, FD2D_ERR_SHAPE,

@@ -337,7 +337,10 @@ fd2d_status fd2d_contract_f32(fd2d_ctx* ctx, const float* A, int64_t lda, const 
  * and receiver must fit, else FD2D_ERR_SHAPE.  The first call on a device looks
  * up that array's device address (make that first call before any stream
  * capture).  Every call reuses the same array, so calls whose work overlaps on
- * the GPU (other streams, other host threads) race: serialise them. */
+ * the GPU (other streams, other host threads) race: serialise them.  The call
+ * waits for its own work on `stream` before it returns (it reads the
+ * device-side error flag back).  Its seismograms are bit-identical to those of
+ * fd2d_forward1_green in FP32, mode 0, on the same inputs. */
 #define FD2D_NOALLOC_SCRATCH_BYTES (16u << 20)
 fd2d_status fd2d_forward1_seismograms_noalloc(const fd2d_config* cfg, const double* mu, const double* rho,
                                               const double* src, int32_t ns, const double* rec, int32_t nr,

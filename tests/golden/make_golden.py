@@ -10,7 +10,7 @@ below.  Inputs are seeded; inputs and outputs are written to
 tests/golden/reference_cases.npz, which the oracle and GPU tests compare
 against.
 
-    python tests/golden/make_golden.py [path-to-reference-checkout]
+    python tests/golden/make_golden.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
 from __future__ import annotations
 
@@ -22,7 +22,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from mini_matlab import A, Interpreter  # noqa: E402
+from mini_matlab import A, Interpreter, reference_checkout  # noqa: E402
 
 OUT = os.path.join(HERE, "reference_cases.npz")
 
@@ -173,7 +173,7 @@ def run_cases(ref_root):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_checkout(sys.argv)
     out = run_cases(ref)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({os.path.getsize(OUT) / 1e6:.2f} MB, {len(out)} arrays)")

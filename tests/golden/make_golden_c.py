@@ -10,7 +10,7 @@ not a case: with n_basis_fct == 0 the reference forms the per-frequency
 distribution as ones(n_sample,1) times the source maps, which only conforms
 for one source.)  Outputs go to tests/golden/reference_cases_c.npz.
 
-    python tests/golden/make_golden_c.py [path-to-reference-checkout]
+    python tests/golden/make_golden_c.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
 from __future__ import annotations
 
@@ -22,14 +22,14 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 from make_golden import E, S, config, inputs, overrides  # noqa: E402
-from mini_matlab import A, Interpreter  # noqa: E402
+from mini_matlab import A, Interpreter, reference_checkout  # noqa: E402
 
 OUT = os.path.join(HERE, "reference_cases_c.npz")
 SIDES = (1.0, 0.0, 1.0, 0.0)  # absorb_left, absorb_right, absorb_top, absorb_bottom
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_checkout(sys.argv)
     paths = [os.path.join(ref, "code"), os.path.join(ref, "code", "propagation")]
     c = config(nx=21, nz=15, nt=36, order=4, K=9, fs=3, fw=3, nb=0, width_pts=3)
     ov = overrides(c)

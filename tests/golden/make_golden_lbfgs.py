@@ -10,7 +10,7 @@ reference's inversion callback does), optlib_restore_lbfgs_information (no
 stored iterations) and optlib_generate_random_string.  Outputs go to
 tests/golden/lbfgs_cases.npz.
 
-    python tests/golden/make_golden_lbfgs.py [path-to-reference-checkout]
+    python tests/golden/make_golden_lbfgs.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
 from __future__ import annotations
 
@@ -22,14 +22,14 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from mini_matlab import A, Interpreter  # noqa: E402
+from mini_matlab import A, Interpreter, reference_checkout  # noqa: E402
 from wolfe_problems import LBFGS_CASES  # noqa: E402
 
 OUT = os.path.join(HERE, "lbfgs_cases.npz")
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_checkout(sys.argv)
     paths = [os.path.join(ref, "inversion", "optlib")]
     out = {}
     for name, fun, m0, opts in LBFGS_CASES:

@@ -4,7 +4,7 @@ TEST INFRASTRUCTURE.  Runs the unmodified tools/addons/gaussblur2d.m through
 the MATLAB-subset interpreter (mini_matlab.py) on seeded maps and writes inputs
 and outputs to tests/golden/map_cases.npz.
 
-    python tests/golden/make_golden_maps.py [path-to-reference-checkout]
+    python tests/golden/make_golden_maps.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
 from __future__ import annotations
 
@@ -15,7 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from mini_matlab import A, Interpreter  # noqa: E402
+from mini_matlab import A, Interpreter, reference_checkout  # noqa: E402
 
 OUT = os.path.join(HERE, "map_cases.npz")
 
@@ -38,4 +38,4 @@ def run_cases(ref_root):
 
 
 if __name__ == "__main__":
-    run_cases(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    run_cases(reference_checkout(sys.argv))

@@ -8,7 +8,7 @@ and outputs to tests/golden/measurement_cases.npz.  MATLAB's closed built-ins
 used there (hann, trapz) are restated in mini_matlab.py from their documented
 definitions.
 
-    python tests/golden/make_golden_measure.py [path-to-reference-checkout]
+    python tests/golden/make_golden_measure.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
 from __future__ import annotations
 
@@ -19,7 +19,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from mini_matlab import A, Interpreter  # noqa: E402
+from mini_matlab import A, Interpreter, reference_checkout  # noqa: E402
 
 OUT = os.path.join(HERE, "measurement_cases.npz")
 
@@ -72,4 +72,4 @@ def run_cases(ref_root):
 
 
 if __name__ == "__main__":
-    run_cases(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    run_cases(reference_checkout(sys.argv))

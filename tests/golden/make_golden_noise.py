@@ -10,7 +10,7 @@ the two parameter sets the reference selects by domain size; 'point' indexes
 past its one-source arrays and 'picture' reads an image file, so neither runs.
 Outputs go to tests/golden/noise_source_cases.npz.
 
-    python tests/golden/make_golden_noise.py [path-to-reference-checkout]
+    python tests/golden/make_golden_noise.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
 from __future__ import annotations
 
@@ -21,7 +21,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from mini_matlab import A, Interpreter  # noqa: E402
+from mini_matlab import A, Interpreter, reference_checkout  # noqa: E402
 
 OUT = os.path.join(HERE, "noise_source_cases.npz")
 
@@ -50,7 +50,7 @@ def overrides(L, n, f):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_checkout(sys.argv)
     paths = [os.path.join(ref, "input"), os.path.join(ref, "code", "propagation"), os.path.join(ref, "code")]
     out = {}
     for name, kind, nb, L, n, K in CASES:

@@ -17,7 +17,7 @@ measurement mixed by the weighting; and eval_hessian_vector_product.m for the
 zero, its Hessian map an identity).  Outputs go to
 tests/golden/objective_cases.npz.
 
-    python tests/golden/make_golden_objective.py [path-to-reference-checkout]
+    python tests/golden/make_golden_objective.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
 from __future__ import annotations
 
@@ -30,7 +30,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, HERE)
 sys.path.insert(0, ROOT)
-from mini_matlab import A, Interpreter  # noqa: E402
+from mini_matlab import A, Interpreter, reference_checkout  # noqa: E402
 
 OUT = os.path.join(HERE, "objective_cases.npz")
 TYPES = ("source", "structure", "joint")
@@ -49,7 +49,7 @@ def problem():
 def main():
     from oracle import pyoracle
     pyoracle.build()
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_checkout(sys.argv)
     cfg, p = problem()
     paths = [os.path.join(ref, "inversion", "optlib_callback_fct"), os.path.join(ref, "tools", "measurement"),
              os.path.join(ref, "tools", "measurement", "addons"), os.path.join(ref, "tools", "addons")]

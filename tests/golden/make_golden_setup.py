@@ -7,7 +7,7 @@ absorb_specs supplied as builtins returning the cases below (non-square grids,
 narrow and wide layers, all four sides or only some).  Outputs go to
 tests/golden/setup_cases.npz.
 
-    python tests/golden/make_golden_setup.py [path-to-reference-checkout]
+    python tests/golden/make_golden_setup.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
 from __future__ import annotations
 
@@ -18,7 +18,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from mini_matlab import A, Interpreter  # noqa: E402
+from mini_matlab import A, Interpreter, reference_checkout  # noqa: E402
 
 OUT = os.path.join(HERE, "setup_cases.npz")
 
@@ -32,7 +32,7 @@ CASES = [
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_checkout(sys.argv)
     paths = [os.path.join(ref, "code", "propagation")]
     out = {}
     for name, Lx, Lz, nx, nz, w, l, r, t, b in CASES:

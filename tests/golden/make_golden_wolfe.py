@@ -7,7 +7,7 @@ wolfe_problems.py; the objective callbacks it calls by name
 optlib_generate_random_string are supplied as builtins that record every
 point the line search evaluates.  Outputs go to tests/golden/wolfe_cases.npz.
 
-    python tests/golden/make_golden_wolfe.py [path-to-reference-checkout]
+    python tests/golden/make_golden_wolfe.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
 from __future__ import annotations
 
@@ -18,14 +18,14 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from mini_matlab import A, Interpreter  # noqa: E402
+from mini_matlab import A, Interpreter, reference_checkout  # noqa: E402
 from wolfe_problems import CASES, DELTA, THETA, direction  # noqa: E402
 
 OUT = os.path.join(HERE, "wolfe_cases.npz")
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_checkout(sys.argv)
     paths = [os.path.join(ref, "inversion", "optlib")]
     out = {}
     for name, fun, x0, rule, sig0, larger in CASES:

@@ -31,6 +31,18 @@ class MatlabError(RuntimeError):
     pass
 
 
+def reference_checkout(argv: List[str]) -> str:
+    """The reference checkout a fixture generator reads: its first command-line
+    argument, else the FD2D_REFERENCE environment variable (no default)."""
+    if len(argv) > 1:
+        return argv[1]
+    path = os.environ.get("FD2D_REFERENCE")
+    if not path:
+        raise SystemExit(f"usage: python {os.path.basename(argv[0])} <reference checkout> "
+                         "(or set FD2D_REFERENCE)")
+    return path
+
+
 # ---------------------------------------------------------------------------
 # tokenizer
 # ---------------------------------------------------------------------------

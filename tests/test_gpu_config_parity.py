@@ -1,0 +1,176 @@
+"""GPU parity against the FP64 CPU oracle at the benchmark configurations' own sizes.
+
+The small-grid parity tests pin every mode on grids of 33-70 points; these
+cases run the oracle on the configurations themselves, so that the paths that
+engage only at size are compared with it directly: 32x40 tiles of two lanes,
+multi-pass DFT contractions whose later passes add into the FP64 spectra by
+reductions, injection planes evaluated in several chunks, and the
+order-8 / K = 300 tables.
+
+* configuration 1 in full: 300x300, dt 0.1 s, nt 1200, order 4, 200
+  frequencies, 10 receivers, one reference station (Green run and correlation
+  run, code/run_forward1_green.m and code/run_forward2_correlation.m);
+* configuration 2 with nt truncated to 400: 600x600, dt 0.05 s, order 8, 300
+  frequencies, 40 receivers, both reference stations -- the plain FP64 form
+  one station at a time, the FP32 form as the benchmark runs it (both
+  stations as lanes of one batch call), and once more with the DFT forced
+  into 32-snapshot passes and the injection into 128-event chunks;
+* configuration 4 with nt 1100 (the 100-200 s measurement window still inside
+  the record): 512x512, snapshots every 5 steps, 200 frequencies, 20 receivers
+  around one reference station, log-amplitude-ratio adjoint sources, adjoint
+  modes 1 and 0 through eval_objective_and_gradient (inversion type 'joint':
+  the source kernel and the mu kernel).
+
+Bars, as in the small-grid tests: the plain FP64 form within 1e-10 relative L2
+of the oracle on spectra, seismograms, correlations, misfit and both kernel
+planes; the FP32 form within 1e-4 (every FP32 error is printed).
+"""
+import numpy as np
+import pytest
+
+from tests.problems import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+TOL32 = 1e-4
+
+
+def _report(label, err, tol):
+    print(f"{label}: rel L2 {err:.3e} (bar {tol:g})")
+    assert err <= tol, (label, err)
+
+
+def _solve_pair(S, w, src, prec):
+    """Green run (mode 0) then correlation run (mode 0) through the C ABI."""
+    G, _, s = S.run_forward1_green(w.mu, w.rho, src, w.receivers, 0, cfg=w.cfg, precision=prec)
+    c, _ = S.run_forward2_correlation(w.mu, w.rho, G, w.spectrum, w.source_dist, w.receivers, 0,
+                                      cfg=w.cfg, precision=prec)
+    return G, s, c
+
+
+def test_config1_full_size_against_oracle(fd2d_lib, oracle):
+    from fd2d_noise_gb300 import solvers as S
+    from fd2d_noise_gb300.workloads import plain_cpu_300
+    w = plain_cpu_300()
+    src = w.ref_stations[:1]
+    Go, so, co = _solve_pair(oracle_solvers(oracle), w, src, None)
+    assert np.abs(co).max() > 0
+    for prec, tol in (("fp64", TOL64), ("fp32", TOL32)):
+        G, s, c = _solve_pair(S, w, src, prec)
+        _report(f"config 1 {prec} Green spectra", rel_l2(G, Go), tol)
+        _report(f"config 1 {prec} Green seismograms", rel_l2(s, so), tol)
+        _report(f"config 1 {prec} correlations", rel_l2(c, co), tol)
+
+
+class oracle_solvers:
+    """The oracle behind the solvers' call signatures (cfg and precision as keywords)."""
+
+    def __init__(self, oracle):
+        self.o = oracle
+
+    def run_forward1_green(self, mu, rho, src, rec, mode, *, cfg, precision):
+        return self.o.forward1_green(cfg, mu, rho, src, rec, mode)
+
+    def run_forward2_correlation(self, mu, rho, G, spec, sd, rec, mode, *, cfg, precision):
+        return self.o.forward2_correlation(cfg, mu, rho, G, spec, sd, rec, mode)
+
+
+@pytest.fixture(scope="module")
+def config2():
+    """Configuration 2 at nt 400 with the oracle's results for both stations."""
+    from oracle import pyoracle
+    from fd2d_noise_gb300.workloads import single_600_o8
+    w = single_600_o8(nt=400)
+    out = []
+    for i in range(w.ref_stations.shape[0]):
+        G, _, s = pyoracle.forward1_green(w.cfg, w.mu, w.rho, w.ref_stations[i:i + 1], w.receivers, 0)
+        c, _ = pyoracle.forward2_correlation(w.cfg, w.mu, w.rho, G, w.spectrum, w.source_dist, w.receivers, 0)
+        # the spectra are 1.7 GB per station: keep station 0's only
+        out.append((G if i == 0 else None, s, c))
+    return w, out
+
+
+def test_config2_fp64_against_oracle(fd2d_lib, oracle, config2):
+    from fd2d_noise_gb300 import solvers as S
+    w, ref = config2
+    for i, (Go, so, co) in enumerate(ref):
+        G, s, c = _solve_pair(S, w, w.ref_stations[i:i + 1], "fp64")
+        if Go is not None:
+            _report(f"config 2 station {i} fp64 Green spectra", rel_l2(G, Go), TOL64)
+        _report(f"config 2 station {i} fp64 Green seismograms", rel_l2(s, so), TOL64)
+        _report(f"config 2 station {i} fp64 correlations", rel_l2(c, co), TOL64)
+
+
+@pytest.mark.parametrize("chunks", [(0, 0), (32, 128)], ids=["default_passes", "dft32_inj128"])
+def test_config2_fp32_batch_against_oracle(fd2d_lib, oracle, config2, chunks):
+    """The benchmark's own call: both stations as lanes of one
+    fd2d_correlation_batch (device buffers), against the oracle per station."""
+    import torch
+    from fd2d_noise_gb300 import _lib
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+    w, ref = config2
+    cfg, nr = w.cfg, w.receivers.shape[0]
+    sess = DeviceSession(cfg, 0, "fp32")
+    _lib.check(sess.ctx.L.fd2d_ctx_set_chunks(sess.ctx.h, *chunks), sess.ctx.h)
+    d = {k: to_device(getattr(w, k), np.float64) for k in ("mu", "rho", "spectrum", "source_dist", "receivers")}
+    outs = [sess.zeros(nr * cfg.ntc, torch.float64) for _ in ref]
+    jobs = [dict(cfg=cfg, mu=d["mu"], rho=d["rho"], spectrum=d["spectrum"], source_dist=d["source_dist"],
+                 src=to_device(w.ref_stations[i:i + 1], np.float64), rec=d["receivers"], nr=nr, out=o)
+            for i, o in enumerate(outs)]
+    sess.correlation_batch(jobs)
+    torch.cuda.synchronize()
+    lanes = sess.ctx.last_batch()
+    sess.ctx.close()
+    assert lanes == [2], lanes  # one launch group of two lanes, as in the benchmark
+    for i, ((_, _, co), o) in enumerate(zip(ref, outs)):
+        c = o.cpu().numpy().reshape(nr, cfg.ntc, order="F")
+        _report(f"config 2 station {i} fp32 batch correlations, chunks {chunks}", rel_l2(c, co), TOL32)
+
+
+def test_config2_fp32_spectra_in_passes_against_oracle(fd2d_lib, oracle, config2):
+    """Station 0's Green spectra and correlations with the DFT in 32-snapshot
+    passes (the first pass stores the FP64 spectra, later ones add into them)
+    and the injection planes in 128-event chunks."""
+    from fd2d_noise_gb300 import _lib
+    from fd2d_noise_gb300 import solvers as S
+    w, ref = config2
+    Go, so, co = ref[0]
+    ctx = S.context(0, "fp32")
+    _lib.check(ctx.L.fd2d_ctx_set_chunks(ctx.h, 32, 128), ctx.h)
+    try:
+        G, s, c = _solve_pair(S, w, w.ref_stations[:1], "fp32")
+    finally:
+        _lib.check(ctx.L.fd2d_ctx_set_chunks(ctx.h, 0, 0), ctx.h)
+    _report("config 2 fp32 Green spectra, 32-snapshot passes", rel_l2(G, Go), TOL32)
+    _report("config 2 fp32 Green seismograms", rel_l2(s, so), TOL32)
+    _report("config 2 fp32 correlations, 128-event injection chunks", rel_l2(c, co), TOL32)
+
+
+def test_config4_reduced_nt_against_oracle(fd2d_lib, oracle):
+    """The structure-kernel workload (512x512, fw 5, K 200, 20 receivers) at
+    nt 1100 through eval_objective_and_gradient, inversion type 'joint'."""
+    from tests.test_gpu_fullsize import _structure_problem
+    from tests.test_objective import oracle_backend
+    from fd2d_noise_gb300.objective import eval_objective_and_gradient, gpu_backend
+    cfg, p = _structure_problem()
+    cfg = cfg.replace(nt=1100)
+    t = (-(cfg.nt - 1) + np.arange(cfg.ntc)) * cfg.dt
+
+    def run(mu, c_data, backend, only=False):
+        return eval_objective_and_gradient(mu, p["rho"], p["spec"], p["sd"], p["ref"], p["arr"], c_data, t,
+                                           cfg=cfg, backend=backend, weighting=1.0, only_objective=only,
+                                           type="joint")
+
+    # observed correlations from the perturbed medium (the plain FP64 form;
+    # both sides of the comparison get the same data)
+    _, _, c_data = run(p["mu_true"], np.zeros((20, cfg.ntc)), gpu_backend(cfg, "fp64"), only=True)
+    jo, go, co = run(p["mu0"], c_data, oracle_backend(cfg))
+    assert jo > 0 and go.shape[2] == 2
+    assert all(np.linalg.norm(go[:, :, q]) > 0 for q in range(2))
+    for prec, tol in (("fp64", TOL64), ("fp32", TOL32)):
+        j, g, c = run(p["mu0"], c_data, gpu_backend(cfg, prec))
+        _report(f"config 4 {prec} correlations", rel_l2(c, co), tol)
+        _report(f"config 4 {prec} misfit", abs(j - jo) / abs(jo), tol)
+        _report(f"config 4 {prec} source kernel", rel_l2(g[:, :, 0], go[:, :, 0]), tol)
+        _report(f"config 4 {prec} mu kernel", rel_l2(g[:, :, 1], go[:, :, 1]), tol)

@@ -143,7 +143,7 @@ def test_forward1_arguments_and_outputs(built):
     kind, r = g.last_call()
     assert kind == "forward1"
     _check_cfg(r, g)
-    assert r["precision"] == FP32
+    assert r["precision"] == FP64  # the reference's precision unless FP32 is asked for
     assert r["mu"] == mu.sum() and r["rho"] == rho.sum() and r["src"] == src.sum() and r["rec"] == rec.sum()
     assert (r["ns"], r["nr"], r["mode"]) == (1, 3, 1)
     assert (r["dmu_set"], r["G_in_set"], r["n_G_in"], r["G_out_set"]) == (0, 0, 0, 1)
@@ -278,13 +278,13 @@ def test_errors_carry_fd2d_identifiers(built):
     assert e.value.ident.startswith("fd2d:") and "configuration" in e.value.msg
 
 
-def test_fp64_form_selected_by_environment(built, monkeypatch):
+def test_fp32_form_selected_by_environment(built, monkeypatch):
     # a fresh copy of the gateway: the context is created at its first call
-    path = _build(built["tmp"], "FORWARD1", "forward1_fp64.so")
+    path = _build(built["tmp"], "FORWARD1", "forward1_fp32.so")
     g = Gateway(path)
     g.set_config()
-    monkeypatch.setenv("FD2D_PRECISION", "fp64")
+    monkeypatch.setenv("FD2D_PRECISION", "fp32")
     mu = _ramp((5, 4))
     g.call(1, [g.array(mu), g.array(mu), g.array(np.array([[1e4, 2e4]])), g.array(np.array([[1e3, 2e3]])),
                g.array(0.0), g.array(), g.array(single=True)])
-    assert g.last_call()[1]["precision"] == FP64
+    assert g.last_call()[1]["precision"] == FP32
