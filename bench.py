@@ -199,8 +199,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=40,
+    ap.add_argument("--serve-requests", type=int, default=24,
                     help="requests of the serving measurement (0: skip it)")
+    ap.add_argument("--serve-fp64-s", type=float, default=90.0,
+                    help="the plain FP64 form serves the leading requests of the same stream whose "
+                         "estimated FP64 time (at 1.1 Gpt/s) adds up to this (at least one; 0: skip it)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the configuration-1, -3 and -4 measurements")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="mean Poisson arrival rate [1/s]")
     ap.add_argument("--serve-slots", type=int, default=8, help="concurrent solves of the serving loop")
     ap.add_argument("--no-hbm-probe", action="store_true",
@@ -349,14 +354,24 @@ def main():
         rel = float(torch.linalg.norm(c32 - c64) / torch.linalg.norm(c64))
         result["fp64_plain"] = {"value": v64, "unit": "Gpt-updates/s", "ms_per_station": ms64,
                                 "speedup_fp32_over_fp64": value / world / v64,
-                                "rel_l2_correlations_fp32_vs_fp64": rel}
+                                "rel_l2_correlations_fp32_vs_fp64": rel,
+                                "roofline": fp64_roofline(cfg, ms64, w.spectrum.shape[1])}
         s64.ctx.close()
 
     if rank == 0 and not args.no_e2e:
         result["e2e"] = e2e(args, w, dev)
 
     if rank == 0 and args.serve_requests > 0:
-        result["serving"] = serving_run(args, dev)
+        result["serving"] = serving_run(args, dev, "fp32", args.serve_requests)
+        if args.serve_fp64_s > 0:
+            result["serving_fp64"] = serving_run(args, dev, "fp64", fp64_prefix(args))
+            result["serving_fp64"]["fp32_gpt_per_s_over_fp64"] = (
+                result["serving"]["gpt_per_s"] / result["serving_fp64"]["gpt_per_s"])
+
+    if rank == 0 and not args.no_configs:
+        result["plain_cpu_300"] = config1_run(dev)
+        result["batch_uneven"] = batch_run(dev)
+        result["structure_512"] = structure_run(dev)
 
     if rank == 0 and not args.no_hbm_probe:
         result["roofline_large_grid"] = hbm_probe(args, dev)
@@ -424,87 +439,81 @@ def run_batch_workload(args, w, dev, world, rank):
     """Reference stations on uneven grids in one fd2d_correlation_batch call per
     step (device buffers); stations of one configuration share launches, the
     others run as parallel graph branches."""
-    import numpy as np
     import torch
-    from fd2d_noise_gb300.device import DeviceSession, to_device
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    st0 = w.stations[0]
-    sess = DeviceSession(st0.cfg, dev, "fp32")
-    cache = {}
-    batch = []
-    for s in w.stations:
-        key = id(s.mu)
-        if key not in cache:
-            cache[key] = dict(mu=to_device(s.mu, np.float64, dev), rho=to_device(s.rho, np.float64, dev),
-                              spectrum=to_device(s.spectrum, np.float64, dev),
-                              source_dist=to_device(s.source_dist, np.float64, dev),
-                              rec=to_device(s.receivers, np.float64, dev))
-        c = cache[key]
-        n_dist = s.source_dist.shape[2] if s.source_dist.ndim == 3 else 1
-        batch.append(dict(cfg=s.cfg, mu=c["mu"], rho=c["rho"], spectrum=c["spectrum"], source_dist=c["source_dist"],
-                          n_dist=n_dist, src=to_device(s.ref_stations, np.float64, dev), rec=c["rec"],
-                          nr=s.receivers.shape[0],
-                          out=sess.zeros(s.receivers.shape[0] * s.cfg.ntc, torch.float64)))
-    for _ in range(max(args.warmup, 0)):
-        sess.correlation_batch(batch)
-    torch.cuda.synchronize()
-    clocks = Clocks(dev)
-    launches0 = sess.ctx.kernel_launches
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if world > 1:
         dist.barrier()
-    torch.cuda.synchronize()
+    clocks = Clocks(dev)
     clocks.start()
-    ev0.record(sess.stream)
-    for _ in range(args.steps):
-        sess.correlation_batch(batch)
-    ev1.record(sess.stream)
-    torch.cuda.synchronize()
+    ms, launches, groups, sess, _ = batch_measure(w, dev, args.steps, args.warmup)
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
+    sess.ctx.close()
     if world > 1:
         t = torch.tensor([ms], device=f"cuda:{dev}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     gpt = w.gpt_per_step()
-    value = world * gpt * args.steps / (ms / 1e3) / 1e9
+    value = world * gpt / (ms / 1e3) / 1e9
     sizes = {}
     for s in w.stations:
         sizes[s.cfg.nx] = sizes.get(s.cfg.nx, 0) + 1
     line = {"metric": METRIC, "value": value, "unit": "Gpt-updates/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w.name, "stations": len(w.stations), "grids": sizes,
-                       "gpt_per_step": gpt, "launch_groups": sess.ctx.last_batch(),
+                       "gpt_per_step": gpt, "launch_groups": groups,
                        "l2": "inputs > L2 per step (FP64 Green spectra of every station)"},
-            "gpu_launches": sess.ctx.kernel_launches - launches0, "clocks": clk}
+            "gpu_launches": int(launches * args.steps), "clocks": clk}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
 
 
-def serving_run(args, dev):
-    """Continuous-batching serving loop: a seeded Poisson stream of correlation
-    (60 %), kernel (30 %) and Hessian-vector (10 %) requests, grids 256-384
-    square, nt 800-1600 (stretched to cover the 100-200 s measurement window),
-    1-4 reference stations per correlation request; p50/p99 of arrival-to-result
-    latency."""
+def fp64_prefix(args) -> int:
+    """Leading requests of the serving stream whose FP64 time, estimated at
+    1.1 Gpt/s, adds up to --serve-fp64-s (at least one)."""
+    from fd2d_noise_gb300.serving import make_request_cfg, serving_mix
+    n, acc = 0, 0.0
+    for (_, kind, nx, nt, n_ref, _sd) in serving_mix(args.serve_requests, args.serve_rate):
+        acc += gpt_of_request(kind, make_request_cfg(kind, nx, nt), n_ref) / 1.1e9
+        if n and acc > args.serve_fp64_s:
+            break
+        n += 1
+    return n
+
+
+def gpt_of_request(kind, cfg, n_ref) -> int:
+    runs = {"correlation": cfg.nt + cfg.ntc, "kernel": cfg.nt + cfg.ntc + cfg.ntc + cfg.nt,
+            "hvp": 2 * cfg.nt + 2 * cfg.ntc + 4 * cfg.ntc}[kind]
+    return cfg.npts * runs * n_ref
+
+
+def serving_run(args, dev, precision, n_requests):
+    """Continuous-batching serving loop at the serving configuration's sizes: a
+    seeded Poisson stream (mean --serve-rate req/s) of correlation (60 %),
+    kernel (30 %) and Hessian-vector (10 %) requests on grids 256^2-1024^2
+    (Hessian requests up to 512^2), nt 1000-5000, 1-8 reference stations each,
+    served by ``slots`` concurrent solves with admission by device-memory
+    footprint; p50/p99 of arrival-to-result latency, requests/s and grid-point
+    updates/s.  ``capacity_req_s`` is what the GPU can serve of this mix: the
+    requests over the sum of their run times alone (the first run of each kind,
+    untimed, warms the tables and graphs)."""
     import torch
-    from fd2d_noise_gb300.serving import Server, make_request, poisson_mix
-    mix = poisson_mix(args.serve_requests, args.serve_rate)
+    from fd2d_noise_gb300.serving import Server, make_request, serving_mix
+    mix = serving_mix(n_requests, args.serve_rate)
     reqs = [make_request(kind, nx, nt, n_ref=n_ref, seed=sd) for (_, kind, nx, nt, n_ref, sd) in mix]
     free, _ = torch.cuda.mem_get_info(dev)
     budget = int(free * 0.6)
-    with Server(budget_bytes=budget, slots=args.serve_slots, device=dev) as srv:
-        # warm-up: one request of each kind alone (graph capture, tables)
-        seen = set()
-        for r in reqs:
-            if r.kind not in seen:
-                seen.add(r.kind)
-                srv.submit(r).result()
+    with Server(budget_bytes=budget, slots=args.serve_slots, device=dev, precision=precision) as srv:
+        if precision == "fp32":
+            # warm-up: one request of each kind alone (graph capture, tables)
+            seen = set()
+            for r in reqs:
+                if r.kind not in seen:
+                    seen.add(r.kind)
+                    srv.submit(r).result()
         srv.log.clear()
         srv.peak_running = srv.peak_bytes = 0
         t0 = time.perf_counter()
@@ -521,9 +530,218 @@ def serving_run(args, dev):
     kinds = {}
     for (kind, *_rest) in srv.log:
         kinds[kind] = kinds.get(kind, 0) + 1
-    st.update({"offered_rate_req_s": args.serve_rate, "slots": args.serve_slots, "budget_bytes": budget, "mix": kinds,
-               "workload": "synthetic Poisson stream, grids 256-384, nt 800-1600, 1-4 stations, FP32 form"})
+    grids = sorted({r.cfg.nx for r in reqs})
+    st.update({"precision": precision, "offered_rate_req_s": args.serve_rate, "slots": args.serve_slots,
+               "budget_bytes": budget, "mix": kinds,
+               "workload": (f"synthetic Poisson stream: {len(reqs)} requests, grids {grids[0]}-{grids[-1]} "
+                            f"square, nt {min(r.cfg.nt for r in reqs)}-{max(r.cfg.nt for r in reqs)}, "
+                            f"{min(len(r.ref_stat) for r in reqs)}-{max(len(r.ref_stat) for r in reqs)} "
+                            f"reference stations, {precision} form")})
     return st
+
+
+def fp64_roofline(cfg, ms, n_src=1):
+    """HBM roofline of the plain FP64 form for one station (Green run and
+    correlation run): per update 72 B (Green step) / 88 B (correlation step)
+    of fields and coefficients, plus the reference's per-step K-term sums --
+    a read-modify-write of the FP64 complex spectra (32 B per point and
+    frequency) at every DFT step, and reads of distribution, Re G and Im G
+    (24 B per point, frequency and noise source) at every injection step."""
+    peak, kind = measured_peaks()
+    np_, K, fs = cfg.npts, cfg.n_sample, cfg.freq_samp
+    n_dft = sum(1 for n in range(1, cfg.nt + 1) if (n + cfg.nt - 1) % fs == 0)
+    n_inj = cfg.ntc // fs
+    b = (72 * np_ * cfg.nt + 88 * np_ * cfg.ntc + 32 * np_ * K * n_dft + 24 * np_ * K * n_src * n_inj)
+    achieved = b / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "bytes_per_station": b, "peak_source": f"{kind} hbm_gbs (burst)"}
+
+
+def _time_gpu(fn, stream):
+    """CUDA-event milliseconds of fn() on ``stream`` (after a synchronisation)."""
+    import torch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def config1_run(dev):
+    """Configuration 1 at its full size (300x300, nt 1200, order 4, K 200, one
+    station, 10 receivers): the Green run and the correlation run in the plain
+    FP64 form and the FP32 form on the GPU, the CPU oracle on all host cores,
+    and each GPU form's error against the oracle."""
+    import numpy as np
+    import torch
+    from oracle import pyoracle
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+    from fd2d_noise_gb300.workloads import plain_cpu_300
+    w = plain_cpu_300()
+    cfg, nr = w.cfg, w.receivers.shape[0]
+    gpt = w.gpt_per_station()
+    out = {"workload": w.name, "nx": cfg.nx, "nz": cfg.nz, "nt": cfg.nt, "order": cfg.order,
+           "n_sample": cfg.n_sample, "receivers": nr, "gpt": gpt}
+    pyoracle.build()
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    t0 = time.perf_counter()
+    Go, _, _ = pyoracle.forward1_green(cfg, w.mu, w.rho, w.ref_stations, w.receivers, 0)
+    co, _ = pyoracle.forward2_correlation(cfg, w.mu, w.rho, Go, w.spectrum, w.source_dist, w.receivers, 0)
+    dt = time.perf_counter() - t0
+    del Go
+    out["cpu_oracle"] = {"value": gpt / dt / 1e9, "unit": "Gpt-updates/s", "seconds": dt, "cores": threads,
+                         "kind": "port"}
+    d = {k: to_device(getattr(w, k), np.float64, dev) for k in ("mu", "rho", "spectrum", "source_dist", "receivers")}
+    src = to_device(w.ref_stations, np.float64, dev)
+    for prec in ("fp64", "fp32"):
+        sess = DeviceSession(cfg, dev, prec)
+        G_re, G_im, _, seis = sess.green_outputs(nr)
+        corr = sess.zeros(nr * cfg.ntc, torch.float64)
+
+        def run():
+            sess.forward1_green(d["mu"], d["rho"], src, 1, d["receivers"], nr, G_re, G_im, seis)
+            sess.forward2_correlation(d["mu"], d["rho"], G_re, G_im, d["spectrum"], 1, d["source_dist"], 1,
+                                      d["receivers"], nr, corr)
+        run()  # warm-up: tables, tile shape, graph capture
+        ms = _time_gpu(run, sess.stream)
+        c = corr.cpu().numpy().reshape(nr, cfg.ntc, order="F")
+        out[prec] = {"value": gpt / (ms / 1e3) / 1e9, "unit": "Gpt-updates/s", "ms": ms,
+                     "rel_l2_correlations_vs_oracle": float(np.linalg.norm(c - co) / np.linalg.norm(co))}
+        if prec == "fp64":
+            out[prec]["roofline"] = fp64_roofline(cfg, ms, w.spectrum.shape[1])
+        sess.ctx.close()
+        del G_re, G_im, seis, corr
+    out["speedup_fp32_over_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    out["speedup_fp32_over_cpu"] = out["fp32"]["value"] / out["cpu_oracle"]["value"]
+    torch.cuda.empty_cache()
+    return out
+
+
+def batch_measure(w, dev, steps, warmup):
+    """fd2d_correlation_batch over every station of a BatchWorkload (device
+    buffers, one call per step); returns (ms per step, launches per step,
+    launch groups, the session, the jobs)."""
+    import numpy as np
+    import torch
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+    sess = DeviceSession(w.stations[0].cfg, dev, "fp32")
+    cache, batch = {}, []
+    for s in w.stations:
+        key = id(s.mu)
+        if key not in cache:
+            cache[key] = dict(mu=to_device(s.mu, np.float64, dev), rho=to_device(s.rho, np.float64, dev),
+                              spectrum=to_device(s.spectrum, np.float64, dev),
+                              source_dist=to_device(s.source_dist, np.float64, dev),
+                              rec=to_device(s.receivers, np.float64, dev))
+        c = cache[key]
+        n_dist = s.source_dist.shape[2] if s.source_dist.ndim == 3 else 1
+        batch.append(dict(cfg=s.cfg, mu=c["mu"], rho=c["rho"], spectrum=c["spectrum"], source_dist=c["source_dist"],
+                          n_dist=n_dist, src=to_device(s.ref_stations, np.float64, dev), rec=c["rec"],
+                          nr=s.receivers.shape[0],
+                          out=sess.zeros(s.receivers.shape[0] * s.cfg.ntc, torch.float64)))
+    for _ in range(max(warmup, 0)):
+        sess.correlation_batch(batch)
+    torch.cuda.synchronize()
+    l0 = sess.ctx.kernel_launches
+
+    def run():
+        for _ in range(steps):
+            sess.correlation_batch(batch)
+    ms = _time_gpu(run, sess.stream) / max(steps, 1)
+    return ms, (sess.ctx.kernel_launches - l0) / max(steps, 1), sess.ctx.last_batch(), sess, batch
+
+
+def batch_run(dev, steps=2, warmup=1):
+    """Configuration 3: 32 reference stations on grids of 256-800 points
+    square, nt 1500-4000, order 4, four frequency bands, in one
+    fd2d_correlation_batch call per step; the FP32 correlations of the
+    smallest- and the largest-grid station against the plain FP64 form."""
+    import numpy as np
+    import torch
+    from fd2d_noise_gb300.device import DeviceSession
+    from fd2d_noise_gb300.workloads import batch_uneven
+    w = batch_uneven()
+    ms, launches, groups, sess, batch = batch_measure(w, dev, steps, warmup)
+    gpt = w.gpt_per_step()
+    sizes = {}
+    for s in w.stations:
+        sizes[s.cfg.nx] = sizes.get(s.cfg.nx, 0) + 1
+    errs = {}
+    picks = [min(range(len(w.stations)), key=lambda i: w.stations[i].cfg.npts),
+             max(range(len(w.stations)), key=lambda i: w.stations[i].cfg.npts)]
+    for i in picks:
+        s, j = w.stations[i], batch[i]
+        cfg, nr = s.cfg, s.receivers.shape[0]
+        s64 = DeviceSession(cfg, dev, "fp64")
+        G_re, G_im, _, seis = s64.green_outputs(nr)
+        out = s64.zeros(nr * cfg.ntc, torch.float64)
+        s64.forward1_green(j["mu"], j["rho"], j["src"], 1, j["rec"], nr, G_re, G_im, seis)
+        s64.forward2_correlation(j["mu"], j["rho"], G_re, G_im, j["spectrum"], 1, j["source_dist"], j["n_dist"],
+                                 j["rec"], nr, out)
+        torch.cuda.synchronize()
+        c64, c32 = out.cpu().numpy(), j["out"].cpu().numpy()
+        errs[f"station{i}_{cfg.nx}"] = float(np.linalg.norm(c32 - c64) / np.linalg.norm(c64))
+        s64.ctx.close()
+        del G_re, G_im, seis, out
+    sess.ctx.close()
+    del batch
+    torch.cuda.empty_cache()
+    return {"workload": w.name, "value": gpt / (ms / 1e3) / 1e9, "unit": "Gpt-updates/s", "ms_per_step": ms,
+            "steps": steps, "warmup": warmup, "stations": len(w.stations), "grids": sizes, "gpt_per_step": gpt,
+            "launch_groups": groups, "gpu_launches_per_step": launches,
+            "rel_l2_correlations_fp32_vs_fp64": errs}
+
+
+def structure_run(dev):
+    """Configuration 4: the structure-kernel path on 512x512, nt 2500 --
+    Green (mode 1) + correlation (mode 1), log-amplitude-ratio adjoint
+    sources of 20 receivers around one reference station, adjoint mode 1 and
+    adjoint mode 0 (eval_objective_and_gradient, inversion type 'structure',
+    spectra and snapshot stacks kept on the device) in the FP32 form and the
+    plain FP64 form: seconds, updates/s, and the FP32 misfit and mu kernel
+    against FP64."""
+    import numpy as np
+    import torch
+    from fd2d_noise_gb300.objective import device_backend, eval_objective_and_gradient
+    from fd2d_noise_gb300.workloads import structure_512
+    w = structure_512()
+    cfg = w.cfg
+    arr = np.concatenate([w.ref_stations, w.receivers])
+    t = (-(cfg.nt - 1) + np.arange(cfg.ntc)) * cfg.dt
+    # Green (nt) + correlation (ntc) + adjoint mode 1 (ntc) + adjoint mode 0 (nt: 3-D source)
+    gpt = cfg.npts * (cfg.nt + cfg.ntc + cfg.ntc + cfg.nt)
+
+    def run(mu, c_data, be, only=False):
+        return eval_objective_and_gradient(mu, w.rho, w.spectrum, w.source_dist, w.ref_stations, arr, c_data, t,
+                                           cfg=cfg, type="structure", weighting=1.0, only_objective=only,
+                                           backend=be)
+    be32 = device_backend(cfg, "fp32", dev)
+    _, _, c_data = run(w.mu_true, np.zeros((w.receivers.shape[0], cfg.ntc)), be32, only=True)
+    out = {"workload": w.name, "nx": cfg.nx, "nt": cfg.nt, "fw_nth": cfg.fw_nth, "n_sample": cfg.n_sample,
+           "receivers": int(w.receivers.shape[0]), "gpt": gpt,
+           "runs": "Green mode 1 + correlation mode 1 + adjoint mode 1 + adjoint mode 0"}
+    res = {}
+    for prec, be in (("fp32", be32), ("fp64", device_backend(cfg, "fp64", dev))):
+        if prec == "fp32":
+            run(w.mu, c_data, be)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res[prec] = run(w.mu, c_data, be)
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        out[prec] = {"seconds": sec, "value": gpt / sec / 1e9, "unit": "Gpt-updates/s", "misfit": res[prec][0]}
+        if be.session is not None:
+            be.session.ctx.close()
+    (j32, g32, _), (j64, g64, _) = res["fp32"], res["fp64"]
+    out["rel_misfit_fp32_vs_fp64"] = abs(j32 - j64) / abs(j64)
+    out["rel_l2_mu_kernel_fp32_vs_fp64"] = float(np.linalg.norm(g32[:, :, -1] - g64[:, :, -1]) /
+                                                np.linalg.norm(g64[:, :, -1]))
+    out["speedup_fp32_over_fp64"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
+    torch.cuda.empty_cache()
+    return out
 
 
 def e2e(args, w, dev):

@@ -69,15 +69,16 @@ __device__ __forceinline__ bool taper_is_one(const Grid32& G) {
 
 // Shared-memory layout of one tile (floats, regions 128-byte aligned); the
 // displacement (HU) and injection (HI) regions exist only in the variants
-// that load them.  The new v is written over the old one in place.  Tiles
-// taller than 32 rows read the injection plane straight from L2 (it is only
-// needed point-wise), which keeps four of them resident per SM.
+// that load them.  The new v is written over the old one in place.  Tiles of
+// 32 rows or more read the injection plane straight from L2 (it is only
+// needed point-wise), which keeps five (32 rows) or four (40 rows) of them
+// resident per SM.
 template <int R, bool HU = true, bool HI = true, int TZ_ = 32>
 struct Tile {
   static constexpr int TZ = TZ_;
   // one 4-wide row segment per thread in phase 2, at most 256 threads
   static constexpr int NT = (TX / 4) * TZ < 256 ? (TX / 4) * TZ : 256;
-  static constexpr bool INJ_SMEM = HI && TZ <= 32;
+  static constexpr bool INJ_SMEM = HI && TZ < 32;
   static constexpr int BWc = TX + 2 * R - 1;  // computed v box width (x from x0-R+1)
   static constexpr int BH = TZ + 2 * R - 1;   // box rows (z from z0-R+1)
   static constexpr int SZH = TZ + 4 * R - 2;  // szy rows (z from z0-2R+1)
@@ -99,9 +100,12 @@ struct Tile {
   // reserved, ~1 KB of static shared variables), at most 8
   static constexpr int CTAS = (228 * 1024) / (BYTES + 2048) < 8 ? (228 * 1024) / (BYTES + 2048) : 8;
   // CTAs per SM to ask of the register allocator: the shared-memory limit, but
-  // no fewer than 64 registers per thread (4 CTAs of 256 threads at order 8;
-  // the kernel spills below that)
-  static constexpr int MINB = CTAS < 65536 / (NT * 64) ? CTAS : 65536 / (NT * 64);
+  // no fewer than 64 registers per thread (4 CTAs of 256 threads at order 8)
+  // -- except for 32-row tiles, which run five CTAs per SM within 48
+  // registers without spilling, so that 722 tiles of two 600x600 lanes fit in
+  // one wave of 760 CTAs
+  static constexpr int MINB_64 = CTAS < 65536 / (NT * 64) ? CTAS : 65536 / (NT * 64);
+  static constexpr int MINB = TZ == 32 ? (CTAS < 5 ? CTAS : 5) : MINB_64;
 };
 
 struct alignas(64) StepMaps {

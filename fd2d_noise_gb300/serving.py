@@ -295,6 +295,21 @@ class Server:
                 "peak_concurrent": self.peak_running, "peak_bytes": self.peak_bytes}
 
 
+def make_request_cfg(kind: str, nx: int, nt: int, K: int = 64) -> Config:
+    """Configuration of a synthetic request on an nx-by-nx grid of 4e5 m: dt at
+    Courant number 0.45 for 4000 m/s, nt stretched to cover the 100-200 s
+    measurement window, 4th order, K frequencies in 0.01-0.2 Hz, snapshots
+    every step (Hessian requests) or every 5 steps."""
+    from .config import matlab_colon
+    L = 4.0e5
+    dx = L / (nx - 1)
+    dt = 0.45 * dx / 4000.0
+    nt = max(int(nt), int(np.ceil(130.0 / dt)) + 1)
+    f = matlab_colon(0.01, (0.2 - 0.01) / (K - 1), 0.2)[:K]
+    return Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=dt, nt=nt, order=4, f_sample=f, freq_samp=5,
+                  fw_nth=1 if kind == "hvp" else 5, absorb_width=20 * dx, source_type="gaussian")
+
+
 def make_request(kind: str, nx: int, nt: int, n_ref: int = 1, K: int = 64, nr: int = 8, seed: int = 0,
                  arrival: Optional[float] = None) -> Request:
     """A seeded synthetic request on an nx-by-nx grid of 4e5 m: random medium
@@ -302,16 +317,10 @@ def make_request(kind: str, nx: int, nt: int, n_ref: int = 1, K: int = 64, nr: i
     receivers; kernel and Hessian requests get synthetic data traces.  The
     time axis is stretched so that it covers the 100-200 s measurement window
     (tools/measurement/make_adjoint_sources.m:87-88)."""
-    from .config import Config, matlab_colon
     from .media import interior_points, random_media
     from .noise_source import make_noise_source
-    L = 4.0e5
-    dx = L / (nx - 1)
-    dt = 0.45 * dx / 4000.0
-    nt = max(int(nt), int(np.ceil(130.0 / dt)) + 1)
-    f = matlab_colon(0.01, (0.2 - 0.01) / (K - 1), 0.2)[:K]
-    cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=dt, nt=nt, order=4, f_sample=f, freq_samp=5,
-                 fw_nth=1 if kind == "hvp" else 5, absorb_width=20 * dx, source_type="gaussian")
+    cfg = make_request_cfg(kind, nx, nt, K)
+    L = cfg.Lx
     mu, rho = random_media(cfg, std=0.05, corr_len=2.0e4, seed=seed)
     sd, spec = make_noise_source("gaussian", 0, cfg,
                                  spectrum_kw=dict(f_peak=[0.1], bandwidth=[0.03], strength=[1.0]),
@@ -338,18 +347,41 @@ def make_request(kind: str, nx: int, nt: int, n_ref: int = 1, K: int = 64, nr: i
 
 
 def poisson_mix(n_requests: int, rate: float, seed: int = 6, sizes=(256, 320, 384), nt_range=(800, 1600),
-                mix=(0.6, 0.3, 0.1), max_ref: int = 4):
+                mix=(0.6, 0.3, 0.1), max_ref: int = 4, max_ref_kernel: int = 1, hvp_sizes=None):
     """[(arrival offset s, kind, nx, nt, n_ref, seed)] for a seeded Poisson stream
-    of correlation / kernel / Hessian requests in the proportions ``mix``."""
+    of correlation / kernel / Hessian requests in the proportions ``mix``.
+    Correlation requests have 1..max_ref reference stations, kernel and Hessian
+    requests 1..max_ref_kernel.  Hessian requests store the wavefields of every
+    step (their Born runs read G_in(:,:,i) at each step,
+    code/run_forward1_green.m:140-144), so their grids are drawn from
+    ``hvp_sizes`` (default: the smallest size)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
     kinds = ("correlation", "kernel", "hvp")
+    hvp_sizes = tuple(hvp_sizes) if hvp_sizes else (min(sizes),)
     for i in range(n_requests):
         t += rng.exponential(1.0 / rate)
         kind = kinds[int(rng.choice(3, p=np.asarray(mix) / np.sum(mix)))]
         nx = int(rng.choice(sizes))
         nt = int(rng.integers(nt_range[0], nt_range[1] + 1))
-        n_ref = int(rng.integers(1, max_ref + 1)) if kind == "correlation" else 1
-        out.append((t, kind, nx if kind != "hvp" else min(sizes), nt, n_ref, seed * 1000 + i))
+        top = max_ref if kind == "correlation" else max_ref_kernel
+        n_ref = int(rng.integers(1, top + 1)) if top > 1 else 1
+        if kind == "hvp" and nx not in hvp_sizes:
+            nx = hvp_sizes[0] if len(hvp_sizes) == 1 else int(hvp_sizes[int(rng.integers(len(hvp_sizes)))])
+        out.append((t, kind, nx, nt, n_ref, seed * 1000 + i))
     return out
+
+
+# Request stream of the serving measurement at the sizes of the serving
+# configuration: grids 256^2-1024^2, nt 1000-5000, 1-8 reference stations per
+# request; Hessian-vector requests on grids up to 512^2 (at 1024^2 and nt 5000
+# their every-step wavefield stores alone would need ~380 GB).
+SERVE_SIZES = (256, 384, 512, 640, 768, 896, 1024)
+SERVE_NT = (1000, 5000)
+SERVE_HVP_SIZES = (256, 384, 512)
+
+
+def serving_mix(n_requests: int, rate: float = 50.0, seed: int = 6):
+    return poisson_mix(n_requests, rate, seed=seed, sizes=SERVE_SIZES, nt_range=SERVE_NT, max_ref=8,
+                       max_ref_kernel=8, hvp_sizes=SERVE_HVP_SIZES)

@@ -8,19 +8,23 @@
                             2 reference stations, 40 receivers, random media
                             (10 % std, 20 km correlation length), ring source.
 * ``structure_512``      -- 512x512, nt 2500, snapshots every 5 steps, 200
-                            frequencies, 1 reference station, 20 receivers.
+                            frequencies, 1 reference station, 20 receivers on
+                            a 450 km ring (1e6 m domain), starting and true
+                            models for the misfit.
 * ``large_2048_o8``      -- 2048x2048, order 8, 4 stations, 8 frequencies, nt 200:
                             fields larger than L2 (stencil HBM roofline).
 * ``batch_uneven``       -- 32 reference stations on grids of 256, 384, 512 or
                             800 points square, nt 1500-4000, order 4, 4
                             frequency bands (see :func:`batch_uneven`).
 
-The domain is 4e5 m square in every workload (the reference's "small setup").
+The domain is 4e5 m square (the reference's "small setup") except in
+``structure_512``, whose 1e6 m domain puts the arrivals inside the
+measurement window.
 """
 from __future__ import annotations
 
 import dataclasses
-from typing import Callable, Dict
+from typing import Callable, Dict, Optional
 
 import numpy as np
 
@@ -41,6 +45,7 @@ class Workload:
     receivers: np.ndarray      # nr-by-2
     spectrum: np.ndarray       # K-by-n_src
     source_dist: np.ndarray    # nx-by-nz-by-n_dist
+    mu_true: Optional[np.ndarray] = None  # model of the observed data (structure-kernel workload)
 
     def gpt_green(self) -> int:
         return self.cfg.npts * self.cfg.nt
@@ -88,18 +93,27 @@ def single_600_o8(nt: int = 3000, K: int = 300, n_ref: int = 2, nx: int = 600) -
 
 
 def structure_512(nt: int = 2500) -> Workload:
-    nx = 512
-    dx = L / (nx - 1)
-    cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.5 * dx / 4000.0 * 0.9, nt=nt, order=4,
-                 f_sample=_freqs(0.01, 0.2, 200), freq_samp=5, fw_nth=5, absorb_width=20 * dx)
-    mu, rho = random_media(cfg, std=0.05, corr_len=2.0e4, seed=5)
-    sd, spec = make_noise_source("gaussian", 0, cfg,
-                                 spectrum_kw=dict(f_peak=[0.1], bandwidth=[0.03], strength=[1.0]),
-                                 x_c=[0.3 * L], z_c=[0.6 * L], width=[0.1 * L], magnitude=[6.0])
-    ref = np.array([[0.5 * L, 0.5 * L]])
+    """Structure-kernel workload: 512x512 on a 1e6 m domain, dt 0.2 s, nt 2500,
+    snapshots every 5 steps, 200 frequencies in 0.006-0.028 Hz, 4th order; one
+    reference station in the centre and 20 receivers on a 450 km ring, so the
+    surface waves arrive at ~110 s, inside the 100-200 s window of the
+    log-amplitude-ratio measurement (tools/measurement/make_adjoint_sources.m:
+    85-86).  ``mu`` is the homogeneous starting model, ``mu_true`` the model
+    the observed correlations come from (a 5 % Gaussian anomaly)."""
+    L2, nx = 1.0e6, 512
+    dx = L2 / (nx - 1)
+    cfg = Config(Lx=L2, Lz=L2, nx=nx, nz=nx, dt=0.2, nt=nt, order=4, n_basis_fct=0, fw_nth=5,
+                 f_sample=np.linspace(0.006, 0.028, 200), freq_samp=5, absorb_width=20 * dx)
+    X, Z = np.meshgrid(np.linspace(0, L2, nx), np.linspace(0, L2, nx), indexing="ij")
+    mu = 4.8e10 * np.ones((nx, nx))
     ang = np.linspace(0, 2 * np.pi, 20, endpoint=False)
-    rec = np.stack([0.5 * L + 0.25 * L * np.cos(ang), 0.5 * L + 0.25 * L * np.sin(ang)], axis=1)
-    return Workload("structure_512", cfg, mu, rho, ref, rec, spec, sd)
+    ref = np.array([[0.5e6, 0.5e6]])
+    rec = np.stack([0.5e6 + 0.45e6 * np.cos(ang), 0.5e6 + 0.45e6 * np.sin(ang)], axis=1)
+    spec = np.exp(-(cfg.f_sample - 0.017) ** 2 / 0.008 ** 2).reshape(-1, 1)
+    sd = np.asfortranarray((1 + 5 * np.exp(-((X - 0.3e6) ** 2 + (Z - 0.7e6) ** 2) / 1.5e5 ** 2))[:, :, None])
+    w = Workload("structure_512", cfg, mu, 3000.0 * np.ones((nx, nx)), ref, rec, spec, sd)
+    w.mu_true = mu * (1 + 0.05 * np.exp(-((X - 0.7e6) ** 2 + (Z - 0.55e6) ** 2) / 1.0e5 ** 2))
+    return w
 
 
 def large_2048_o8(nt: int = 200, K: int = 8, n_ref: int = 4) -> Workload:

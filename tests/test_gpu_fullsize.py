@@ -130,26 +130,17 @@ def test_correlations_linear_in_source_distribution(W, dev_inputs):
     assert err <= FP32_TOL, err
 
 
-def _structure_problem():
-    """512x512, nt 2500, snapshots every 5 steps, 200 frequencies, one reference
-    station in the centre and 20 receivers on a 450 km ring: the surface waves
-    arrive at ~110 s, inside the 100-200 s window of the log-amplitude-ratio
-    measurement (tools/measurement/make_adjoint_sources.m:85-86)."""
-    from fd2d_noise_gb300.config import Config
-    L, nx = 1.0e6, 512
-    dx = L / (nx - 1)
-    cfg = Config(Lx=L, Lz=L, nx=nx, nz=nx, dt=0.2, nt=2500, order=4, n_basis_fct=0, fw_nth=5,
-                 f_sample=np.linspace(0.006, 0.028, 200), freq_samp=5, absorb_width=20 * dx)
-    X, Z = np.meshgrid(np.linspace(0, L, nx), np.linspace(0, L, nx), indexing="ij")
-    mu0 = 4.8e10 * np.ones((nx, nx))
-    ang = np.linspace(0, 2 * np.pi, 20, endpoint=False)
-    arr = np.concatenate([[[0.5e6, 0.5e6]], np.stack([0.5e6 + 0.45e6 * np.cos(ang),
-                                                      0.5e6 + 0.45e6 * np.sin(ang)], axis=1)])
-    p = dict(mu0=mu0, rho=3000.0 * np.ones((nx, nx)),
-             mu_true=mu0 * (1 + 0.05 * np.exp(-((X - 0.7e6) ** 2 + (Z - 0.55e6) ** 2) / 1.0e5 ** 2)),
-             spec=np.exp(-(cfg.f_sample - 0.017) ** 2 / 0.008 ** 2).reshape(-1, 1),
-             sd=np.asfortranarray((1 + 5 * np.exp(-((X - 0.3e6) ** 2 + (Z - 0.7e6) ** 2) / 1.5e5 ** 2))[:, :, None]),
-             ref=arr[:1], arr=arr, t=(-(cfg.nt - 1) + np.arange(cfg.ntc)) * cfg.dt)
+def _structure_problem(nt: int = 2500):
+    """The structure-kernel workload (fd2d_noise_gb300.workloads.structure_512):
+    512x512, snapshots every 5 steps, 200 frequencies, one reference station in
+    the centre and 20 receivers on a 450 km ring -- the surface waves arrive at
+    ~110 s, inside the 100-200 s window of the log-amplitude-ratio measurement
+    (tools/measurement/make_adjoint_sources.m:85-86)."""
+    from fd2d_noise_gb300.workloads import structure_512
+    w = structure_512(nt=nt)
+    cfg = w.cfg
+    p = dict(mu0=w.mu, rho=w.rho, mu_true=w.mu_true, spec=w.spectrum, sd=w.source_dist, ref=w.ref_stations,
+             arr=np.concatenate([w.ref_stations, w.receivers]), t=(-(cfg.nt - 1) + np.arange(cfg.ntc)) * cfg.dt)
     return cfg, p
 
 

@@ -39,6 +39,9 @@ def test_structure_512():
     assert w.ref_stations.shape == (1, 2) and w.receivers.shape == (20, 2)
     r = np.hypot(*(w.receivers - w.ref_stations[0]).T)
     assert np.allclose(r, r[0])  # a ring around the reference station
+    # arrivals (~4 km/s) inside the 100-200 s measurement window
+    assert 100.0 < r[0] / 4000.0 < 200.0 and (c.nt - 1) * c.dt >= 200.0
+    assert w.mu_true is not None and w.mu_true.shape == w.mu.shape and np.any(w.mu_true != w.mu)
 
 
 def test_batch_uneven():
