@@ -504,8 +504,10 @@ def serving_run(args, dev, precision, n_requests):
     from fd2d_noise_gb300.serving import Server, make_request, serving_mix
     mix = serving_mix(n_requests, args.serve_rate)
     reqs = [make_request(kind, nx, nt, n_ref=n_ref, seed=sd) for (_, kind, nx, nt, n_ref, sd) in mix]
-    free, _ = torch.cuda.mem_get_info(dev)
-    budget = int(free * 0.6)
+    from fd2d_noise_gb300 import _lib
+    torch.cuda.empty_cache()
+    # free device memory, counting released workspace still held by the pool
+    budget = int(_lib.device_free_bytes(dev) * 0.6)
     with Server(budget_bytes=budget, slots=args.serve_slots, device=dev, precision=precision) as srv:
         if precision == "fp32":
             # warm-up: one request of each kind alone (graph capture, tables)

@@ -34,7 +34,7 @@ EXPORTED = [
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
     "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch", "fd2d_ctx_release", "fd2d_ctx_workspace_bytes",
     "fd2d_gaussblur2d", "fd2d_ctx_set_chunks", "fd2d_ctx_set_tile_rows", "fd2d_ctx_last_tile_rows",
-    "fd2d_ctx_set_shared_gpu",
+    "fd2d_ctx_set_shared_gpu", "fd2d_device_free_bytes",
 ]
 TILE_ROWS_AUTO = 0
 TILE_ROWS_RULE = -1
@@ -98,6 +98,7 @@ def load(path: str = LIB_PATH):
         L.fd2d_ctx_workspace_bytes.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.restype = _i64
         L.fd2d_ctx_release.argtypes = [_vp, ctypes.POINTER(_i64)]
+        L.fd2d_device_free_bytes.argtypes = [_i32, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]
         L.fd2d_gaussblur2d.argtypes = [_vp, _vp, _i32, _i32, _vp, _vp, ctypes.c_double, ctypes.c_double, _vp]
         L.fd2d_last_error.argtypes = [_vp]
         L.fd2d_last_error.restype = ctypes.c_char_p
@@ -215,6 +216,15 @@ class Context:
         u = (_i64 * TIMER_COUNT)()
         check(self.L.fd2d_ctx_timing(self.h, ms, n, u), self.h)
         return [(float(ms[c]), int(n[c]), int(u[c])) for c in range(TIMER_COUNT)]
+
+
+def device_free_bytes(device: int = 0) -> int:
+    """Device memory libfd2d can still allocate (free memory plus the unused
+    part of the device's stream-ordered pool)."""
+    L = load()
+    f, t = _i64(0), _i64(0)
+    check(L.fd2d_device_free_bytes(int(device), ctypes.byref(f), ctypes.byref(t)))
+    return int(f.value)
 
 
 def query_sizes(cfg, nr: int) -> FD2DSizes:

@@ -442,6 +442,36 @@ fd2d_status fd2d_ctx_destroy(fd2d_ctx* ctx) {
   return FD2D_OK;
 }
 
+fd2d_status fd2d_device_free_bytes(int32_t device, int64_t* free_bytes, int64_t* total_bytes) {
+  if (!free_bytes) return set_error(nullptr, FD2D_ERR_ARG, "free_bytes is NULL");
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return set_error(nullptr, FD2D_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  }
+  if (device < 0 || device >= n) return set_error(nullptr, FD2D_ERR_ARG, "device index out of range");
+  int prev = 0;
+  cudaGetDevice(&prev);
+  FD2D_CUDA(nullptr, cudaSetDevice(device));
+  size_t f = 0, t = 0;
+  e = cudaMemGetInfo(&f, &t);
+  if (e == cudaSuccess) {
+    cudaMemPool_t pool;
+    uint64_t reserved = 0, used = 0;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess &&
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+      f += (size_t)(reserved - used);
+    cudaGetLastError();
+  }
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) return set_error(nullptr, FD2D_ERR_CUDA, std::string("cudaMemGetInfo: ") + cudaGetErrorString(e));
+  *free_bytes = (int64_t)f;
+  if (total_bytes) *total_bytes = (int64_t)t;
+  return FD2D_OK;
+}
+
 fd2d_status fd2d_ctx_release(fd2d_ctx* ctx, int64_t* bytes) {
   if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
   cudaSetDevice(ctx->device);

@@ -66,11 +66,15 @@ class Request:
         return c.npts * runs * n_ref
 
 
-def footprint(req: Request) -> int:
-    """Upper bound of the device bytes a request holds while it runs (FP32
-    form): per-lane fields and coefficient planes, the DFT snapshot chunk, FP64
-    spectra, injection planes, and for kernel / Hessian requests the staged
-    snapshot stacks of the Green and correlation runs."""
+def footprint(req: Request, precision: str = "fp32") -> int:
+    """Upper bound of the device bytes a request holds while it runs.  FP32
+    form: per-lane fields and coefficient planes, the DFT snapshot chunk, FP64
+    spectra, injection planes; plain FP64 form (one station at a time): FP64
+    fields and coefficients, spectra and per-frequency distributions of every
+    station of the call.  Kernel / Hessian requests add the staged snapshot
+    stacks of the Green and correlation runs."""
+    if precision == "fp64":
+        return footprint_fp64(req)
     c = req.cfg
     P = (c.nx + 31) // 32 * 32
     plane = ((P * c.nz + 127) // 128 * 128) * 4
@@ -85,6 +89,24 @@ def footprint(req: Request) -> int:
         return int(n_ref * per + (1 << 20))
     snaps = (n_fw_green(c) + n_fw_corr(c)) * np_ * 4
     extra = 2 * snaps + 3 * 16 * np_ * K  # staged inputs and outputs of the adjoint runs
+    if req.kind == "hvp":
+        extra = 3 * extra
+    return int(per + extra + (1 << 20))
+
+
+def footprint_fp64(req: Request) -> int:
+    c = req.cfg
+    np_, K = c.npts, c.n_sample
+    n_ref = np.asarray(req.ref_stat).reshape(-1, 2).shape[0]
+    nr = max(np.asarray(req.receivers).reshape(-1, 2).shape[0], 1)
+    n_dist = max(np.asarray(req.source_dist).size // max(np_, 1), 1)
+    # fields, coefficients, staged model and source maps (FP64), Green spectra
+    # (16 B per point and frequency) and per-frequency distribution (8 B)
+    per = 8 * np_ * (12 + n_dist) + 24 * np_ * K + 8 * nr * (c.nt + c.ntc)
+    if req.kind == "correlation":
+        return int(n_ref * per + (1 << 20))
+    snaps = (n_fw_green(c) + n_fw_corr(c)) * np_ * 4
+    extra = 2 * snaps + 3 * 16 * np_ * K
     if req.kind == "hvp":
         extra = 3 * extra
     return int(per + extra + (1 << 20))
@@ -157,10 +179,11 @@ class _Entry:
 
 class Server:
     def __init__(self, budget_bytes: int, slots: int = 4, device: int = 0, precision: str = "fp32",
-                 max_bypass: int = 4, runner: Optional[Callable] = None, footprint_fn: Callable = footprint,
+                 max_bypass: int = 4, runner: Optional[Callable] = None, footprint_fn: Optional[Callable] = None,
                  contexts: bool = True):
         """``runner(req)`` replaces run_request and ``contexts=False`` skips the
-        per-slot libfd2d contexts (host-only tests of the admission logic)."""
+        per-slot libfd2d contexts (host-only tests of the admission logic);
+        ``footprint_fn(req)`` defaults to the footprint of ``precision``."""
         if slots < 1 or budget_bytes <= 0:
             raise ValueError("need at least one slot and a positive budget")
         self.budget = int(budget_bytes)
@@ -168,7 +191,7 @@ class Server:
         self.max_bypass = max_bypass
         self.device, self.precision = device, precision
         self.runner = runner or (lambda r: run_request(r, precision, device))
-        self.footprint = footprint_fn
+        self.footprint = footprint_fn or (lambda r: footprint(r, precision))
         self.queue: deque = deque()
         self.cv = threading.Condition()
         self.stop = False

@@ -142,8 +142,14 @@ fd2d_status fd2d_ctx_set_shared_gpu(fd2d_ctx* ctx, int32_t shared);
 /* Device memory the context keeps between calls (workspace buffers). */
 int64_t fd2d_ctx_workspace_bytes(const fd2d_ctx* ctx);
 /* Wait for the stream, then free the workspace and the cached CUDA graphs;
- * *bytes (may be NULL) receives the workspace size that was freed. */
+ * *bytes (may be NULL) receives the workspace size that was freed.  Freed
+ * workspace stays in the device's stream-ordered memory pool for reuse. */
 fd2d_status fd2d_ctx_release(fd2d_ctx* ctx, int64_t* bytes);
+/* Device memory the library can still allocate on `device`: the free bytes of
+ * cudaMemGetInfo plus what the device's stream-ordered pool holds unused
+ * (released workspace).  No reference counterpart: admission control of the
+ * serving loop sizes its budget with it. */
+fd2d_status fd2d_device_free_bytes(int32_t device, int64_t* free_bytes, int64_t* total_bytes);
 /* Kernels launched by this context since creation (instrumentation). */
 int64_t fd2d_ctx_kernel_launches(const fd2d_ctx* ctx);
 /* Device-time instrumentation.  When enabled, every launch of the classes

@@ -15,11 +15,10 @@ order-8 / K = 300 tables.
   one station at a time, the FP32 form as the benchmark runs it (both
   stations as lanes of one batch call), and once more with the DFT forced
   into 32-snapshot passes and the injection into 128-event chunks;
-* configuration 4 with nt 1100 (the 100-200 s measurement window still inside
-  the record): 512x512, snapshots every 5 steps, 200 frequencies, 20 receivers
-  around one reference station, log-amplitude-ratio adjoint sources, adjoint
-  modes 1 and 0 through eval_objective_and_gradient (inversion type 'joint':
-  the source kernel and the mu kernel).
+* configuration 4 in full: 512x512, nt 2500, snapshots every 5 steps, 200
+  frequencies, 20 receivers around one reference station, log-amplitude-ratio
+  adjoint sources, adjoint modes 1 and 0 through eval_objective_and_gradient
+  (inversion type 'joint': the source kernel and the mu kernel).
 
 Bars: the plain FP64 form within 1e-10 relative L2 of the oracle on spectra,
 seismograms, correlations, misfit and both kernel planes; the FP32 form within
@@ -150,13 +149,18 @@ def test_config2_fp32_spectra_in_passes_against_oracle(fd2d_lib, oracle, config2
     _report("config 2 fp32 correlations, 128-event injection chunks", rel_l2(c, co), TOL32)
 
 
-def test_config4_reduced_nt_against_oracle(fd2d_lib, oracle):
-    """The structure-kernel workload (512x512, fw 5, K 200, 20 receivers) at
-    nt 1100 through eval_objective_and_gradient, inversion type 'joint'."""
+def test_config4_full_size_against_oracle(fd2d_lib, oracle):
+    """The structure-kernel workload (512x512, nt 2500, fw 5, K 200, 20
+    receivers) through eval_objective_and_gradient, inversion type 'joint'.
+    (At nt 1100 the same chain gave FP32 errors of 5.7e-5 on the misfit and
+    2.1e-4 on the mu kernel: the misfit 0.5 (A - A0)^2 and the adjoint sources,
+    proportional to A - A0 (tools/measurement/log_amp_ratio.m), carry the
+    FP32 error of the log energy ratio A relative to A - A0, and that
+    difference depends on the record length.)"""
     from tests.test_gpu_fullsize import _structure_problem
     from tests.test_objective import oracle_backend
     from fd2d_noise_gb300.objective import eval_objective_and_gradient, gpu_backend
-    cfg, p = _structure_problem(nt=1100)
+    cfg, p = _structure_problem()
     t = p["t"]
 
     def run(mu, c_data, backend, only=False):
