@@ -187,8 +187,9 @@ class Context:
         return int(self.L.fd2d_ctx_workspace_bytes(self.h))
 
     def set_tile_rows(self, rows: int):
-        """Step-kernel tile rows: 16 or 32 forced, TILE_ROWS_AUTO (0) timed per
-        grid when the stream is idle, TILE_ROWS_RULE (-1) by grid size only."""
+        """Step-kernel tile rows: 16, 30, 32 or 40 forced, TILE_ROWS_AUTO (0)
+        timed per grid when the stream is idle, TILE_ROWS_RULE (-1) by grid size
+        only."""
         check(self.L.fd2d_ctx_set_tile_rows(self.h, int(rows)), self.h)
 
     def set_shared_gpu(self, shared: bool):

@@ -898,8 +898,10 @@ extern "C" fd2d_status fd2d_ctx_set_chunks(fd2d_ctx* ctx, int32_t max_snapshots,
 
 extern "C" fd2d_status fd2d_ctx_set_tile_rows(fd2d_ctx* ctx, int32_t rows) {
   if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
-  if (rows != FD2D_TILE_ROWS_AUTO && rows != FD2D_TILE_ROWS_RULE && rows != 16 && rows != 32 && rows != 40)
-    return set_error(ctx, FD2D_ERR_ARG, "tile rows must be 16, 32, 40, FD2D_TILE_ROWS_AUTO or FD2D_TILE_ROWS_RULE");
+  if (rows != FD2D_TILE_ROWS_AUTO && rows != FD2D_TILE_ROWS_RULE && rows != 16 && rows != 30 && rows != 32 &&
+      rows != 40)
+    return set_error(ctx, FD2D_ERR_ARG,
+                     "tile rows must be 16, 30, 32, 40, FD2D_TILE_ROWS_AUTO or FD2D_TILE_ROWS_RULE");
   ctx->tile_rows = rows;
   return FD2D_OK;
 }

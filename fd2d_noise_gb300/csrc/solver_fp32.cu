@@ -40,11 +40,12 @@
 namespace fd2d {
 namespace {
 
-// Tiles are TX = 32 points wide and TZ rows high; TZ is 16 or 32 (chosen per
-// grid and lane count by tune_tile_rows), with TX/4 * TZ threads per CTA.
+// Tiles are TX = 32 points wide and TZ rows high; TZ is 16, 30, 32 or 40
+// (chosen per grid and lane count by tune_tile_rows), with TX/4 * TZ threads
+// per CTA.
 constexpr int TX = 32;
-constexpr int N_TILE_ROWS = 3;
-constexpr int TILE_ROWS[N_TILE_ROWS] = {16, 32, 40};
+constexpr int N_TILE_ROWS = 4;
+constexpr int TILE_ROWS[N_TILE_ROWS] = {16, 30, 32, 40};
 constexpr int MAX_BOX_SRC = 64;
 constexpr int MAX_TILE_REC = 32;  // receivers of one tile kept in shared memory
 
@@ -70,15 +71,15 @@ __device__ __forceinline__ bool taper_is_one(const Grid32& G) {
 // Shared-memory layout of one tile (floats, regions 128-byte aligned); the
 // displacement (HU) and injection (HI) regions exist only in the variants
 // that load them.  The new v is written over the old one in place.  Tiles of
-// 32 rows or more read the injection plane straight from L2 (it is only
-// needed point-wise), which keeps five (32 rows) or four (40 rows) of them
+// 30 rows or more read the injection plane straight from L2 (it is only
+// needed point-wise), which keeps five (30, 32 rows) or four (40 rows) of them
 // resident per SM.
 template <int R, bool HU = true, bool HI = true, int TZ_ = 32>
 struct Tile {
   static constexpr int TZ = TZ_;
   // one 4-wide row segment per thread in phase 2, at most 256 threads
   static constexpr int NT = (TX / 4) * TZ < 256 ? (TX / 4) * TZ : 256;
-  static constexpr bool INJ_SMEM = HI && TZ < 32;
+  static constexpr bool INJ_SMEM = HI && TZ < 30;
   static constexpr int BWc = TX + 2 * R - 1;  // computed v box width (x from x0-R+1)
   static constexpr int BH = TZ + 2 * R - 1;   // box rows (z from z0-R+1)
   static constexpr int SZH = TZ + 4 * R - 2;  // szy rows (z from z0-2R+1)
@@ -101,11 +102,12 @@ struct Tile {
   static constexpr int CTAS = (228 * 1024) / (BYTES + 2048) < 8 ? (228 * 1024) / (BYTES + 2048) : 8;
   // CTAs per SM to ask of the register allocator: the shared-memory limit, but
   // no fewer than 64 registers per thread (4 CTAs of 256 threads at order 8)
-  // -- except for 32-row tiles, which run five CTAs per SM within 48
-  // registers without spilling, so that 722 tiles of two 600x600 lanes fit in
-  // one wave of 760 CTAs
+  // -- except for 30- and 32-row tiles, which run five CTAs per SM within 48
+  // registers without spilling: two 600x600 lanes are 760 tiles of 32x30,
+  // exactly five on each of the 152 SMs (722 tiles of 32x32 leave 38 SMs with
+  // four while the step waits for the SMs with five)
   static constexpr int MINB_64 = CTAS < 65536 / (NT * 64) ? CTAS : 65536 / (NT * 64);
-  static constexpr int MINB = TZ == 32 ? (CTAS < 5 ? CTAS : 5) : MINB_64;
+  static constexpr int MINB = (TZ == 30 || TZ == 32) ? (CTAS < 5 ? CTAS : 5) : MINB_64;
 };
 
 struct alignas(64) StepMaps {
@@ -710,6 +712,7 @@ void launch_step_t(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
 template <int R, bool HU, bool HI>
 void launch_step_v(fd2d_ctx* ctx, const Run& r, int par, const Step32& s) {
   if (r.tz == 16) launch_step_t<R, HU, HI, 16>(ctx, r, par, s);
+  else if (r.tz == 30) launch_step_t<R, HU, HI, 30>(ctx, r, par, s);
   else if (r.tz == 40) launch_step_t<R, HU, HI, 40>(ctx, r, par, s);
   else launch_step_t<R, HU, HI, 32>(ctx, r, par, s);
 }
@@ -742,6 +745,7 @@ fd2d_status step_attributes_t(fd2d_ctx* ctx) {
 template <int R>
 fd2d_status step_attributes_r(fd2d_ctx* ctx) {
   FD2D_TRY((step_attributes_t<R, 16>(ctx)));
+  FD2D_TRY((step_attributes_t<R, 30>(ctx)));
   FD2D_TRY((step_attributes_t<R, 40>(ctx)));
   return step_attributes_t<R, 32>(ctx);
 }
@@ -905,7 +909,8 @@ int step_ctas_t() {
 
 template <int R>
 int step_ctas_r(int tz) {
-  return tz == 16 ? step_ctas_t<R, 16>() : tz == 40 ? step_ctas_t<R, 40>() : step_ctas_t<R, 32>();
+  return tz == 16 ? step_ctas_t<R, 16>() : tz == 30 ? step_ctas_t<R, 30>()
+                  : tz == 40 ? step_ctas_t<R, 40>() : step_ctas_t<R, 32>();
 }
 
 int step_ctas(int R, int tz) {

@@ -120,8 +120,8 @@ fd2d_status fd2d_ctx_synchronize(fd2d_ctx* ctx);
  * in two FP32 halves and the chunks in FP64: longer chunks lose FP32 accuracy
  * (the default keeps FP32 mu kernels within 1e-4 of FP64 at nt 2500). */
 fd2d_status fd2d_ctx_set_chunks(fd2d_ctx* ctx, int32_t max_snapshots, int32_t max_injection_planes);
-/* Tile rows of the FP32 step kernel (tiles are 32 points wide): 16, 32 or 40
- * to force a shape; FD2D_TILE_ROWS_AUTO (0, default) to time every shape once
+/* Tile rows of the FP32 step kernel (tiles are 32 points wide): 16, 30, 32 or
+ * 40 to force a shape; FD2D_TILE_ROWS_AUTO (0, default) to time every shape once
  * per context for each grid, FD order and lane count when the stream is idle
  * and keep the fastest (the size rule otherwise); FD2D_TILE_ROWS_RULE (-1) for
  * the size rule only (fewest waves of resident CTAs, the shortest tiles among
