@@ -68,6 +68,17 @@ __device__ __forceinline__ bool taper_is_one(const Grid32& G) {
          (int)blockIdx.y <= G.t1z1;
 }
 
+// Rows of the first part of a tile's field loads: the box rows the first
+// round of phase-1 items covers (NT items of `quads` per row), rounded up to a
+// multiple of 4 so that the second part starts 128-byte aligned in shared
+// memory (rows are 160 or 192 bytes); and the szy rows those box rows read.
+__host__ __device__ constexpr int split_top_rows(int nt, int quads, int bh) {
+  return ((nt + quads - 1) / quads + 3) / 4 * 4 < bh ? ((nt + quads - 1) / quads + 3) / 4 * 4 : bh - 1;
+}
+__host__ __device__ constexpr int split_top_szy(int h1, int r, int szh) {
+  return (h1 + 2 * r - 1 + 3) / 4 * 4 < szh ? (h1 + 2 * r - 1 + 3) / 4 * 4 : szh;
+}
+
 // Shared-memory layout of one tile (floats, regions 128-byte aligned); the
 // displacement (HU) and injection (HI) regions exist only in the variants
 // that load them.  The new v is written over the old one in place.  Tiles of
@@ -80,6 +91,9 @@ struct Tile {
   // one 4-wide row segment per thread in phase 2, at most 256 threads
   static constexpr int NT = (TX / 4) * TZ < 256 ? (TX / 4) * TZ : 256;
   static constexpr bool INJ_SMEM = HI && TZ < 30;
+  // otherwise interior tiles (taper all ones) load the injection box into the
+  // taper region, and edge tiles read it from L2
+  static constexpr bool INJ_IN_T = HI && !INJ_SMEM;
   static constexpr int BWc = TX + 2 * R - 1;  // computed v box width (x from x0-R+1)
   static constexpr int BH = TZ + 2 * R - 1;   // box rows (z from z0-R+1)
   static constexpr int SZH = TZ + 4 * R - 2;  // szy rows (z from z0-2R+1)
@@ -96,6 +110,13 @@ struct Tile {
   static constexpr int O_U = O_MU + al(TZ * TX);
   static constexpr int TOTAL = O_U + (HU ? al(TZ * TX) : 0);
   static_assert(BH + 2 * R - 1 <= SZH, "the z sum of the last box row stays inside the szy rows");
+  // The field boxes arrive in two parts with a barrier each: rows [0, H1) of
+  // sxy and v and rows [0, H1Z) of szy (everything the first round of
+  // phase-1 items reads), then the rest and u, so the first round computes
+  // while the second part is still in flight.
+  static constexpr int H1 = split_top_rows(NT, BWa / 4, BH);
+  static constexpr int H1Z = split_top_szy(H1, R, SZH);
+  static_assert(H1 > 0 && H1 < BH && H1Z > 0 && H1Z <= SZH, "two-part field loads");
   static constexpr int BYTES = TOTAL * 4 + 128;      // + alignment slack
   // resident CTAs per SM the shared memory allows (228 KB per SM, 1 KB per CTA
   // reserved, ~1 KB of static shared variables), at most 8
@@ -110,8 +131,10 @@ struct Tile {
   static constexpr int MINB = (TZ == 30 || TZ == 32) ? (CTAS < 5 ? CTAS : 5) : MINB_64;
 };
 
+// Field maps come in pairs: the top part (rows [0, H1) of the box, [0, H1Z)
+// of szy) and the bottom part of the tile's boxes.
 struct alignas(64) StepMaps {
-  CUtensorMap sxy, szy, v, u, b, taper, dtmu, inj;
+  CUtensorMap sxy_t, sxy_b, szy_t, szy_b, v_t, v_b, u, b, taper, dtmu, inj;
 };
 
 // Per-step arguments.  Arrays marked "per lane" hold lane l's part at the
@@ -151,23 +174,34 @@ __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, c
   using T = Tile<R, HU, HI, TZ>;
   int x0, z0, lane;
   tile_coords<R, TZ>(G, t, x0, z0, lane);
-  const int bz0 = z0 - R + 1;
+  const int bz0 = z0 - R + 1, zz0 = z0 - 2 * R + 1;
   if (coeffs) {
+    // Coefficient planes and the injection plane are not written by the time
+    // loop, so they load before the wait for the previous step.  Tiles whose
+    // taper is all ones do not load it; the injection box takes its place.
     const bool t1 = taper_is_one(G);
-    uint32_t bytes = 4u * (T::BH * T::SXWa + T::SZH * T::BWa + (t1 ? 2 : 3) * T::BH * T::BWa + TZ * TX);
-    if (HU) bytes += 4u * TZ * TX;
-    if (T::INJ_SMEM) bytes += 4u * T::BH * T::BWa;
-    mbar_expect_tx(bar, bytes);
-    tma_load_3d(buf + T::O_B, &M.b, x0 - 4, bz0, lane, bar);
-    if (!t1) tma_load_3d(buf + T::O_T, &M.taper, x0 - 4, bz0, lane, bar);
-    tma_load_3d(buf + T::O_MU, &M.dtmu, x0, z0, lane, bar);
+    const bool inj_t = T::INJ_IN_T && t1;
+    uint32_t b0 = 4u * (T::BH * T::BWa + TZ * TX + T::H1 * T::SXWa + T::H1Z * T::BWa + T::H1 * T::BWa);
+    if (!t1) b0 += 4u * T::BH * T::BWa;
+    if (T::INJ_SMEM || inj_t) b0 += 4u * T::BH * T::BWa;
+    uint32_t b1 = 4u * ((T::BH - T::H1) * (T::SXWa + T::BWa) + (T::SZH - T::H1Z) * T::BWa);
+    if (HU) b1 += 4u * TZ * TX;
+    mbar_expect_tx(&bar[0], b0);
+    mbar_expect_tx(&bar[1], b1);
+    tma_load_3d(buf + T::O_B, &M.b, x0 - 4, bz0, lane, &bar[0]);
+    if (!t1) tma_load_3d(buf + T::O_T, &M.taper, x0 - 4, bz0, lane, &bar[0]);
+    tma_load_3d(buf + T::O_MU, &M.dtmu, x0, z0, lane, &bar[0]);
+    if (T::INJ_SMEM) tma_load_3d(buf + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, &bar[0]);
+    else if (inj_t) tma_load_3d(buf + T::O_T, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, &bar[0]);
   }
   if (fields) {
-    tma_load_3d(buf + T::O_SXY, &M.sxy, x0 - 8, bz0, lane, bar);
-    tma_load_3d(buf + T::O_SZY, &M.szy, x0 - 4, z0 - 2 * R + 1, lane, bar);
-    tma_load_3d(buf + T::O_V, &M.v, x0 - 4, bz0, lane, bar);
-    if (HU) tma_load_3d(buf + T::O_U, &M.u, x0, z0, lane, bar);
-    if (T::INJ_SMEM) tma_load_3d(buf + T::O_I, &M.inj, x0 - 4, bz0, S.inj_plane * G.S + lane, bar);
+    tma_load_3d(buf + T::O_SXY, &M.sxy_t, x0 - 8, bz0, lane, &bar[0]);
+    tma_load_3d(buf + T::O_SZY, &M.szy_t, x0 - 4, zz0, lane, &bar[0]);
+    tma_load_3d(buf + T::O_V, &M.v_t, x0 - 4, bz0, lane, &bar[0]);
+    tma_load_3d(buf + T::O_SXY + T::H1 * T::SXWa, &M.sxy_b, x0 - 8, bz0 + T::H1, lane, &bar[1]);
+    if (T::SZH > T::H1Z) tma_load_3d(buf + T::O_SZY + T::H1Z * T::BWa, &M.szy_b, x0 - 4, zz0 + T::H1Z, lane, &bar[1]);
+    tma_load_3d(buf + T::O_V + T::H1 * T::BWa, &M.v_b, x0 - 4, bz0 + T::H1, lane, &bar[1]);
+    if (HU) tma_load_3d(buf + T::O_U, &M.u, x0, z0, lane, &bar[1]);
   }
 }
 
@@ -186,7 +220,7 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
 #define inv_dx G.inv_dx
 #define inv_dz G.inv_dz
 #define gdt G.dt
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bar[2];  // top part (+ coefficients), bottom part (+ u)
   __shared__ int s_src[MAX_BOX_SRC];
   __shared__ float s_amp[MAX_BOX_SRC];
   __shared__ int s_nsrc;
@@ -206,17 +240,18 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
   if (tid == 0) {
     s_nsrc = 0;
     s_nrec = 0;
-    mbar_init(&bar, 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
     fence_mbar_init();
     // coefficient planes are not written by the time loop: their loads may
     // overlap the end of the previous step (programmatic dependent launch)
-    issue_tile<R, HU, HI, TZ>(G, M, S, sm, &bar, t, true, false);
+    issue_tile<R, HU, HI, TZ>(G, M, S, sm, bar, t, true, false);
     // The fields are what the previous launch wrote (or will write what it
     // read: ping-pong buffers): wait for it to complete, then load them.  The
     // other threads touch those buffers only after this tile's loads land, so
     // this thread's wait orders the whole CTA after the previous step.
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    issue_tile<R, HU, HI, TZ>(G, M, S, sm, &bar, t, false, true);
+    issue_tile<R, HU, HI, TZ>(G, M, S, sm, bar, t, false, true);
   }
   {
     const float* buf = sm;
@@ -248,16 +283,22 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
         }
       }
     }
-    // one warp waits for the tile (suspending); the others wait at the barrier
+    // one warp waits for the top part of the tile (suspending); the others
+    // wait at the barrier
     bool ok = true;
-    if (tid < 32) ok = mbar_wait_bounded_sleep(&bar, 0);
+    if (tid < 32) ok = mbar_wait_bounded_sleep(&bar[0], 0);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         set_error_flag(G.err, 1);
-        mbar_wait_bounded_sleep(&bar, 0, 100000000ull);  // let started copies land (bounded)
+        // let started copies land (bounded)
+        mbar_wait_bounded_sleep(&bar[0], 0, 100000000ull);
+        mbar_wait_bounded_sleep(&bar[1], 0, 100000000ull);
       }
       return;
     }
+    // the bottom part: waited for by every thread with a second-round
+    // phase-1 item before it, and by warp 0 before phase 2
+    bool ok1 = true, waited1 = false, bad = false;
     // the tile is in shared memory: the next step may launch and run its
     // prologue (its own wait orders it after this grid's stores)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -289,6 +330,11 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
       constexpr int NB1 = 1;
       constexpr int NQ = W / 4, NRB = (T::BH + NB1 - 1) / NB1;
       for (int item = tid; item < NQ * NRB; item += NT) {
+        if (item >= NT && !waited1) {
+          ok1 = mbar_wait_bounded_sleep(&bar[1], 0);
+          waited1 = true;
+        }
+        if (!ok1) break;
         const int q = item % NQ, r0 = NB1 * (item / NQ);
         const int c0 = 4 * q;  // box column of element 0; global x = vx0 + c0 + e
         float zs[2 * R + NB1 - 1][4];
@@ -362,6 +408,8 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
           float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
           if (T::INJ_SMEM) {
             i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
+          } else if (inj && t1) {
+            i4 = *reinterpret_cast<const float4*>(s_t + rr * W + c0);  // the injection box (issue_tile)
           } else if (inj) {
             // from L2; outside the grid the plane is zero (as the TMA fill)
             const int gx0 = vx0 + c0;
@@ -391,7 +439,15 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
         }
       }
     }
-    __syncthreads();
+    if (tid < 32 && !waited1) ok1 = mbar_wait_bounded_sleep(&bar[1], 0);
+    if (__syncthreads_or(!ok1)) {
+      if (tid == 0) {
+        set_error_flag(G.err, 1);
+        mbar_wait_bounded_sleep(&bar[1], 0, 100000000ull);  // let started copies land (bounded)
+      }
+      bad = true;
+      return;
+    }
 
     // ---- stress, displacement and outputs: each thread 4-wide row segments -----------
     constexpr int NQ2 = TX / 4;  // 8 quads per row
@@ -494,6 +550,7 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
       compute(std::true_type{});
     else
       compute(std::false_type{});
+    if (bad) return;
     if (S.nrec && s_nrec < 0) {
       // more receivers in this tile than the shared list holds: read them back
       __syncthreads();
@@ -790,14 +847,21 @@ fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, int par, Step32 s) {
 fd2d_status make_maps(fd2d_ctx* ctx, Run& r) {
   const int nx = r.G.nx, nz = r.G.nz, P = r.G.P, R = r.R, TZ = r.tz;
   const int BH = TZ + 2 * R - 1, SZH = TZ + 4 * R - 2, BWa = TX + 8, SXWa = TX + 16;
+  // the two parts of the field boxes (Tile::H1, Tile::H1Z)
+  const int NT = std::min(TX / 4 * TZ, 256);
+  const int H1 = split_top_rows(NT, BWa / 4, BH), H1Z = split_top_szy(H1, R, SZH);
   for (int q = 0; q < 2; ++q) {
     StepMaps& m = r.maps[q];
     // lanes are the third dimension (plane stride ps)
     const int S = r.S;
     const int64_t ps = r.ps;
-    FD2D_TRY(make_tmap_f32(ctx, &m.sxy, r.sxy[q], nx, nz, P, SXWa, BH, S, ps));
-    FD2D_TRY(make_tmap_f32(ctx, &m.szy, r.szy[q], nx, nz, P, BWa, SZH, S, ps));
-    FD2D_TRY(make_tmap_f32(ctx, &m.v, r.v[q], nx, nz, P, BWa, BH, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.sxy_t, r.sxy[q], nx, nz, P, SXWa, H1, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.sxy_b, r.sxy[q], nx, nz, P, SXWa, BH - H1, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.szy_t, r.szy[q], nx, nz, P, BWa, H1Z, S, ps));
+    // (no bottom szy part when the top part holds every row; the map is then unused)
+    FD2D_TRY(make_tmap_f32(ctx, &m.szy_b, r.szy[q], nx, nz, P, BWa, std::max(SZH - H1Z, 1), S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.v_t, r.v[q], nx, nz, P, BWa, H1, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.v_b, r.v[q], nx, nz, P, BWa, BH - H1, S, ps));
     FD2D_TRY(make_tmap_f32(ctx, &m.u, r.u[q] ? r.u[q] : r.v[q], nx, nz, P, TX, TZ, S, ps));
     FD2D_TRY(make_tmap_f32(ctx, &m.b, r.b, nx, nz, P, BWa, BH, S, ps));
     FD2D_TRY(make_tmap_f32(ctx, &m.taper, r.taper, nx, nz, P, BWa, BH, S, ps));

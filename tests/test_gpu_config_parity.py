@@ -21,10 +21,9 @@ order-8 / K = 300 tables.
   (inversion type 'joint': the source kernel and the mu kernel).
 
 Bars: the plain FP64 form within 1e-10 relative L2 of the oracle on spectra,
-seismograms, correlations, misfit and both kernel planes; the FP32 form within
-1e-4 on spectra, seismograms, correlations, misfit and the mu kernel, and
-within 1e-3 on the source kernel (see the configuration-4 test); every error
-is printed.
+seismograms, correlations, misfit and both kernel planes (the mu kernel of
+configuration 4: within twice its own one-ulp sensitivity, see that test);
+the FP32 form within 1e-4; every error is printed.
 """
 import numpy as np
 import pytest
@@ -35,7 +34,6 @@ pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-10
 TOL32 = 1e-4
-SOURCE_KERNEL_TOL32 = 1e-3
 
 
 def _report(label, err, tol):
@@ -152,40 +150,52 @@ def test_config2_fp32_spectra_in_passes_against_oracle(fd2d_lib, oracle, config2
 def test_config4_full_size_against_oracle(fd2d_lib, oracle):
     """The structure-kernel workload (512x512, nt 2500, fw 5, K 200, 20
     receivers) through eval_objective_and_gradient, inversion type 'joint'.
-    (At nt 1100 the same chain gave FP32 errors of 5.7e-5 on the misfit and
-    2.1e-4 on the mu kernel: the misfit 0.5 (A - A0)^2 and the adjoint sources,
-    proportional to A - A0 (tools/measurement/log_amp_ratio.m), carry the
-    FP32 error of the log energy ratio A relative to A - A0, and that
-    difference depends on the record length.)"""
+
+    The mu kernel of this chain is sensitive to rounding at the 1e-10 level
+    in the reference's own arithmetic: the oracle with rho multiplied by
+    (1 + 2^-52) moves its mu kernel by 1.2e-10 relative L2 (the forward
+    wavefields are stored as single() snapshots, and K_mu is built from their
+    derivatives).  So every FP64 quantity q must be within
+    max(1e-10, 2 S(q)) of the oracle, where S(q) is the change the same
+    one-ulp perturbation of rho causes in the plain FP64 GPU form itself; for
+    every quantity but the mu kernel that is the 1e-10 bar.  (At nt 1100 the
+    same chain gave FP32 errors of 5.7e-5 on the misfit and 2.1e-4 on the mu
+    kernel: the misfit 0.5 (A - A0)^2 and the adjoint sources, proportional to
+    A - A0 (tools/measurement/log_amp_ratio.m), carry the FP32 error of the
+    log energy ratio A relative to A - A0, and that difference depends on the
+    record length.)"""
     from tests.test_gpu_fullsize import _structure_problem
     from tests.test_objective import oracle_backend
     from fd2d_noise_gb300.objective import eval_objective_and_gradient, gpu_backend
     cfg, p = _structure_problem()
     t = p["t"]
 
-    def run(mu, c_data, backend, only=False):
-        return eval_objective_and_gradient(mu, p["rho"], p["spec"], p["sd"], p["ref"], p["arr"], c_data, t,
-                                           cfg=cfg, backend=backend, weighting=1.0, only_objective=only,
-                                           type="joint")
+    def run(mu, c_data, backend, only=False, rho=None):
+        return eval_objective_and_gradient(mu, p["rho"] if rho is None else rho, p["spec"], p["sd"], p["ref"],
+                                           p["arr"], c_data, t, cfg=cfg, backend=backend, weighting=1.0,
+                                           only_objective=only, type="joint")
+
+    def errs_of(j, g, c, jr, gr, cr):
+        return {"correlations": rel_l2(c, cr), "misfit": abs(j - jr) / abs(jr),
+                "source kernel": rel_l2(g[:, :, 0], gr[:, :, 0]), "mu kernel": rel_l2(g[:, :, 1], gr[:, :, 1])}
 
     # observed correlations from the perturbed medium (the plain FP64 form;
     # both sides of the comparison get the same data)
-    _, _, c_data = run(p["mu_true"], np.zeros((20, cfg.ntc)), gpu_backend(cfg, "fp64"), only=True)
+    be64 = gpu_backend(cfg, "fp64")
+    _, _, c_data = run(p["mu_true"], np.zeros((20, cfg.ntc)), be64, only=True)
     jo, go, co = run(p["mu0"], c_data, oracle_backend(cfg))
     assert jo > 0 and go.shape[2] == 2
     assert all(np.linalg.norm(go[:, :, q]) > 0 for q in range(2))
-    errs = {}
+    out = {}
     for prec in ("fp64", "fp32"):
-        j, g, c = run(p["mu0"], c_data, gpu_backend(cfg, prec))
-        errs[prec] = {"correlations": rel_l2(c, co), "misfit": abs(j - jo) / abs(jo),
-                      "source kernel": rel_l2(g[:, :, 0], go[:, :, 0]), "mu kernel": rel_l2(g[:, :, 1], go[:, :, 1])}
+        out[prec] = run(p["mu0"], c_data, gpu_backend(cfg, prec))
+    errs = {prec: errs_of(*out[prec], jo, go, co) for prec in out}
+    sens = errs_of(*run(p["mu0"], c_data, be64, rho=p["rho"] * (1 + 2.0 ** -52)), *out["fp64"])
+    for prec in ("fp64", "fp32"):
         for k, e in errs[prec].items():
-            print(f"config 4 {prec} {k}: rel L2 {e:.3e}")
+            extra = f" (one-ulp sensitivity of the FP64 form {sens[k]:.3e})" if prec == "fp64" else ""
+            print(f"config 4 {prec} {k}: rel L2 {e:.3e}{extra}")
     for k, e in errs["fp64"].items():
-        assert e <= TOL64, ("fp64", k, e)
-    # 1e-4 is the FP32 bar of correlations and mu kernels.  The source kernel
-    # (code/run_noise_adjoint.m:302-320) is a per-pixel sum over frequencies of
-    # Green spectrum times adjoint spectrum, both from FP32 wavefields, so the
-    # errors of the two spectra add in it; it gets SOURCE_KERNEL_TOL32.
+        assert e <= max(TOL64, 2 * sens[k]), ("fp64", k, e, sens[k])
     for k, e in errs["fp32"].items():
-        assert e <= (SOURCE_KERNEL_TOL32 if k == "source kernel" else TOL32), ("fp32", k, e)
+        assert e <= TOL32, ("fp32", k, e)
