@@ -158,10 +158,11 @@ namespace fd2d {
 
 // Snapshots per DFT contraction unless fd2d_ctx_set_chunks says otherwise.  A
 // chunk is summed in two halves, each in FP32 in tensor memory, and the chunks
-// in FP64, so every FP32 sum covers at most 256 snapshots: the FP32 mu kernel
-// of a 512x512, nt 2500 structure-kernel run is then within 1e-4 of the FP64
-// form (1.4e-4 with one FP32 sum over all 500 snapshots).
-constexpr int DFT_CHUNK_DEFAULT = 512;
+// in FP64, so every FP32 sum covers at most 320 snapshots: the FP32 mu kernel
+// of a 512x512, nt 2500 structure-kernel run (500 snapshots, halves of 250)
+// is then within 1e-4 of the FP64 form (1.4e-4 with one FP32 sum over all
+// 500), and the 600 snapshots of an nt 3000 Green run take one pass.
+constexpr int DFT_CHUNK_DEFAULT = 640;
 
 // Returns a device buffer of at least `bytes` under `name` (grown when needed).
 fd2d_status workspace(fd2d_ctx* ctx, const char* name, size_t bytes, void** out);

@@ -81,7 +81,7 @@ def footprint(req: Request, precision: str = "fp32") -> int:
     np_, K = c.npts, c.n_sample
     n_ref = np.asarray(req.ref_stat).reshape(-1, 2).shape[0]
     nr = max(np.asarray(req.receivers).reshape(-1, 2).shape[0], 1)
-    n_dft = min(c.nt // max(c.freq_samp, 1) + 1, 512, (2 << 30) // plane)  # the library's DFT chunk
+    n_dft = min(c.nt // max(c.freq_samp, 1) + 1, 640, (2 << 30) // plane)  # the library's DFT chunk
     n_inj = min(c.ntc // max(c.freq_samp, 1), (4 << 30) // plane)
     per = (11 * plane + 3 * n_dft * plane + 16 * np_ * K + 3 * 2 * K * plane + n_inj * plane
            + 8 * nr * (c.nt + c.ntc) + 8 * np_ * (3 + np.asarray(req.source_dist).size // max(np_, 1)))

@@ -113,7 +113,7 @@ fd2d_status fd2d_ctx_set_precision(fd2d_ctx* ctx, int32_t precision);
 /* Wait for all work queued on the context's stream. */
 fd2d_status fd2d_ctx_synchronize(fd2d_ctx* ctx);
 /* Device-memory bounds of the FP32 form: at most `max_snapshots` stored
- * snapshots per DFT contraction (rounded down to a multiple of 32; 0 = 512)
+ * snapshots per DFT contraction (rounded down to a multiple of 32; 0 = 640)
  * and `max_injection_planes` resident injection planes (rounded down to a
  * multiple of 128; 0 = as many as fit in 4 GiB).  Smaller chunks use less
  * memory at the cost of more, smaller contractions.  Each DFT chunk is summed
