@@ -307,6 +307,12 @@ fd2d_status run_parallel(fd2d_ctx* ctx, const char* name, uint64_t key, std::vec
 // Born term, spectra and seismograms of lane l at constant strides from lane 0's).
 fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S, LoopPlan& plan);
 fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S, LoopPlan& plan);
+// Solves on grids of different sizes (one configuration each, equal FD order
+// and freq_samp, mode 0, no Born term) advanced by one launch per time step.
+fd2d_status fp32_multi_forward1_plan(fd2d_ctx* ctx, const std::vector<const Geometry*>& g,
+                                     const std::vector<const SolveArgs*>& a, LoopPlan& plan);
+fd2d_status fp32_multi_correlation_plan(fd2d_ctx* ctx, const std::vector<const Geometry*>& g,
+                                        const std::vector<const SolveArgs*>& a, LoopPlan& plan);
 fd2d_status fp64_forward1(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
 fd2d_status fp64_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);
 fd2d_status fp64_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a);

@@ -6,6 +6,8 @@
 // reference raises a MATLAB error.
 #include "common.cuh"
 
+#include <cstring>
+
 #include <algorithm>
 #include <mutex>
 
@@ -986,9 +988,22 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
         lanes[gi].push_back(j);
       }
     }
+    // Several geometries of one FD order and decimation advance together in
+    // one multi-geometry launch per time step (FD2D_BATCH_MULTI=0 runs them as
+    // parallel graph branches instead, one launch chain per geometry).
+    bool multi = ctx->precision == FD2D_PREC_FP32 && lanes.size() > 1;
+    for (int j = j0; j < j1 && multi; ++j)
+      multi = B[j].g.r == B[j0].g.r && B[j].g.fs == B[j0].g.fs;
+    if (multi) {
+      const char* e = std::getenv("FD2D_BATCH_MULTI");
+      if (e && std::strcmp(e, "0") == 0) multi = false;
+    }
     if (lanes.empty())
       for (int j = j0; j < j1; ++j) ctx->last_lanes.push_back(1);
-    for (const auto& l : lanes) ctx->last_lanes.push_back((int32_t)l.size());
+    if (multi)
+      ctx->last_lanes.push_back((int32_t)(j1 - j0));  // one launch group of every job
+    else
+      for (const auto& l : lanes) ctx->last_lanes.push_back((int32_t)l.size());
     // group buffers: spectra, Green seismograms and correlations of all lanes,
     // lane after lane
     std::vector<double*> grp_gre(lanes.size()), grp_gim(lanes.size()), grp_sg(lanes.size()), grp_c(lanes.size());
@@ -1062,6 +1077,21 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
         st = fp64_forward1(ctx, B[j].g, B[j].green);
         if (st == FD2D_OK) st = fp64_correlation(ctx, B[j].g, B[j].corr);
       }
+    } else if (multi) {
+      std::vector<const Geometry*> gs;
+      std::vector<const SolveArgs*> green, corr;
+      for (int j = j0; j < j1; ++j) {
+        gs.push_back(&B[j].g);
+        green.push_back(&B[j].green);
+        corr.push_back(&B[j].corr);
+      }
+      const std::string part = "@" + std::to_string(j0);
+      LoopPlan p;
+      ctx->ws_prefix.clear();
+      st = fp32_multi_forward1_plan(ctx, gs, green, p);
+      if (st == FD2D_OK) st = run_captured(ctx, ("batch_green_multi" + part).c_str(), p.key, p.loop);
+      if (st == FD2D_OK) st = fp32_multi_correlation_plan(ctx, gs, corr, p);
+      if (st == FD2D_OK) st = run_captured(ctx, ("batch_corr_multi" + part).c_str(), p.key, p.loop);
     } else {
       // one plan per lane group; the groups' loops run as parallel graph branches
       std::vector<LoopPlan> plans(lanes.size());

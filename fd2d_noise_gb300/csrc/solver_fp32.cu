@@ -62,10 +62,9 @@ struct Grid32 {
   int t1x0, t1x1, t1z0, t1z1;
 };
 
-// blockIdx (x, y) in the all-ones taper rectangle of G
-__device__ __forceinline__ bool taper_is_one(const Grid32& G) {
-  return (int)blockIdx.x >= G.t1x0 && (int)blockIdx.x <= G.t1x1 && (int)blockIdx.y >= G.t1z0 &&
-         (int)blockIdx.y <= G.t1z1;
+// tile (tx, tz) in the all-ones taper rectangle of G
+__device__ __forceinline__ bool taper_is_one(const Grid32& G, int tx, int tz) {
+  return tx >= G.t1x0 && tx <= G.t1x1 && tz >= G.t1z0 && tz <= G.t1z1;
 }
 
 // Rows of the first part of a tile's field loads: the box rows the first
@@ -160,27 +159,33 @@ struct Step32 {
   int rec_u;
 };
 
-// One CTA per tile: blockIdx = (tile column, tile row, lane).
-template <int R, int TZ>
-__device__ __forceinline__ void tile_coords(const Grid32&, int, int& x0, int& z0, int& lane) {
-  lane = blockIdx.z;
-  z0 = blockIdx.y * TZ;
-  x0 = blockIdx.x * TX;
-}
+// Where a CTA's tile lies.  One-geometry launches: blockIdx = (tile column,
+// tile row, lane); multi-geometry launches: one solve's rows of the stacked
+// field arrays (k32_step_multi).
+struct TileLoc {
+  int tx, tz;      // tile column and row in the solve
+  int x0, z0;      // first point of the tile
+  int lane;        // lane (third tensor-map coordinate)
+  int t;           // tile number in the solve's receiver tables
+  int ty0;         // first row of the solve in the field arrays (tensor-map y offset)
+  int64_t lo;      // element offset of the solve's plane in the field arrays (row pitch G.P)
+  int64_t slo;     // offset of the tile's lane in the DFT snapshot planes
+  int sp;          // row pitch of the DFT snapshot and injection planes
+};
 
-template <int R, bool HU, bool HI, int TZ>
+template <int R, bool HU, bool HI, int TZ, bool MULTI>
 __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, const Step32& S, float* buf,
-                                           uint64_t* bar, int t, bool coeffs, bool fields) {
+                                           uint64_t* bar, const TileLoc& L, bool coeffs, bool fields) {
   using T = Tile<R, HU, HI, TZ>;
-  int x0, z0, lane;
-  tile_coords<R, TZ>(G, t, x0, z0, lane);
+  static_assert(!(MULTI && T::INJ_SMEM), "multi-geometry launches read the injection planes from L2");
+  const int x0 = L.x0, z0 = L.ty0 + L.z0, lane = L.lane;
   const int bz0 = z0 - R + 1, zz0 = z0 - 2 * R + 1;
   if (coeffs) {
     // Coefficient planes and the injection plane are not written by the time
     // loop, so they load before the wait for the previous step.  Tiles whose
     // taper is all ones do not load it; the injection box takes its place.
-    const bool t1 = taper_is_one(G);
-    const bool inj_t = T::INJ_IN_T && t1;
+    const bool t1 = taper_is_one(G, L.tx, L.tz);
+    const bool inj_t = T::INJ_IN_T && !MULTI && t1;
     uint32_t b0 = 4u * (T::BH * T::BWa + TZ * TX + T::H1 * T::SXWa + T::H1Z * T::BWa + T::H1 * T::BWa);
     if (!t1) b0 += 4u * T::BH * T::BWa;
     if (T::INJ_SMEM || inj_t) b0 += 4u * T::BH * T::BWa;
@@ -205,9 +210,12 @@ __device__ __forceinline__ void issue_tile(const Grid32& G, const StepMaps& M, c
   }
 }
 
-template <int R, bool HU, bool HI, int TZ>
-__global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB) void k32_step(
-    Grid32 G, const __grid_constant__ StepMaps M, Step32 S) {
+// The step of one tile: everything a CTA of k32_step or k32_step_multi does.
+// G, S and L are the kernel's parameters (one-geometry launches) or shared
+// copies resolved per CTA (multi-geometry launches); cf are the FD weights.
+template <int R, bool HU, bool HI, int TZ, bool MULTI>
+__device__ __forceinline__ void step_tile(const Grid32& G, const StepMaps& M, const Step32& S, const TileLoc& L,
+                                          const float* cf) {
   using T = Tile<R, HU, HI, TZ>;
   constexpr int NT = T::NT;
   extern __shared__ __align__(128) unsigned char sm_raw[];
@@ -215,8 +223,6 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
   // (offset arithmetic on the shared array keeps the pointer in the shared
   // address space, so the float4 accesses below compile to shared loads)
   float* sm = reinterpret_cast<float*>(sm_raw + ((128u - (smem_u32(sm_raw) & 127u)) & 127u));
-  // coefficients stay in the parameter bank (FFMA constant operands, no registers)
-  const float* cf = G.c;
 #define inv_dx G.inv_dx
 #define inv_dz G.inv_dz
 #define gdt G.dt
@@ -229,14 +235,10 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
 
   const int tid = threadIdx.x;
   const int nx = G.nx, nz = G.nz, P = G.P;
-  const int n_tiles = G.ntx * G.ntz * G.S;
   constexpr int W = T::BWa;  // 40: row stride of the box regions
   float* s_vn = sm + T::O_V;  // new v, written over the old v of the same point
   constexpr bool inj = HI;
-
-  // tile number in the per-(lane, tile) tables
-  const int t = blockIdx.x + G.ntx * (blockIdx.y + G.ntz * blockIdx.z);
-  if (t >= n_tiles) return;
+  const int t = L.t;  // tile number in the receiver tables
   if (tid == 0) {
     s_nsrc = 0;
     s_nrec = 0;
@@ -245,20 +247,19 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
     fence_mbar_init();
     // coefficient planes are not written by the time loop: their loads may
     // overlap the end of the previous step (programmatic dependent launch)
-    issue_tile<R, HU, HI, TZ>(G, M, S, sm, bar, t, true, false);
+    issue_tile<R, HU, HI, TZ, MULTI>(G, M, S, sm, bar, L, true, false);
     // The fields are what the previous launch wrote (or will write what it
     // read: ping-pong buffers): wait for it to complete, then load them.  The
     // other threads touch those buffers only after this tile's loads land, so
     // this thread's wait orders the whole CTA after the previous step.
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    issue_tile<R, HU, HI, TZ>(G, M, S, sm, bar, t, false, true);
+    issue_tile<R, HU, HI, TZ, MULTI>(G, M, S, sm, bar, L, false, true);
   }
   {
     const float* buf = sm;
-    int x0, z0, lane;
-    tile_coords<R, TZ>(G, t, x0, z0, lane);
+    const int x0 = L.x0, z0 = L.z0, lane = L.lane;
     const int bz0 = z0 - R + 1, vx0 = x0 - 4;
-    const int64_t lo = (int64_t)lane * G.ps;
+    const int64_t lo = L.lo;
     const int2* src_xy = S.src_xy + (int64_t)lane * S.nsrc;
     const double* amp = S.amp ? S.amp + (int64_t)lane * S.nsrc : nullptr;
     __syncthreads();  // barrier initialised, lists cleared
@@ -308,7 +309,7 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
     const float* s_v = buf + T::O_V;
     const float* s_b = buf + T::O_B;
     const float* s_t = buf + T::O_T;
-    const bool t1 = taper_is_one(G);
+    const bool t1 = taper_is_one(G, L.tx, L.tz);
     const float* s_i = buf + T::O_I;
     const float* s_mu = buf + T::O_MU;
     const float* s_u = buf + T::O_U;
@@ -408,14 +409,14 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
           float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
           if (T::INJ_SMEM) {
             i4 = *reinterpret_cast<const float4*>(s_i + rr * W + c0);
-          } else if (inj && t1) {
+          } else if (inj && t1 && !MULTI) {
             i4 = *reinterpret_cast<const float4*>(s_t + rr * W + c0);  // the injection box (issue_tile)
           } else if (inj) {
             // from L2; outside the grid the plane is zero (as the TMA fill)
             const int gx0 = vx0 + c0;
-            if (gx0 >= 0 && gx0 < P && gz >= 0 && gz < nz)
-              i4 = __ldg(reinterpret_cast<const float4*>(
-                  S.inj_base + ((int64_t)S.inj_plane * G.S + lane) * G.ps + (int64_t)P * gz + gx0));
+            if (gx0 >= 0 && gx0 < L.sp && gz >= 0 && gz < nz)
+              i4 = __ldg(reinterpret_cast<const float4*>(S.inj_base + ((int64_t)S.inj_plane * G.S + lane) * G.ps +
+                                                         (int64_t)L.sp * gz + gx0));
           }
           if (S.snap_pre && !S.snap_pre_u && rr >= R - 1 && rr < R - 1 + TZ && c0 >= 4 && c0 < 4 + TX) {
             // single(v) before the update at the tile's own points, taken here
@@ -499,6 +500,7 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
           nu[e] = HU ? __fmaf_rn(vn[e], gdt, uo[e]) : vn[e];
         }
         const int64_t p = lo + i0 + (int64_t)P * j;
+        const int64_t ps_ = L.slo + i0 + (int64_t)L.sp * j;  // in the DFT snapshot plane
         if (!EDGE || i0 + 3 < nx) {
           // whole quad inside the grid: vector stores
           *reinterpret_cast<float4*>(S.vo + p) = make_float4(vn[0], vn[1], vn[2], vn[3]);
@@ -511,7 +513,7 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
           }
           if (!EDGE || j <= nz - 2) *reinterpret_cast<float4*>(S.szyo + p) = make_float4(nsz[0], nsz[1], nsz[2], nsz[3]);
           if (HU) *reinterpret_cast<float4*>(S.uo + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
-          if (S.snap_dft) *reinterpret_cast<float4*>(S.snap_dft + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
+          if (S.snap_dft) *reinterpret_cast<float4*>(S.snap_dft + ps_) = make_float4(nu[0], nu[1], nu[2], nu[3]);
         } else {
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
@@ -520,7 +522,7 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
             if (i0 + e <= nx - 2) S.sxyo[p + e] = nsx[e];
             if (j <= nz - 2) S.szyo[p + e] = nsz[e];
             if (HU) S.uo[p + e] = nu[e];
-            if (S.snap_dft) S.snap_dft[p + e] = nu[e];
+            if (S.snap_dft) S.snap_dft[ps_ + e] = nu[e];
           }
         }
         if (S.nrec && s_nrec > 0) {
@@ -569,6 +571,128 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
 #undef inv_dx
 #undef inv_dz
 #undef gdt
+
+// One-geometry step: one CTA per tile, blockIdx = (tile column, tile row, lane).
+template <int R, bool HU, bool HI, int TZ>
+__global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB) void k32_step(
+    Grid32 G, const __grid_constant__ StepMaps M, Step32 S) {
+  TileLoc L;
+  L.tx = blockIdx.x;
+  L.tz = blockIdx.y;
+  L.lane = blockIdx.z;
+  L.x0 = L.tx * TX;
+  L.z0 = L.tz * TZ;
+  L.t = L.tx + G.ntx * (L.tz + G.ntz * L.lane);
+  L.ty0 = 0;
+  L.lo = (int64_t)L.lane * G.ps;
+  L.slo = L.lo;
+  L.sp = G.P;
+  // coefficients stay in the parameter bank (FFMA constant operands, no registers)
+  step_tile<R, HU, HI, TZ, false>(G, M, S, L, G.c);
+}
+
+// ---- multi-geometry step -----------------------------------------------------------
+// Solves on grids of different sizes (the reference stations of a batch, one
+// configuration each) advance together, one launch per time step.  Their
+// fields are stacked in tall arrays of a common row pitch: solve i occupies
+// rows [row0, row0 + nz) with rows of zeros above and below it and zeros past
+// its nx columns, so one set of tensor maps serves every solve and a halo box
+// reads zeros outside each grid, as the tensor-map fill does for one grid.
+// DFT snapshots and injection planes stay compact per solve (pitch P).
+struct Seg {
+  int nx, nz, P, ntx, ntz;  // grid, compact row pitch, tiles
+  int row0;                 // first row in the stacked field arrays
+  int tile0;                // first CTA of the solve in a launch
+  int nt;                   // forward steps (DFT schedule of the Green run)
+  int dft_T;                // snapshots per DFT chunk
+  int inj_chunk;            // injection planes per chunk
+  int nsrc, nrec;
+  int t1[4];                // all-ones taper tile rectangle
+  float inv_dx, inv_dz, dt;
+  int64_t ps;               // compact plane stride
+  float* snaps;             // DFT snapshot chunk
+  const float* inj;         // resident injection planes
+  const int2 *src_xy, *rec_xy, *tile_rec, *rec_ent;
+  double* seis;             // nrec-by-steps seismograms
+};
+
+struct MultiStep {
+  int n;         // time step (1-based)
+  int n_seg;     // solves active at this step (a prefix of the table)
+  int fs;        // DFT / injection decimation
+  int green;     // 1: Green run (point force, DFT of v), 0: correlation run
+  int Pf;        // row pitch of the stacked field arrays
+  float c[4];    // FD weights
+  const Seg* segs;
+  float *vo, *sxyo, *szyo, *uo;  // stacked fields written this step
+  int* err;
+};
+
+template <int R, bool HU, bool HI, int TZ>
+__global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB) void k32_step_multi(
+    MultiStep Q, const __grid_constant__ StepMaps M) {
+  __shared__ Grid32 s_G;
+  __shared__ Step32 s_S;
+  __shared__ TileLoc s_L;
+  if (threadIdx.x == 0) {
+    // the solve of this CTA: the last one whose first CTA is at or before it
+    const int b = blockIdx.x;
+    int lo = 0, hi = Q.n_seg - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (Q.segs[mid].tile0 <= b) lo = mid;
+      else hi = mid - 1;
+    }
+    const Seg& g = Q.segs[lo];
+    Grid32 G{};
+    G.nx = g.nx; G.nz = g.nz; G.P = Q.Pf; G.S = 1; G.ntx = g.ntx; G.ntz = g.ntz; G.ps = g.ps;
+    for (int m = 0; m < 4; ++m) G.c[m] = Q.c[m];
+    G.inv_dx = g.inv_dx; G.inv_dz = g.inv_dz; G.dt = g.dt; G.err = Q.err;
+    G.t1x0 = g.t1[0]; G.t1x1 = g.t1[1]; G.t1z0 = g.t1[2]; G.t1z1 = g.t1[3];
+    Step32 S{};
+    S.vo = Q.vo; S.sxyo = Q.sxyo; S.szyo = Q.szyo; S.uo = Q.uo;
+    S.has_u = HU;
+    S.inj_plane = -1;
+    const int n = Q.n;
+    if (Q.green) {
+      S.src_xy = g.src_xy;
+      S.nsrc = g.nsrc;
+      S.amp_const = 1.0e9f;  // stf = 1.0e9*ones(1,nt), code/run_forward1_green.m:64
+      if ((n + g.nt - 1) % Q.fs == 0) {
+        // DFT events so far, this one included: the snapshot slot of the chunk
+        const int e = (n + g.nt - 1) / Q.fs - (g.nt - 1) / Q.fs;
+        S.snap_dft = g.snaps + (int64_t)((e - 1) % g.dft_T) * g.ps;
+      }
+    } else {
+      S.src_xy = g.src_xy;
+      S.rec_u = 1;
+      if (HI) S.inj_plane = (n / Q.fs - 1) % g.inj_chunk;
+    }
+    S.inj_base = g.inj;
+    S.rec_xy = g.rec_xy;
+    S.nrec = g.nrec;
+    S.tile_rec = g.tile_rec;
+    S.rec_ent = g.rec_ent;
+    S.seis_col = g.seis + (int64_t)g.nrec * (n - 1);
+    TileLoc L;
+    L.t = b - g.tile0;
+    L.tx = L.t % g.ntx;
+    L.tz = L.t / g.ntx;
+    L.x0 = L.tx * TX;
+    L.z0 = L.tz * TZ;
+    L.lane = 0;
+    L.ty0 = g.row0;
+    L.lo = (int64_t)g.row0 * Q.Pf;
+    L.slo = 0;
+    L.sp = g.P;
+    s_G = G;
+    s_S = S;
+    s_L = L;
+  }
+  __syncthreads();
+  // the FD weights from the parameter bank; the per-solve values from shared memory
+  step_tile<R, HU, HI, TZ, true>(s_G, M, s_S, s_L, Q.c);
+}
 
 // ---- point kernels ---------------------------------------------------------------
 // FP32 staggered derivatives of a field with row pitch `ld` (f, or f - g).
@@ -1744,6 +1868,406 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
   }
   if (nt_loop < ntc && nr > 0)
     FD2D_CUDA(ctx, cudaMemsetAsync(a.seis + (size_t)nr * nt_loop, 0, (size_t)nr * (ntc - nt_loop) * 8, ctx->stream));
+  return FD2D_OK;
+}
+
+
+// ---------------------------------------------------------------------------------
+// Multi-geometry loops: the reference stations of a batch whose grids differ
+// (the parfor over stations of code/calculate_data.m:189-202) advance in one
+// k32_step_multi launch per time step, each solve for its own nt / ntc steps;
+// the DFT and injection contractions stay per solve.
+namespace {
+
+constexpr int MULTI_TZ = 32;  // tile rows of the multi-geometry step
+
+template <int R, bool HU, bool HI>
+void launch_multi_t(fd2d_ctx* ctx, const MultiStep& q, const StepMaps& m, int n_tiles, bool pdl) {
+  using T = Tile<R, HU, HI, MULTI_TZ>;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(n_tiles);
+  cfg.blockDim = dim3(T::NT);
+  cfg.dynamicSmemBytes = T::BYTES;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k32_step_multi<R, HU, HI, MULTI_TZ>, q, m);
+}
+
+template <int R>
+void launch_multi_r(fd2d_ctx* ctx, bool hu, bool hi, const MultiStep& q, const StepMaps& m, int n_tiles, bool pdl) {
+  if (!hu) launch_multi_t<R, false, false>(ctx, q, m, n_tiles, pdl);
+  else if (hi) launch_multi_t<R, true, true>(ctx, q, m, n_tiles, pdl);
+  else launch_multi_t<R, true, false>(ctx, q, m, n_tiles, pdl);
+}
+
+fd2d_status launch_multi(fd2d_ctx* ctx, int R, bool hu, bool hi, const MultiStep& q, const StepMaps& m,
+                         int n_tiles, bool pdl) {
+  switch (R) {
+    case 1: launch_multi_r<1>(ctx, hu, hi, q, m, n_tiles, pdl); break;
+    case 2: launch_multi_r<2>(ctx, hu, hi, q, m, n_tiles, pdl); break;
+    case 3: launch_multi_r<3>(ctx, hu, hi, q, m, n_tiles, pdl); break;
+    default: launch_multi_r<4>(ctx, hu, hi, q, m, n_tiles, pdl); break;
+  }
+  return after_launch(ctx, "k32_step_multi");
+}
+
+template <int R>
+fd2d_status multi_attributes_r(fd2d_ctx* ctx) {
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step_multi<R, false, false, MULTI_TZ>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, false, false, MULTI_TZ>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step_multi<R, true, false, MULTI_TZ>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, true, false, MULTI_TZ>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step_multi<R, true, true, MULTI_TZ>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile<R, true, true, MULTI_TZ>::BYTES));
+  return FD2D_OK;
+}
+
+PerDeviceOnce g_multi_attributes;
+fd2d_status multi_attributes(fd2d_ctx* ctx) {
+  return g_multi_attributes.run(ctx, [ctx]() -> fd2d_status {
+    FD2D_TRY(multi_attributes_r<1>(ctx));
+    FD2D_TRY(multi_attributes_r<2>(ctx));
+    FD2D_TRY(multi_attributes_r<3>(ctx));
+    return multi_attributes_r<4>(ctx);
+  });
+}
+
+// Host state of one solve of a multi-geometry loop.
+struct MultiSolve {
+  Geometry g;
+  SolveArgs a;
+  Run r;          // one-lane compact layout of the solve's DFT snapshots and injection planes
+  Dft d;
+  Injection inj;
+  Seg seg{};
+  int nsteps = 0;
+};
+
+// The stacked field arrays and the device table of the solves.
+struct MultiLayout {
+  int R = 2, Pf = 32, rows = 0, fs = 1;
+  float *v[2] = {}, *sxy[2] = {}, *szy[2] = {}, *u[2] = {};
+  float *b = nullptr, *taper = nullptr, *dtmu = nullptr;
+  StepMaps maps[2];
+  Seg* segs = nullptr;
+  std::vector<int> tiles;  // tiles[k]: CTAs of the first k solves
+  float c[4] = {0, 0, 0, 0};
+  bool pdl = true;
+};
+
+// Solves sorted by steps (longest first, so the solves still running at a
+// step are a prefix), stacked fields, coefficient planes, node tables and
+// tensor maps.  The DFT / injection parts are added by the callers.
+fd2d_status multi_layout(fd2d_ctx* ctx, std::vector<MultiSolve>& ms, bool with_u, MultiLayout& L) {
+  std::stable_sort(ms.begin(), ms.end(), [](const MultiSolve& x, const MultiSolve& y) { return x.nsteps > y.nsteps; });
+  L.R = ms[0].g.r;
+  L.fs = ms[0].g.fs;
+  for (int m = 0; m < 4; ++m) L.c[m] = (float)ms[0].g.c[m];
+  const int R = L.R, TZ = MULTI_TZ, MZ = 2 * R;  // zero rows above and below every solve
+  L.Pf = 32;
+  int rows = 0, tiles = 0;
+  L.tiles.assign(1, 0);
+  for (auto& s : ms) {
+    const Geometry& g = s.g;
+    Seg& q = s.seg;
+    q.nx = g.nx;
+    q.nz = g.nz;
+    q.P = (g.nx + 31) / 32 * 32;
+    q.ps = ((int64_t)q.P * g.nz + 127) / 128 * 128;
+    q.ntx = (g.nx + TX - 1) / TX;
+    q.ntz = (g.nz + TZ - 1) / TZ;
+    q.row0 = rows + MZ;
+    rows += MZ + q.ntz * TZ + MZ;
+    q.tile0 = tiles;
+    tiles += q.ntx * q.ntz;
+    L.tiles.push_back(tiles);
+    q.nt = g.nt;
+    q.inv_dx = (float)(1.0 / g.dx);
+    q.inv_dz = (float)(1.0 / g.dz);
+    q.dt = (float)g.dt;
+    L.Pf = std::max(L.Pf, q.P);
+  }
+  L.rows = rows;
+  const size_t n = (size_t)L.Pf * rows;
+  static const char* names[2][4] = {{"m.v0", "m.sxy0", "m.szy0", "m.u0"}, {"m.v1", "m.sxy1", "m.szy1", "m.u1"}};
+  for (int q = 0; q < 2; ++q) {
+    FD2D_TRY(workspace_t(ctx, names[q][0], n, &L.v[q]));
+    FD2D_TRY(workspace_t(ctx, names[q][1], n, &L.sxy[q]));
+    FD2D_TRY(workspace_t(ctx, names[q][2], n, &L.szy[q]));
+    FD2D_CUDA(ctx, cudaMemsetAsync(L.v[q], 0, n * 4, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(L.sxy[q], 0, n * 4, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(L.szy[q], 0, n * 4, ctx->stream));
+    if (with_u) {
+      FD2D_TRY(workspace_t(ctx, names[q][3], n, &L.u[q]));
+      FD2D_CUDA(ctx, cudaMemsetAsync(L.u[q], 0, n * 4, ctx->stream));
+    }
+  }
+  FD2D_TRY(workspace_t(ctx, "m.b", n, &L.b));
+  FD2D_TRY(workspace_t(ctx, "m.taper", n, &L.taper));
+  FD2D_TRY(workspace_t(ctx, "m.dtmu", n, &L.dtmu));
+  FD2D_CUDA(ctx, cudaMemsetAsync(L.b, 0, n * 4, ctx->stream));
+  FD2D_CUDA(ctx, cudaMemsetAsync(L.taper, 0, n * 4, ctx->stream));
+  FD2D_CUDA(ctx, cudaMemsetAsync(L.dtmu, 0, n * 4, ctx->stream));
+  int ti = 0;
+  for (int c = 0; c < N_TILE_ROWS; ++c)
+    if (TILE_ROWS[c] == TZ) ti = c;
+  for (size_t i = 0; i < ms.size(); ++i) {
+    MultiSolve& s = ms[i];
+    const Geometry& g = s.g;
+    Seg& q = s.seg;
+    ctx->ws_prefix = "m" + std::to_string(i) + ":";
+    double* ab;
+    FD2D_TRY(upload_tagged<double>(ctx, "f32.absbound64", g.key, g.absbound->size(),
+                                    [&](std::vector<double>& h) { h = *g.absbound; }, &ab));
+    const size_t off = (size_t)q.row0 * L.Pf;
+    dim3 pg((L.Pf + 31) / 32, (g.nz + 7) / 8);
+    k32_prep<<<pg, dim3(32, 8), 0, ctx->stream>>>(s.a.mu, s.a.rho, ab, g.dt, g.nx, g.nz, L.Pf, L.b + off,
+                                                  L.taper + off, L.dtmu + off);
+    FD2D_TRY(after_launch(ctx, "k32_prep"));
+    int t1[N_TILE_ROWS][4];
+    taper_ones(*g.absbound, g.nx, g.nz, R, t1);
+    for (int k = 0; k < 4; ++k) q.t1[k] = t1[ti][k];
+    std::vector<int2> rxy, sxy, table, ent;
+    for (int p : s.a.rec_idx) rxy.push_back(make_int2(p % g.nx, p / g.nx));
+    for (int p : s.a.src_idx) sxy.push_back(make_int2(p % g.nx, p / g.nx));
+    if (rxy.empty()) rxy.push_back(make_int2(-1 << 30, -1 << 30));
+    if (sxy.empty()) sxy.push_back(make_int2(-1 << 30, -1 << 30));
+    std::vector<const std::vector<int>*> lanes{&s.a.rec_idx};
+    build_tile_receivers_idx(g.nx, g.nz, TZ, lanes, table, ent);
+    int2 *d_rxy, *d_sxy, *d_tab, *d_ent;
+    FD2D_TRY(upload(ctx, "m.rec", rxy, &d_rxy));
+    FD2D_TRY(upload(ctx, "m.src", sxy, &d_sxy));
+    FD2D_TRY(upload(ctx, "m.tile_rec", table, &d_tab));
+    FD2D_TRY(upload(ctx, "m.rec_ent", ent, &d_ent));
+    q.rec_xy = d_rxy;
+    q.src_xy = d_sxy;
+    q.tile_rec = d_tab;
+    q.rec_ent = d_ent;
+    q.nrec = (int)s.a.rec_idx.size();
+    q.nsrc = (int)s.a.src_idx.size();
+    q.seis = s.a.seis;
+    // the solve's compact one-lane layout for its DFT and injection
+    Run& r = s.r;
+    r.S = 1;
+    r.np = g.npts();
+    r.ps = q.ps;
+    r.R = R;
+    r.tz = TZ;
+    r.G.nx = g.nx;
+    r.G.nz = g.nz;
+    r.G.P = q.P;
+    r.G.S = 1;
+    r.G.ps = q.ps;
+    r.G.err = ctx->d_err;
+  }
+  ctx->ws_prefix.clear();
+  // tensor maps over the stacked arrays (2-D arrays as 3-D maps of depth 1)
+  const int BH = TZ + 2 * R - 1, SZH = TZ + 4 * R - 2, BWa = TX + 8, SXWa = TX + 16;
+  const int NT = std::min(TX / 4 * TZ, 256);
+  const int H1 = split_top_rows(NT, BWa / 4, BH), H1Z = split_top_szy(H1, R, SZH);
+  const int W = L.Pf, Hh = rows;
+  const int64_t pl = (int64_t)L.Pf * rows;
+  for (int q = 0; q < 2; ++q) {
+    StepMaps& m = L.maps[q];
+    FD2D_TRY(make_tmap_f32(ctx, &m.sxy_t, L.sxy[q], W, Hh, L.Pf, SXWa, H1, 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.sxy_b, L.sxy[q], W, Hh, L.Pf, SXWa, BH - H1, 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.szy_t, L.szy[q], W, Hh, L.Pf, BWa, H1Z, 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.szy_b, L.szy[q], W, Hh, L.Pf, BWa, std::max(SZH - H1Z, 1), 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.v_t, L.v[q], W, Hh, L.Pf, BWa, H1, 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.v_b, L.v[q], W, Hh, L.Pf, BWa, BH - H1, 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.u, L.u[q] ? L.u[q] : L.v[q], W, Hh, L.Pf, TX, TZ, 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.b, L.b, W, Hh, L.Pf, BWa, BH, 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.taper, L.taper, W, Hh, L.Pf, BWa, BH, 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.dtmu, L.dtmu, W, Hh, L.Pf, TX, TZ, 1, pl));
+    FD2D_TRY(make_tmap_f32(ctx, &m.inj, L.b, W, Hh, L.Pf, BWa, BH, 1, pl));  // unused: planes come from L2
+  }
+  L.pdl = ctx->concurrent_groups <= 1 && !ctx->shared_gpu;
+  FD2D_TRY(step_attributes(ctx));
+  FD2D_TRY(multi_attributes(ctx));
+  return contract_prepare(ctx);
+}
+
+fd2d_status multi_upload_segs(fd2d_ctx* ctx, const std::vector<MultiSolve>& ms, MultiLayout& L) {
+  std::vector<Seg> h(ms.size());
+  for (size_t i = 0; i < ms.size(); ++i) h[i] = ms[i].seg;
+  return upload(ctx, "m.segs", h, &L.segs);
+}
+
+void sig_multi(Sig& sg, const std::vector<MultiSolve>& ms, const MultiLayout& L) {
+  sg.add(L.R); sg.add(L.Pf); sg.add(L.rows); sg.add(L.fs); sg.add(L.segs); sg.add((int)L.pdl);
+  sg.bytes(L.maps, sizeof(L.maps));
+  for (const auto& s : ms) {
+    sg.bytes(&s.seg, sizeof(Seg));
+    sig_args(sg, s.g, s.a);
+    sig_dft(sg, s.d);
+    sig_inj(sg, s.inj);
+    sg.add(s.nsteps);
+  }
+}
+
+}  // namespace
+
+fd2d_status fp32_multi_forward1_plan(fd2d_ctx* ctx, const std::vector<const Geometry*>& gs,
+                                     const std::vector<const SolveArgs*>& as, LoopPlan& plan) {
+  std::vector<MultiSolve> ms(gs.size());
+  for (size_t i = 0; i < gs.size(); ++i) {
+    ms[i].g = *gs[i];
+    ms[i].a = *as[i];
+    ms[i].nsteps = gs[i]->nt;
+  }
+  MultiLayout L;
+  FD2D_TRY(multi_layout(ctx, ms, false, L));
+  for (size_t i = 0; i < ms.size(); ++i) {
+    MultiSolve& s = ms[i];
+    const Geometry& g = s.g;
+    const int nt = g.nt, K = g.K;
+    ctx->ws_prefix = "m" + std::to_string(i) + ":";
+    // DFT events and coefficients as in fp32_forward1_plan
+    std::vector<int> ev;
+    for (int n = 1; n <= nt; ++n)
+      if ((n + nt - 1) % g.fs == 0) ev.push_back(n);
+    FD2D_TRY(dft_init(ctx, s.r, (int)ev.size(), s.d));
+    if (!ev.empty()) {
+      auto fill = [&](std::vector<float>& rows) {
+        for (size_t e = 0; e < ev.size(); ++e)
+          for (int k = 0; k < K; ++k) {
+            double re, im;
+            dft_coeff(-(g.w[k] * g.t_fwd[ev[e] - 1]), g.dt, re, im);
+            rows[e * 2 * K + k] = (float)re;
+            rows[e * 2 * K + K + k] = (float)(-im);
+          }
+      };
+      FD2D_TRY(dft_add_target(ctx, "f32.dftB0", table_tag(g, 0, ev), ev.size() * 2 * K, fill, s.a.G_re,
+                              s.a.G_im, 0, s.d));
+    } else {
+      FD2D_CUDA(ctx, cudaMemsetAsync(s.a.G_re, 0, (size_t)g.npts() * K * 8, ctx->stream));
+      FD2D_CUDA(ctx, cudaMemsetAsync(s.a.G_im, 0, (size_t)g.npts() * K * 8, ctx->stream));
+    }
+    s.seg.dft_T = std::max(s.d.T, 1);
+    s.seg.snaps = s.d.snaps;
+  }
+  ctx->ws_prefix.clear();
+  FD2D_TRY(multi_upload_segs(ctx, ms, L));
+  Sig sg;
+  sg.add(1);
+  sig_multi(sg, ms, L);
+  plan.name = "fp32_multi_forward1";
+  plan.key = sg.h;
+  plan.loop = [ctx, ms, L]() -> fd2d_status {
+    std::vector<Dft> dd(ms.size());
+    for (size_t i = 0; i < ms.size(); ++i) dd[i] = ms[i].d;  // the loop's own chunk bookkeeping
+    const int nmax = ms[0].nsteps;
+    int64_t units = 0;
+    for (const auto& s : ms) units += s.g.npts() * s.g.nt;
+    const int tl = timer_begin(ctx, ctx->stream);
+    int n_seg = (int)ms.size(), par = 0;
+    for (int n = 1; n <= nmax; ++n) {
+      while (n_seg > 0 && ms[n_seg - 1].nsteps < n) --n_seg;
+      MultiStep q{};
+      q.n = n;
+      q.n_seg = n_seg;
+      q.fs = L.fs;
+      q.green = 1;
+      q.Pf = L.Pf;
+      for (int m = 0; m < 4; ++m) q.c[m] = L.c[m];
+      q.segs = L.segs;
+      q.vo = L.v[1 - par];
+      q.sxyo = L.sxy[1 - par];
+      q.szyo = L.szy[1 - par];
+      q.uo = nullptr;
+      q.err = ctx->d_err;
+      FD2D_TRY(launch_multi(ctx, L.R, false, false, q, L.maps[par], L.tiles[n_seg], L.pdl));
+      for (int i = 0; i < n_seg; ++i) {
+        const MultiSolve& s = ms[i];
+        if (dd[i].n_events && (n + s.g.nt - 1) % s.g.fs == 0) FD2D_TRY(dft_push(ctx, s.r, s.g, dd[i]));
+      }
+      par ^= 1;
+    }
+    timer_end(ctx, ctx->stream, tl, FD2D_TIMER_STEP_V, units, nmax);
+    return FD2D_OK;
+  };
+  return FD2D_OK;
+}
+
+fd2d_status fp32_multi_correlation_plan(fd2d_ctx* ctx, const std::vector<const Geometry*>& gs,
+                                        const std::vector<const SolveArgs*>& as, LoopPlan& plan) {
+  std::vector<MultiSolve> ms(gs.size());
+  for (size_t i = 0; i < gs.size(); ++i) {
+    ms[i].g = *gs[i];
+    ms[i].a = *as[i];
+    ms[i].nsteps = gs[i]->ntc;
+  }
+  MultiLayout L;
+  FD2D_TRY(multi_layout(ctx, ms, true, L));
+  for (size_t i = 0; i < ms.size(); ++i) {
+    MultiSolve& s = ms[i];
+    const Geometry& g = s.g;
+    ctx->ws_prefix = "m" + std::to_string(i) + ":";
+    double *M, *spec;
+    FD2D_TRY(interp_dev(ctx, g, &M));
+    FD2D_TRY(spectrum_eff(ctx, g, &s.a, 1, &spec));
+    for (int n = 1; n <= g.ntc; ++n)
+      if (n % g.fs == 0) {
+        s.inj.step_of_event.push_back(n);
+        s.inj.row_of_event.push_back(n / g.fs - 1);
+      }
+    const double* xre = s.a.Gin_re;
+    const double* xim = s.a.Gin_im;
+    const double* sd = s.a.source_dist;
+    FD2D_TRY(build_injection(ctx, g, s.r, &xre, &xim, 1.0, spec, M, &sd, s.inj));
+    s.seg.inj = s.inj.planes;
+    s.seg.inj_chunk = std::max(s.inj.chunk, 1);
+    s.seg.nsrc = 0;
+  }
+  ctx->ws_prefix.clear();
+  FD2D_TRY(multi_upload_segs(ctx, ms, L));
+  Sig sg;
+  sg.add(2);
+  sig_multi(sg, ms, L);
+  plan.name = "fp32_multi_correlation";
+  plan.key = sg.h;
+  plan.loop = [ctx, ms, L]() -> fd2d_status {
+    std::vector<Injection> ij(ms.size());
+    for (size_t i = 0; i < ms.size(); ++i) ij[i] = ms[i].inj;  // the loop's own chunk bookkeeping
+    const int nmax = ms[0].nsteps;
+    int64_t units = 0;
+    for (const auto& s : ms) units += s.g.npts() * s.g.ntc;
+    const int tl = timer_begin(ctx, ctx->stream);
+    int n_seg = (int)ms.size(), par = 0;
+    for (int n = 1; n <= nmax; ++n) {
+      while (n_seg > 0 && ms[n_seg - 1].nsteps < n) --n_seg;
+      const bool hi = n % L.fs == 0;
+      if (hi)
+        for (int i = 0; i < n_seg; ++i) {
+          int plane = 0;  // the kernel derives it; this makes the event's chunk resident
+          if (ij[i].n_events) FD2D_TRY(injection_plane(ctx, ms[i].r, ms[i].g, ij[i], n / L.fs - 1, &plane));
+        }
+      MultiStep q{};
+      q.n = n;
+      q.n_seg = n_seg;
+      q.fs = L.fs;
+      q.green = 0;
+      q.Pf = L.Pf;
+      for (int m = 0; m < 4; ++m) q.c[m] = L.c[m];
+      q.segs = L.segs;
+      q.vo = L.v[1 - par];
+      q.sxyo = L.sxy[1 - par];
+      q.szyo = L.szy[1 - par];
+      q.uo = L.u[1 - par];
+      q.err = ctx->d_err;
+      FD2D_TRY(launch_multi(ctx, L.R, true, hi, q, L.maps[par], L.tiles[n_seg], L.pdl));
+      par ^= 1;
+    }
+    timer_end(ctx, ctx->stream, tl, FD2D_TIMER_STEP_VU, units, nmax);
+    return FD2D_OK;
+  };
   return FD2D_OK;
 }
 

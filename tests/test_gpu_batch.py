@@ -68,3 +68,52 @@ def test_batch_matches_single_solves(fd2d_lib, prec, budget):
             got = d["out"].cpu().numpy().reshape(j["rec"].shape[0], j["cfg"].ntc, order="F")
             ref = _single(j, prec)
             assert rel_l2(got, ref) < (1e-12 if prec == "fp64" else 1e-6), rep
+
+
+def _uneven_jobs(sizes=(256, 384, 512, 800), nts=(150, 220, 180, 120, 260)):
+    """Stations on the grid sizes of the uneven-batch configuration (order 4,
+    four frequency bands, dt from CFL 0.5 at 4000 m/s, taper 30 points), each
+    with its own nt, short enough for a test."""
+    from fd2d_noise_gb300.workloads import batch_uneven
+    b = batch_uneven(n_stations=16, K=24, nr=6, sizes=sizes, nt_range=(100, 300))
+    picked = [next(w for w in b.stations if w.cfg.nx == nx) for nx in sizes]
+    picked.append(next(w for w in b.stations if w.cfg.nx == sizes[-1] and w is not picked[-1]))
+    out = []
+    for i, w in enumerate(picked):
+        cfg = w.cfg.replace(nt=nts[i])
+        out.append(dict(cfg=cfg, mu=w.mu, rho=w.rho, spec=w.spectrum, sd=w.source_dist, src=w.ref_stations,
+                        rec=w.receivers))
+    return out
+
+
+def test_uneven_grids_advance_in_one_launch_per_step(fd2d_lib):
+    """Stations on 256^2 to 800^2 grids with different nt: one multi-geometry
+    launch per time step (one launch group of every job), correlations bit for
+    bit those of the single solves, on the eager run, the captured run and a
+    replay."""
+    import torch
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+    jobs = _uneven_jobs()
+    assert len({j["cfg"].nx for j in jobs}) >= 3 and len({j["cfg"].nt for j in jobs}) == len(jobs)
+    sess = DeviceSession(jobs[0]["cfg"], 0, "fp32")
+    dj = []
+    for j in jobs:
+        c = j["cfg"]
+        n_dist = j["sd"].shape[2] if j["sd"].ndim == 3 else 1
+        dj.append(dict(cfg=c, mu=to_device(j["mu"], np.float64), rho=to_device(j["rho"], np.float64),
+                       spectrum=to_device(j["spec"], np.float64), source_dist=to_device(j["sd"], np.float64),
+                       n_dist=n_dist, src=to_device(j["src"], np.float64), rec=to_device(j["rec"], np.float64),
+                       nr=j["rec"].shape[0],
+                       out=torch.zeros(j["rec"].shape[0] * c.ntc, dtype=torch.float64, device="cuda")))
+    refs = [_single(j, "fp32") for j in jobs]
+    for rep in range(3):
+        for d in dj:
+            d["out"].zero_()
+        sess.correlation_batch(dj)
+        sess.ctx.synchronize()
+        assert sess.ctx.last_batch() == [len(jobs)], sess.ctx.last_batch()
+        for i, (j, d, ref) in enumerate(zip(jobs, dj, refs)):
+            got = d["out"].cpu().numpy().reshape(j["rec"].shape[0], j["cfg"].ntc, order="F")
+            assert np.abs(ref).max() > 0
+            assert np.array_equal(got, ref), (rep, i, rel_l2(got, ref))
+    sess.ctx.close()
