@@ -437,8 +437,8 @@ def hbm_probe(args, dev):
 
 def run_batch_workload(args, w, dev, world, rank):
     """Reference stations on uneven grids in one fd2d_correlation_batch call per
-    step (device buffers); stations of one configuration share launches, the
-    others run as parallel graph branches."""
+    step (device buffers): every station advances in one multi-geometry launch
+    per time step."""
     import torch
     if world > 1:
         import torch.distributed as dist
@@ -446,7 +446,7 @@ def run_batch_workload(args, w, dev, world, rank):
         dist.barrier()
     clocks = Clocks(dev)
     clocks.start()
-    ms, launches, groups, sess, _ = batch_measure(w, dev, args.steps, args.warmup)
+    ms, launches, groups, sess, _, roof = batch_measure(w, dev, args.steps, args.warmup)
     clk = clocks.stop()
     sess.ctx.close()
     if world > 1:
@@ -464,7 +464,7 @@ def run_batch_workload(args, w, dev, world, rank):
             "config": {"workload": w.name, "stations": len(w.stations), "grids": sizes,
                        "gpt_per_step": gpt, "launch_groups": groups,
                        "l2": "inputs > L2 per step (FP64 Green spectra of every station)"},
-            "gpu_launches": int(launches * args.steps), "clocks": clk}
+            "gpu_launches": int(launches * args.steps), "clocks": clk, "roofline": roof}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -653,7 +653,22 @@ def batch_measure(w, dev, steps, warmup):
         for _ in range(steps):
             sess.correlation_batch(batch)
     ms = _time_gpu(run, sess.stream) / max(steps, 1)
-    return ms, (sess.ctx.kernel_launches - l0) / max(steps, 1), sess.ctx.last_batch(), sess, batch
+    launches = (sess.ctx.kernel_launches - l0) / max(steps, 1)
+    # one more call, instrumented: stencil time = time loops minus the
+    # contractions (and their operand images) inside them
+    sess.ctx.timing()
+    sess.ctx.set_timing(True)
+    sess.correlation_batch(batch)
+    sess.ctx.set_timing(False)
+    (msV, nV, uV), (msVU, nVU, uVU), (msC, nC, uC) = sess.ctx.timing()
+    st_ms = msV + msVU - msC
+    peak, kind = measured_peaks()
+    ach = (B_STEP_V * uV + B_STEP_VU * uVU) / (st_ms / 1e3) / 1e9 if st_ms > 0 else None
+    roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak if ach else None,
+            "peak_source": f"{kind} hbm_gbs (burst)", "kernel": "k32_step_multi (all solves, one launch per step)",
+            "stencil_ms_per_step": st_ms, "stencil_launches": nV + nVU, "contract_ms_per_step": msC,
+            "bytes_per_update": "36 (Green step) / 44 (correlation step), algorithmic"}
+    return ms, launches, sess.ctx.last_batch(), sess, batch, roof
 
 
 def batch_run(dev, steps=2, warmup=1):
@@ -666,7 +681,7 @@ def batch_run(dev, steps=2, warmup=1):
     from fd2d_noise_gb300.device import DeviceSession
     from fd2d_noise_gb300.workloads import batch_uneven
     w = batch_uneven()
-    ms, launches, groups, sess, batch = batch_measure(w, dev, steps, warmup)
+    ms, launches, groups, sess, batch, roof = batch_measure(w, dev, steps, warmup)
     gpt = w.gpt_per_step()
     sizes = {}
     for s in w.stations:
@@ -693,7 +708,7 @@ def batch_run(dev, steps=2, warmup=1):
     torch.cuda.empty_cache()
     return {"workload": w.name, "value": gpt / (ms / 1e3) / 1e9, "unit": "Gpt-updates/s", "ms_per_step": ms,
             "steps": steps, "warmup": warmup, "stations": len(w.stations), "grids": sizes, "gpt_per_step": gpt,
-            "launch_groups": groups, "gpu_launches_per_step": launches,
+            "launch_groups": groups, "gpu_launches_per_step": launches, "roofline": roof,
             "rel_l2_correlations_fp32_vs_fp64": errs}
 
 

@@ -24,10 +24,10 @@ constexpr int CONTRACT_BN = 128, CONTRACT_BK = 32;
 
 struct ContractArgs {
   int M = 0, N = 0, Kd = 0;
-  // A (Kd planes of M points) as its split image (contract_image), a_nkb K
-  // blocks per row tile
-  const float* aimg = nullptr;
-  int a_nkb = 0;
+  // A: Kd planes of M points, FP32, plane k at a32 + k*lda (lda a multiple of
+  // 4, a32 16-byte aligned); split into TF32 halves inside the contraction
+  const float* a32 = nullptr;
+  int64_t lda = 0;
   // B as its split image (contract_image): column n of this call is column
   // img_nt0*CONTRACT_BN + n of the imaged table, K row k is its row
   // img_kb0*CONTRACT_BK + k; img_nkb = K blocks of the imaged table.

@@ -7,16 +7,19 @@
 // lo*lo (~2^-22 relative), and accumulates in FP32 in tensor memory.  Spectra
 // are then accumulated across snapshot chunks in FP64.
 //
-// Both operands are first split into "images" (k_image): for each 128-row
-// tile and 32-deep K block, the hi and lo halves already in the K-major,
-// 128-byte-swizzled layout the tensor core reads, so the contraction kernel
-// itself only moves blocks with bulk copies and issues MMAs.  A is the
-// wavefield snapshot chunk or the injection planes (points contiguous), B the
-// DFT / inverse-DFT basis (one image per table, shared by every CTA).
+// B (the DFT / inverse-DFT basis, one table shared by every CTA) is split
+// once into an "image" (k_image): for each 128-row tile and 32-deep K block,
+// its hi and lo halves already in the K-major, 128-byte-swizzled layout the
+// tensor core reads.  A (the wavefield snapshot chunk or the injection P
+// planes, points contiguous, as the stencil writes them) is read as FP32 by
+// TMA, one 128-point by 32-deep block at a time, and split into the same
+// layout by converter warps in shared memory, so it crosses HBM once, at
+// 4 bytes per element.
 //
 // k_contract_tc is persistent (one CTA per SM) over 128 x 128 output tiles,
-// with a 3-stage ring of 64 KB stages (A and B blocks, hi and lo) and two TMEM
-// accumulators, so the epilogue of one tile overlaps the main loop of the next.
+// with a 3-stage ring of 64 KB stages (A and B blocks, hi and lo), a 2-deep
+// ring of raw FP32 A blocks and two TMEM accumulators, so the epilogue of one
+// tile overlaps the main loop of the next.
 // Each accumulator has two halves (all 512 TMEM columns): with k_partials = 2
 // the first half of the K blocks sums into one and the rest into the other,
 // and the epilogue adds the two FP32 partial sums.
@@ -36,7 +39,13 @@ constexpr int BM = 128, BN = CONTRACT_BN, BK = CONTRACT_BK, STAGES = 3;
 constexpr int A_BYTES = BM * BK * 4;        // 16 KB per split half
 constexpr int B_BYTES = BN * BK * 4;        // 16 KB per split half
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;  // + 1024-byte alignment slack
+// A arrives as FP32 (points contiguous, one 32-deep K block of 128 points per
+// copy) in a ring of raw buffers, and the converter warps split it into the
+// stage's hi / lo blocks
+constexpr int RAW_STAGES = 2;
+constexpr int RAW_BYTES = BM * BK * 4;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + RAW_STAGES * RAW_BYTES + 1024;  // + 1024-byte alignment slack
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory of the contraction");
 constexpr uint32_t TMEM_COLS = BN;          // one partial accumulator
 constexpr uint32_t TMEM_ALLOC = 4 * TMEM_COLS;  // 2 accumulators x 2 partials = 512 columns
 
@@ -134,23 +143,33 @@ __global__ __launch_bounds__(256) void k_image(const float* __restrict__ src, in
 }
 
 // Persistent contraction over output tiles (m_tile, n_tile), column tile
-// fastest, tile = blockIdx.x, blockIdx.x + gridDim.x, ...  Both operands come
-// as images: one bulk copy of A's block and one of B's per stage.
-//   warp 0   : one lane issues the bulk copies (STAGES-deep ring);
-//   warp 1   : allocates TMEM (two 128-column accumulators); one lane issues
-//              the MMAs (12 per K block) and commits stages and accumulators;
-//   warps 2-9: epilogue, TMEM lanes 32*(warp%4) .. +31 of the accumulator the
-//              MMAs are not writing, columns 64*((warp-2)/4) .. +63 -- it
-//              overlaps the next tile's main loop.  Two warps per TMEM lane
-//              quarter keep enough stores in flight for the FP64 spectra.
+// fastest, tile = blockIdx.x, blockIdx.x + gridDim.x, ...
+//   warp 0    : one lane issues the copies: B's image block by bulk copy into
+//               the stage (STAGES-deep ring), A's FP32 block by TMA into a
+//               raw buffer (RAW_STAGES-deep ring);
+//   warp 1    : allocates TMEM (two 128-column accumulators); one lane issues
+//               the MMAs (12 per K block) and commits stages and accumulators;
+//   warps 2-3 : split each raw A block into its hi / lo halves, written in
+//               the K-major 128-byte-swizzled layout the MMAs read;
+//   warps 4-11: epilogue, TMEM lanes 32*(warp%4) .. +31 of the accumulator the
+//               MMAs are not writing, columns 64*((warp-4)/4) .. +63 -- it
+//               overlaps the next tile's main loop.  Two warps per TMEM lane
+//               quarter keep enough stores in flight for the FP64 spectra.
 constexpr int EPI_WARPS = 8;
-constexpr int NTHREADS_P = 64 + 32 * EPI_WARPS;
+constexpr int CONV_WARPS = 2;
+constexpr int EPI_WARP0 = 2 + CONV_WARPS;
+constexpr int NTHREADS_P = 32 * EPI_WARP0 + 32 * EPI_WARPS;
+static_assert(EPI_WARP0 % 4 == 0, "epilogue warps start on a TMEM lane quarter");
 static_assert(EPI_WARPS % 4 == 0 && BN % (32 * (EPI_WARPS / 4)) == 0, "epilogue warps split the columns in 32s");
 
-__global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, int ntn, int n_tiles, int* err) {
+__global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, int ntn, int n_tiles, int* err,
+                                                              const __grid_constant__ CUtensorMap amap) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t full_bar[STAGES];   // both blocks of the stage landed (tx)
+  __shared__ __align__(8) uint64_t full_bar[STAGES];   // B's blocks of the stage landed (tx)
+  __shared__ __align__(8) uint64_t afull_bar[STAGES];  // A's split blocks of the stage written (converters)
   __shared__ __align__(8) uint64_t empty_bar[STAGES];  // MMAs done reading the stage
+  __shared__ __align__(8) uint64_t rfull_bar[RAW_STAGES];   // raw A block landed (tx)
+  __shared__ __align__(8) uint64_t rempty_bar[RAW_STAGES];  // raw A block split (converters)
   __shared__ __align__(8) uint64_t accf_bar[2];        // accumulator complete
   __shared__ __align__(8) uint64_t acce_bar[2];        // accumulator read out (every epilogue warp)
   __shared__ uint32_t tmem_base;
@@ -167,11 +186,17 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
   auto a_lo = [&](int s) { return sbase + s * STAGE_BYTES + A_BYTES; };
   auto b_hi = [&](int s) { return sbase + s * STAGE_BYTES + 2 * A_BYTES; };
   auto b_lo = [&](int s) { return sbase + s * STAGE_BYTES + 2 * A_BYTES + B_BYTES; };
+  float* raw0 = reinterpret_cast<float*>(smem + STAGES * STAGE_BYTES);  // RAW_STAGES blocks of [BK][BM]
 
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full_bar[s], 1);
+      mbar_init(&afull_bar[s], CONV_WARPS);
       mbar_init(&empty_bar[s], 1);
+    }
+    for (int r = 0; r < RAW_STAGES; ++r) {
+      mbar_init(&rfull_bar[r], 1);
+      mbar_init(&rempty_bar[r], CONV_WARPS);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf_bar[b], 1);
@@ -194,29 +219,33 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
   if (warp == 0) {
     // ---------------- bulk copies ----------------
     if (lane == 0) {
-      const unsigned char* ai = reinterpret_cast<const unsigned char*>(a.aimg);
       const unsigned char* bi = reinterpret_cast<const unsigned char*>(a.bimg);
       int g = 0;  // stage uses so far
       bool bad = false;
       for (int t = blockIdx.x; t < n_tiles && !bad; t += gridDim.x) {
         const int mt = t / ntn, nt = a.img_nt0 + (t - mt * ntn);
         for (int kb = 0; kb < nkb; ++kb, ++g) {
-          const int s = g % STAGES;
-          if (!mbar_wait_bounded_sleep(&empty_bar[s], ((g / STAGES) & 1) ^ 1) || fail) {
+          const int s = g % STAGES, r = g % RAW_STAGES;
+          if (!mbar_wait_bounded_sleep(&empty_bar[s], ((g / STAGES) & 1) ^ 1) ||
+              !mbar_wait_bounded_sleep(&rempty_bar[r], ((g / RAW_STAGES) & 1) ^ 1) || fail) {
             atomicExch(&fail, 1);
             bad = true;
             break;
           }
-          mbar_expect_tx(&full_bar[s], 2 * A_BYTES + 2 * B_BYTES);
-          bulk_copy(a_hi(s), ai + ((size_t)mt * a.a_nkb + kb) * 2 * A_BYTES, 2 * A_BYTES, &full_bar[s]);
+          mbar_expect_tx(&full_bar[s], 2 * B_BYTES);
           bulk_copy(b_hi(s), bi + ((size_t)nt * a.img_nkb + a.img_kb0 + kb) * 2 * B_BYTES, 2 * B_BYTES,
                     &full_bar[s]);
+          // rows past Kd and points past M arrive as zeros
+          mbar_expect_tx(&rfull_bar[r], RAW_BYTES);
+          tma_load_2d(raw0 + r * (BM * BK), &amap, mt * BM, kb * BK, &rfull_bar[r]);
         }
       }
       if (bad) {
         // let this CTA's copies land before it exits (bounded)
         for (int h = (g > STAGES ? g - STAGES : 0); h < g; ++h)
           mbar_wait_bounded_sleep(&full_bar[h % STAGES], (h / STAGES) & 1, 100000000ull);
+        for (int h = (g > RAW_STAGES ? g - RAW_STAGES : 0); h < g; ++h)
+          mbar_wait_bounded_sleep(&rfull_bar[h % RAW_STAGES], (h / RAW_STAGES) & 1, 100000000ull);
       }
     }
     __syncwarp();
@@ -235,7 +264,7 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           const int s = g % STAGES;
-          if (!mbar_wait_bounded(&full_bar[s], (g / STAGES) & 1)) {
+          if (!mbar_wait_bounded(&full_bar[s], (g / STAGES) & 1) || !mbar_wait_bounded(&afull_bar[s], (g / STAGES) & 1)) {
             ok = false;
             break;
           }
@@ -258,11 +287,52 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
       if (!ok) atomicExch(&fail, 1);
     }
     __syncwarp();
+  } else if (warp < EPI_WARP0) {
+    // ---------------- converters: warps 2-3 ----------------
+    // Thread c splits rows c, c + 64 of the block: 32 K values each, read down
+    // the raw block's columns (consecutive lanes: consecutive banks), written
+    // as 8 hi and 8 lo 16-byte chunks of the swizzled rows.
+    const int c = tid - 64;
+    int g = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+      for (int kb = 0; kb < nkb; ++kb, ++g) {
+        const int s = g % STAGES, r = g % RAW_STAGES;
+        ok = mbar_wait_bounded_sleep(&rfull_bar[r], (g / RAW_STAGES) & 1);
+        if (__any_sync(0xffffffffu, !ok || fail)) {
+          ok = false;
+          if (lane == 0) atomicExch(&fail, 1);
+          break;
+        }
+        const float* rb = raw0 + r * (BM * BK);
+        unsigned char* hi = smem + s * STAGE_BYTES;
+        unsigned char* lo = hi + A_BYTES;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          const int row = c + 64 * half;
+#pragma unroll
+          for (int q = 0; q < BK / 4; ++q) {
+            float h4[4], l4[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) split_tf32(rb[(4 * q + j) * BM + row], h4[j], l4[j]);
+            *reinterpret_cast<float4*>(hi + sw128(row, q)) = make_float4(h4[0], h4[1], h4[2], h4[3]);
+            *reinterpret_cast<float4*>(lo + sw128(row, q)) = make_float4(l4[0], l4[1], l4[2], l4[3]);
+          }
+        }
+        // the tensor core reads these blocks through the async proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(&rempty_bar[r]);
+          mbar_arrive(&afull_bar[s]);
+        }
+      }
+    }
   } else {
-    // ---------------- epilogue: warps 2-9 ----------------
+    // ---------------- epilogue: warps 4-11 ----------------
     const int quarter = warp & 3;  // TMEM lanes 32*quarter .. +31
     constexpr int CW = BN / (EPI_WARPS / 4);   // columns per warp
-    const int cbeg = CW * ((warp - 2) / 4);    // this warp's first column
+    const int cbeg = CW * ((warp - EPI_WARP0) / 4);  // this warp's first column
     int i = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++i) {
       const int acc = i & 1;
@@ -372,7 +442,10 @@ fd2d_status contract_image(fd2d_ctx* ctx, cudaStream_t stream, const float* src,
                            float* img) {
   if (X <= 0 || Kd <= 0) return FD2D_OK;
   dim3 grid((X + 127) / 128, (Kd + BK - 1) / BK);
+  // timed with the contractions it feeds (inside a time loop it is not stencil time)
+  const int t0 = timer_begin(ctx, stream);
   k_image<<<grid, 256, 0, stream>>>(src, ld, X, Kd, (Kd + BK - 1) / BK, img);
+  timer_end(ctx, stream, t0, FD2D_TIMER_CONTRACT, 0);
   return after_launch(ctx, "k_image");
 }
 
@@ -387,8 +460,12 @@ fd2d_status contract_prepare(fd2d_ctx* ctx) {
 fd2d_status contract(fd2d_ctx* ctx, cudaStream_t stream, const ContractArgs& a) {
   if (a.M <= 0 || a.N <= 0 || a.Kd <= 0) return FD2D_OK;
   const int nkb = (a.Kd + BK - 1) / BK;
-  if (!a.aimg || !a.bimg || a.a_nkb < nkb || a.img_nkb < nkb + a.img_kb0)
-    return set_error(ctx, FD2D_ERR_ARG, "contraction without operand images covering its K blocks");
+  if (!a.a32 || !a.bimg || a.img_nkb < nkb + a.img_kb0 || a.lda < a.M || a.lda % 4 ||
+      (reinterpret_cast<uintptr_t>(a.a32) & 15))
+    return set_error(ctx, FD2D_ERR_ARG, "contraction without an aligned A or a B image covering its K blocks");
+  // A in FP32, one 128-point by 32-deep block per copy (zeros past M and Kd)
+  CUtensorMap amap;
+  FD2D_TRY(make_tmap_f32(ctx, &amap, a.a32, a.M, a.Kd, a.lda, BM, BK));
   const int ntn = (a.N + BN - 1) / BN;
   const int64_t tiles = (int64_t)((a.M + BM - 1) / BM) * ntn;
   if (tiles > 0x7fffffff) return set_error(ctx, FD2D_ERR_SHAPE, "contraction too large for one launch");
@@ -409,7 +486,7 @@ fd2d_status contract(fd2d_ctx* ctx, cudaStream_t stream, const ContractArgs& a) 
   at[0].val.priority = prio_greatest;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_contract_tc, a, ntn, (int)tiles, ctx->d_err);
+  cudaLaunchKernelEx(&cfg, k_contract_tc, a, ntn, (int)tiles, ctx->d_err, amap);
   timer_end(ctx, stream, t0, FD2D_TIMER_CONTRACT, (int64_t)a.M * a.N * a.Kd);
   return after_launch(ctx, "k_contract_tc");
 }
@@ -426,14 +503,24 @@ extern "C" fd2d_status fd2d_contract_f32(fd2d_ctx* ctx, const float* A, int64_t 
   cudaSetDevice(ctx->device);
   FD2D_TRY(contract_prepare(ctx));
   if (M == 0 || N == 0 || Kd == 0) return FD2D_OK;
-  float *aimg = nullptr, *bimg = nullptr;
-  FD2D_TRY(workspace_t(ctx, "contract.aimg", contract_image_floats(M, Kd), &aimg));
+  // A is read by the tensor-memory copies: a 16-byte aligned copy with a row
+  // stride of a multiple of 4 floats when the caller's is not
+  const float* a32 = A;
+  int64_t la = lda;
+  if ((reinterpret_cast<uintptr_t>(A) & 15) || lda % 4) {
+    la = (M + 3) / 4 * 4;
+    float* ac = nullptr;
+    FD2D_TRY(workspace_t(ctx, "contract.a", (size_t)la * Kd, &ac));
+    FD2D_CUDA(ctx, cudaMemcpy2DAsync(ac, la * 4, A, lda * 4, (size_t)M * 4, Kd, cudaMemcpyDeviceToDevice,
+                                     ctx->stream));
+    a32 = ac;
+  }
+  float* bimg = nullptr;
   FD2D_TRY(workspace_t(ctx, "contract.bimg", contract_image_floats(N, Kd), &bimg));
-  FD2D_TRY(contract_image(ctx, ctx->stream, A, lda, M, Kd, aimg));
   FD2D_TRY(contract_image(ctx, ctx->stream, B, ldb, N, Kd, bimg));
   ContractArgs c;
   c.M = M; c.N = N; c.Kd = Kd; c.out32 = R; c.ldo = ldr;
-  c.aimg = aimg; c.a_nkb = (Kd + CONTRACT_BK - 1) / CONTRACT_BK;
-  c.bimg = bimg; c.img_nkb = c.a_nkb;
+  c.a32 = a32; c.lda = la;
+  c.bimg = bimg; c.img_nkb = (Kd + CONTRACT_BK - 1) / CONTRACT_BK;
   return contract(ctx, ctx->stream, c);
 }

@@ -968,7 +968,8 @@ extern "C" fd2d_status fd2d_correlation_batch(fd2d_ctx* ctx, const fd2d_job* job
   while (j0 < n_jobs && st == FD2D_OK) {
     int j1 = j0 + 1;
     size_t used = B[j0].bytes;
-    while (j1 < n_jobs && used + B[j1].bytes <= budget) used += B[j1++].bytes;
+    // (at most 64 jobs: the solves of one multi-geometry loop)
+    while (j1 < n_jobs && j1 - j0 < 64 && used + B[j1].bytes <= budget) used += B[j1++].bytes;
     // lane groups: jobs of one geometry (configuration) and receiver count
     // advance together, one launch per time step for the whole group
     std::vector<std::vector<int>> lanes;

@@ -616,9 +616,12 @@ struct Seg {
   double* seis;             // nrec-by-steps seismograms
 };
 
+constexpr int MULTI_MAX_SEG = 64;  // solves of one multi-geometry loop
+
 struct MultiStep {
   int n;         // time step (1-based)
   int n_seg;     // solves active at this step (a prefix of the table)
+  int tile0[MULTI_MAX_SEG];  // first CTA of each solve (the parameter bank serves the search)
   int fs;        // DFT / injection decimation
   int green;     // 1: Green run (point force, DFT of v), 0: correlation run
   int Pf;        // row pitch of the stacked field arrays
@@ -640,7 +643,7 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
     int lo = 0, hi = Q.n_seg - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) / 2;
-      if (Q.segs[mid].tile0 <= b) lo = mid;
+      if (Q.tile0[mid] <= b) lo = mid;
       else hi = mid - 1;
     }
     const Seg& g = Q.segs[lo];
@@ -1332,7 +1335,6 @@ struct Injection {
   float* P = nullptr;              // 2K planes of S lanes: [k][lane][ps]
   float* B = nullptr;              // [2K][n_events] float
   float* bimg = nullptr;           // split image of B for the tensor cores
-  float* aimg = nullptr;           // split image of the P planes
   int n_events = 0;
 };
 
@@ -1372,8 +1374,6 @@ fd2d_status build_injection(fd2d_ctx* ctx, const Geometry& g, Run& r, const doub
   FD2D_TRY(upload_tagged<float>(ctx, "f32.injB", table_tag(g, 2, inj.row_of_event),
                                 (size_t)2 * K * inj.n_events, fill, &inj.B));
   FD2D_TRY(workspace_t(ctx, "f32.inj_bimg", contract_image_floats(inj.n_events, 2 * K), &inj.bimg));
-  FD2D_TRY(workspace_t(ctx, "f32.inj_aimg", contract_image_floats((int)sps, 2 * K), &inj.aimg));
-  FD2D_TRY(contract_image(ctx, ctx->stream, inj.P, sps, (int)sps, 2 * K, inj.aimg));
   FD2D_TRY(contract_image(ctx, ctx->stream, inj.B, inj.n_events, inj.n_events, 2 * K, inj.bimg));
   const size_t cap = (size_t)4 << 30;  // resident injection planes <= 4 GiB
   inj.chunk = (int)std::max<int64_t>(1, std::min<int64_t>(inj.n_events, (int64_t)(cap / (sps * 4))));
@@ -1392,8 +1392,8 @@ fd2d_status injection_plane(fd2d_ctx* ctx, const Run& r, const Geometry& g, Inje
     inj.first = j;
     inj.count = std::min(inj.chunk, inj.n_events - j);
     ContractArgs c;
-    c.aimg = inj.aimg;
-    c.a_nkb = (2 * g.K + CONTRACT_BK - 1) / CONTRACT_BK;
+    c.a32 = inj.P;
+    c.lda = r.lanes_ps();
     c.Kd = 2 * g.K;
     c.bimg = inj.bimg;
     c.img_nt0 = j / CONTRACT_BN;
@@ -1422,7 +1422,6 @@ struct Dft {
   };
   std::vector<Target> targets;
   int n_events = 0;
-  float* aimg = nullptr;  // split image of the snapshot chunk
 };
 
 fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
@@ -1437,7 +1436,6 @@ fd2d_status dft_init(fd2d_ctx* ctx, const Run& r, int n_events, Dft& d) {
   FD2D_TRY(workspace_t(ctx, "f32.dft_snaps", (size_t)sps * d.T, &d.snaps));
   // the pitch padding of the snapshot planes is never written by the stencil
   FD2D_CUDA(ctx, cudaMemsetAsync(d.snaps, 0, (size_t)sps * d.T * 4, ctx->stream));
-  FD2D_TRY(workspace_t(ctx, "f32.dft_aimg", contract_image_floats((int)sps, d.T), &d.aimg));
   return FD2D_OK;
 }
 
@@ -1462,11 +1460,10 @@ float* dft_slot(const Run& r, Dft& d) { return d.snaps + (size_t)d.filled * r.la
 
 fd2d_status dft_flush(fd2d_ctx* ctx, const Run& r, const Geometry& g, Dft& d) {
   if (d.filled == 0) return FD2D_OK;
-  FD2D_TRY(contract_image(ctx, ctx->stream, d.snaps, r.lanes_ps(), (int)r.lanes_ps(), d.filled, d.aimg));
   for (auto& t : d.targets) {
     ContractArgs c;
-    c.aimg = d.aimg;
-    c.a_nkb = (d.filled + CONTRACT_BK - 1) / CONTRACT_BK;
+    c.a32 = d.snaps;
+    c.lda = r.lanes_ps();
     c.Kd = d.filled;
     c.bimg = t.bimg;
     c.img_kb0 = d.done / CONTRACT_BK;
@@ -1519,12 +1516,12 @@ void sig_args(Sig& sg, const Geometry& g, const SolveArgs& a) {
 }
 
 void sig_dft(Sig& sg, const Dft& d) {
-  sg.add(d.T); sg.add(d.n_events); sg.add(d.snaps); sg.add(d.aimg); sg.add(d.targets.size());
+  sg.add(d.T); sg.add(d.n_events); sg.add(d.snaps); sg.add(d.targets.size());
   for (const auto& t : d.targets) { sg.add(t.B); sg.add(t.bimg); sg.add(t.re); sg.add(t.im); sg.add(t.lane_stride); }
 }
 
 void sig_inj(Sig& sg, const Injection& j) {
-  sg.add(j.n_events); sg.add(j.chunk); sg.add(j.planes); sg.add(j.P); sg.add(j.B); sg.add(j.bimg); sg.add(j.aimg);
+  sg.add(j.n_events); sg.add(j.chunk); sg.add(j.planes); sg.add(j.P); sg.add(j.B); sg.add(j.bimg);
   sg.add_vec(j.step_of_event);
 }
 
@@ -1966,6 +1963,8 @@ struct MultiLayout {
 // step are a prefix), stacked fields, coefficient planes, node tables and
 // tensor maps.  The DFT / injection parts are added by the callers.
 fd2d_status multi_layout(fd2d_ctx* ctx, std::vector<MultiSolve>& ms, bool with_u, MultiLayout& L) {
+  if (ms.empty() || ms.size() > (size_t)MULTI_MAX_SEG)
+    return set_error(ctx, FD2D_ERR_ARG, "a multi-geometry loop takes 1 to 64 solves");
   std::stable_sort(ms.begin(), ms.end(), [](const MultiSolve& x, const MultiSolve& y) { return x.nsteps > y.nsteps; });
   L.R = ms[0].g.r;
   L.fs = ms[0].g.fs;
@@ -2173,6 +2172,7 @@ fd2d_status fp32_multi_forward1_plan(fd2d_ctx* ctx, const std::vector<const Geom
       MultiStep q{};
       q.n = n;
       q.n_seg = n_seg;
+      for (int i = 0; i < n_seg; ++i) q.tile0[i] = ms[i].seg.tile0;
       q.fs = L.fs;
       q.green = 1;
       q.Pf = L.Pf;
@@ -2252,6 +2252,7 @@ fd2d_status fp32_multi_correlation_plan(fd2d_ctx* ctx, const std::vector<const G
       MultiStep q{};
       q.n = n;
       q.n_seg = n_seg;
+      for (int i = 0; i < n_seg; ++i) q.tile0[i] = ms[i].seg.tile0;
       q.fs = L.fs;
       q.green = 0;
       q.Pf = L.Pf;

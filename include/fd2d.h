@@ -160,7 +160,7 @@ int64_t fd2d_ctx_kernel_launches(const fd2d_ctx* ctx);
 enum {
   FD2D_TIMER_STEP_V = 0,   /* stencil step without displacement (Green run)  */
   FD2D_TIMER_STEP_VU = 1,  /* stencil step with u (correlation / adjoint)    */
-  FD2D_TIMER_CONTRACT = 2, /* DFT / injection contractions                   */
+  FD2D_TIMER_CONTRACT = 2, /* DFT / injection contractions, operand images    */
   FD2D_TIMER_COUNT = 3
 };
 fd2d_status fd2d_ctx_set_timing(fd2d_ctx* ctx, int32_t enable);
