@@ -13,13 +13,14 @@
 // tensor core reads.  A (the wavefield snapshot chunk or the injection P
 // planes, points contiguous, as the stencil writes them) is read as FP32 by
 // TMA, one 128-point by 32-deep block at a time, and split into the same
-// layout by converter warps in shared memory, so it crosses HBM once, at
-// 4 bytes per element.
+// layout by converter warps in shared memory (the raw block lands in the lo
+// slot of its stage and is split in place), so it crosses HBM once, at 4
+// bytes per element.
 //
 // k_contract_tc is persistent (one CTA per SM) over 128 x 128 output tiles,
-// with a 3-stage ring of 64 KB stages (A and B blocks, hi and lo), a 2-deep
-// ring of raw FP32 A blocks and two TMEM accumulators, so the epilogue of one
-// tile overlaps the main loop of the next.
+// with a 3-stage ring of 64 KB stages (A and B blocks, hi and lo) and two
+// TMEM accumulators, so the epilogue of one tile overlaps the main loop of
+// the next.
 // Each accumulator has two halves (all 512 TMEM columns): with k_partials = 2
 // the first half of the K blocks sums into one and the rest into the other,
 // and the epilogue adds the two FP32 partial sums.
@@ -40,11 +41,11 @@ constexpr int A_BYTES = BM * BK * 4;        // 16 KB per split half
 constexpr int B_BYTES = BN * BK * 4;        // 16 KB per split half
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 // A arrives as FP32 (points contiguous, one 32-deep K block of 128 points per
-// copy) in a ring of raw buffers, and the converter warps split it into the
-// stage's hi / lo blocks
-constexpr int RAW_STAGES = 2;
+// copy) in the stage's lo slot, and the converter warps split it into the
+// stage's hi / lo blocks in place
 constexpr int RAW_BYTES = BM * BK * 4;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + RAW_STAGES * RAW_BYTES + 1024;  // + 1024-byte alignment slack
+static_assert(RAW_BYTES == A_BYTES, "the raw A block fills the lo slot of its stage");
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;  // + 1024-byte alignment slack
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory of the contraction");
 constexpr uint32_t TMEM_COLS = BN;          // one partial accumulator
 constexpr uint32_t TMEM_ALLOC = 4 * TMEM_COLS;  // 2 accumulators x 2 partials = 512 columns
@@ -144,32 +145,31 @@ __global__ __launch_bounds__(256) void k_image(const float* __restrict__ src, in
 
 // Persistent contraction over output tiles (m_tile, n_tile), column tile
 // fastest, tile = blockIdx.x, blockIdx.x + gridDim.x, ...
-//   warp 0    : one lane issues the copies: B's image block by bulk copy into
-//               the stage (STAGES-deep ring), A's FP32 block by TMA into a
-//               raw buffer (RAW_STAGES-deep ring);
+//   warp 0    : one lane issues the copies of each stage (STAGES-deep ring):
+//               B's image block by bulk copy, A's FP32 block by TMA into the
+//               stage's A lo slot;
 //   warp 1    : allocates TMEM (two 128-column accumulators); one lane issues
 //               the MMAs (12 per K block) and commits stages and accumulators;
-//   warps 2-3 : split each raw A block into its hi / lo halves, written in
-//               the K-major 128-byte-swizzled layout the MMAs read;
-//   warps 4-11: epilogue, TMEM lanes 32*(warp%4) .. +31 of the accumulator the
-//               MMAs are not writing, columns 64*((warp-4)/4) .. +63 -- it
+//   warps 2-5 : split each raw A block into its hi / lo halves, written in
+//               the K-major 128-byte-swizzled layout the MMAs read (every
+//               converter reads its row first, then all write);
+//   warps 6-13: epilogue, TMEM lanes 32*(warp%4) .. +31 of the accumulator the
+//               MMAs are not writing, columns 64*((warp-6)/4) .. +63 -- it
 //               overlaps the next tile's main loop.  Two warps per TMEM lane
 //               quarter keep enough stores in flight for the FP64 spectra.
 constexpr int EPI_WARPS = 8;
-constexpr int CONV_WARPS = 2;
+constexpr int CONV_WARPS = 4;
 constexpr int EPI_WARP0 = 2 + CONV_WARPS;
 constexpr int NTHREADS_P = 32 * EPI_WARP0 + 32 * EPI_WARPS;
-static_assert(EPI_WARP0 % 4 == 0, "epilogue warps start on a TMEM lane quarter");
+static_assert(32 * CONV_WARPS == BM, "one converter thread per row of A's block");
 static_assert(EPI_WARPS % 4 == 0 && BN % (32 * (EPI_WARPS / 4)) == 0, "epilogue warps split the columns in 32s");
 
 __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, int ntn, int n_tiles, int* err,
                                                               const __grid_constant__ CUtensorMap amap) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t full_bar[STAGES];   // B's blocks of the stage landed (tx)
+  __shared__ __align__(8) uint64_t full_bar[STAGES];   // B's blocks and the raw A block landed (tx)
   __shared__ __align__(8) uint64_t afull_bar[STAGES];  // A's split blocks of the stage written (converters)
   __shared__ __align__(8) uint64_t empty_bar[STAGES];  // MMAs done reading the stage
-  __shared__ __align__(8) uint64_t rfull_bar[RAW_STAGES];   // raw A block landed (tx)
-  __shared__ __align__(8) uint64_t rempty_bar[RAW_STAGES];  // raw A block split (converters)
   __shared__ __align__(8) uint64_t accf_bar[2];        // accumulator complete
   __shared__ __align__(8) uint64_t acce_bar[2];        // accumulator read out (every epilogue warp)
   __shared__ uint32_t tmem_base;
@@ -186,7 +186,6 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
   auto a_lo = [&](int s) { return sbase + s * STAGE_BYTES + A_BYTES; };
   auto b_hi = [&](int s) { return sbase + s * STAGE_BYTES + 2 * A_BYTES; };
   auto b_lo = [&](int s) { return sbase + s * STAGE_BYTES + 2 * A_BYTES + B_BYTES; };
-  float* raw0 = reinterpret_cast<float*>(smem + STAGES * STAGE_BYTES);  // RAW_STAGES blocks of [BK][BM]
 
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -194,10 +193,7 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
       mbar_init(&afull_bar[s], CONV_WARPS);
       mbar_init(&empty_bar[s], 1);
     }
-    for (int r = 0; r < RAW_STAGES; ++r) {
-      mbar_init(&rfull_bar[r], 1);
-      mbar_init(&rempty_bar[r], CONV_WARPS);
-    }
+
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf_bar[b], 1);
       mbar_init(&acce_bar[b], EPI_WARPS);
@@ -225,27 +221,23 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
       for (int t = blockIdx.x; t < n_tiles && !bad; t += gridDim.x) {
         const int mt = t / ntn, nt = a.img_nt0 + (t - mt * ntn);
         for (int kb = 0; kb < nkb; ++kb, ++g) {
-          const int s = g % STAGES, r = g % RAW_STAGES;
-          if (!mbar_wait_bounded_sleep(&empty_bar[s], ((g / STAGES) & 1) ^ 1) ||
-              !mbar_wait_bounded_sleep(&rempty_bar[r], ((g / RAW_STAGES) & 1) ^ 1) || fail) {
+          const int s = g % STAGES;
+          if (!mbar_wait_bounded_sleep(&empty_bar[s], ((g / STAGES) & 1) ^ 1) || fail) {
             atomicExch(&fail, 1);
             bad = true;
             break;
           }
-          mbar_expect_tx(&full_bar[s], 2 * B_BYTES);
+          mbar_expect_tx(&full_bar[s], 2 * B_BYTES + RAW_BYTES);
           bulk_copy(b_hi(s), bi + ((size_t)nt * a.img_nkb + a.img_kb0 + kb) * 2 * B_BYTES, 2 * B_BYTES,
                     &full_bar[s]);
-          // rows past Kd and points past M arrive as zeros
-          mbar_expect_tx(&rfull_bar[r], RAW_BYTES);
-          tma_load_2d(raw0 + r * (BM * BK), &amap, mt * BM, kb * BK, &rfull_bar[r]);
+          // into the lo slot; rows past Kd and points past M arrive as zeros
+          tma_load_2d(smem + s * STAGE_BYTES + A_BYTES, &amap, mt * BM, kb * BK, &full_bar[s]);
         }
       }
       if (bad) {
         // let this CTA's copies land before it exits (bounded)
         for (int h = (g > STAGES ? g - STAGES : 0); h < g; ++h)
           mbar_wait_bounded_sleep(&full_bar[h % STAGES], (h / STAGES) & 1, 100000000ull);
-        for (int h = (g > RAW_STAGES ? g - RAW_STAGES : 0); h < g; ++h)
-          mbar_wait_bounded_sleep(&rfull_bar[h % RAW_STAGES], (h / RAW_STAGES) & 1, 100000000ull);
       }
     }
     __syncwarp();
@@ -288,44 +280,49 @@ __global__ __launch_bounds__(NTHREADS_P, 1) void k_contract_tc(ContractArgs a, i
     }
     __syncwarp();
   } else if (warp < EPI_WARP0) {
-    // ---------------- converters: warps 2-3 ----------------
-    // Thread c splits rows c, c + 64 of the block: 32 K values each, read down
-    // the raw block's columns (consecutive lanes: consecutive banks), written
-    // as 8 hi and 8 lo 16-byte chunks of the swizzled rows.
+    // ---------------- converters: warps 2-5 ----------------
+    // Thread c splits row c of the block: its 32 K values are read down the
+    // raw block's columns (consecutive lanes: consecutive banks) into
+    // registers; once every converter has read (named barrier 1), the 8 hi
+    // and 8 lo 16-byte chunks of the swizzled row overwrite the stage's A slots.
     const int c = tid - 64;
     int g = 0;
-    bool ok = true;
-    for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+    bool done = false;
+    for (int t = blockIdx.x; t < n_tiles && !done; t += gridDim.x) {
       for (int kb = 0; kb < nkb; ++kb, ++g) {
-        const int s = g % STAGES, r = g % RAW_STAGES;
-        ok = mbar_wait_bounded_sleep(&rfull_bar[r], (g / RAW_STAGES) & 1);
-        if (__any_sync(0xffffffffu, !ok || fail)) {
-          ok = false;
-          if (lane == 0) atomicExch(&fail, 1);
-          break;
-        }
-        const float* rb = raw0 + r * (BM * BK);
+        const int s = g % STAGES;
+        const bool ok = mbar_wait_bounded_sleep(&full_bar[s], (g / STAGES) & 1);
         unsigned char* hi = smem + s * STAGE_BYTES;
         unsigned char* lo = hi + A_BYTES;
+        const float* rb = reinterpret_cast<const float*>(lo);
+        float x[BK];
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          const int row = c + 64 * half;
+        for (int k = 0; k < BK; ++k) x[k] = rb[k * BM + c];
+        // every converter has read the raw block (and agrees on a failure)
+        int any_bad;
+        asm volatile(
+            "{\n .reg .pred p, q;\n setp.ne.s32 q, %1, 0;\n bar.red.or.pred p, 1, %2, q;\n"
+            " selp.s32 %0, 1, 0, p;\n}\n"
+            : "=r"(any_bad)
+            : "r"((int)(!ok || fail)), "n"(32 * CONV_WARPS)
+            : "memory");
+        if (any_bad) {
+          if (c == 0) atomicExch(&fail, 1);
+          done = true;
+          break;
+        }
 #pragma unroll
-          for (int q = 0; q < BK / 4; ++q) {
-            float h4[4], l4[4];
+        for (int q = 0; q < BK / 4; ++q) {
+          float h4[4], l4[4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) split_tf32(rb[(4 * q + j) * BM + row], h4[j], l4[j]);
-            *reinterpret_cast<float4*>(hi + sw128(row, q)) = make_float4(h4[0], h4[1], h4[2], h4[3]);
-            *reinterpret_cast<float4*>(lo + sw128(row, q)) = make_float4(l4[0], l4[1], l4[2], l4[3]);
-          }
+          for (int j = 0; j < 4; ++j) split_tf32(x[4 * q + j], h4[j], l4[j]);
+          *reinterpret_cast<float4*>(hi + sw128(c, q)) = make_float4(h4[0], h4[1], h4[2], h4[3]);
+          *reinterpret_cast<float4*>(lo + sw128(c, q)) = make_float4(l4[0], l4[1], l4[2], l4[3]);
         }
         // the tensor core reads these blocks through the async proxy
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
-        if (lane == 0) {
-          mbar_arrive(&rempty_bar[r]);
-          mbar_arrive(&afull_bar[s]);
-        }
+        if (lane == 0) mbar_arrive(&afull_bar[s]);
       }
     }
   } else {
