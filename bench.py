@@ -217,11 +217,18 @@ def main():
     world, rank, local = dist_setup()
 
     from fd2d_noise_gb300.workloads import WORKLOADS
-    kw = {"nt": args.nt} if args.nt else {}
-    if args.stations:
-        kw["n_ref"] = args.stations
-    if args.grid:
-        kw["nx"] = args.grid
+    if args.workload == "batch_uneven":
+        # a smaller batch of the same kind for profiling: --stations stations,
+        # nt in [--nt, 1.5 --nt]
+        kw = {"n_stations": args.stations} if args.stations else {}
+        if args.nt:
+            kw["nt_range"] = (args.nt, args.nt + args.nt // 2)
+    else:
+        kw = {"nt": args.nt} if args.nt else {}
+        if args.stations:
+            kw["n_ref"] = args.stations
+        if args.grid:
+            kw["nx"] = args.grid
     w = WORKLOADS[args.workload](**kw)
     if args.impl == "reference":
         run_reference(args, w, world, rank)
