@@ -40,6 +40,8 @@ TILE_ROWS_AUTO = 0
 TILE_ROWS_RULE = -1
 MEAS_WAVEFORM_DIFFERENCE = 0
 MEAS_LOG_AMPLITUDE_RATIO = 1
+MEAS_CC_TIME_SHIFT = 2
+MEAS_AMPLITUDE_DIFFERENCE = 3
 
 
 class FD2DJob(ctypes.Structure):

@@ -4,8 +4,8 @@
                                              src, rec, deriv_order)
 
 mirrors tools/measurement/make_adjoint_sources.m:31 (measurements
-'log_amplitude_ratio' and 'waveform_difference'; 'amplitude_difference' and
-'cc_time_shift' are not on the structure-kernel path and raise).  u, u_0, du are
+'log_amplitude_ratio', 'waveform_difference', 'cc_time_shift' -- first order
+only, as in the reference -- and 'amplitude_difference').  u, u_0, du are
 n_rec-by-nt numpy arrays; the computation runs in libfd2d
 (fd2d_make_adjoint_sources).  ``src`` and ``rec`` are accepted for signature
 parity; the reference only uses them in commented-out window choices.
@@ -20,7 +20,9 @@ from . import _lib
 from .solvers import context
 
 KINDS = {"waveform_difference": _lib.MEAS_WAVEFORM_DIFFERENCE,
-         "log_amplitude_ratio": _lib.MEAS_LOG_AMPLITUDE_RATIO}
+         "log_amplitude_ratio": _lib.MEAS_LOG_AMPLITUDE_RATIO,
+         "cc_time_shift": _lib.MEAS_CC_TIME_SHIFT,
+         "amplitude_difference": _lib.MEAS_AMPLITUDE_DIFFERENCE}
 
 
 def _pd(a):
@@ -30,7 +32,7 @@ def _pd(a):
 def make_adjoint_sources(u, u_0, du, t, veldis, measurement, src=None, rec=None, deriv_order="1st",
                          device: int = 0):
     if measurement not in KINDS:
-        raise NotImplementedError(f"measurement {measurement!r} is not on the structure-kernel path")
+        raise ValueError(f"unknown measurement {measurement!r}")
     if deriv_order not in ("1st", "2nd"):
         raise ValueError("deriv_order must be '1st' or '2nd'")
     u = np.asfortranarray(np.array(u, dtype=np.float64, ndmin=2))

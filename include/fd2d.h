@@ -294,8 +294,10 @@ int32_t fd2d_ctx_last_batch(const fd2d_ctx* ctx, int32_t* lanes, int32_t cap);
  * [misfit_n, adstf] = make_adjoint_sources(u, u_0, du, t, veldis, measurement,
  *                                          src, rec, deriv_order)
  * tools/measurement/make_adjoint_sources.m:31-175 with log_amp_ratio.m:23-93
- * (fixed 100-200 s Hann window on the causal branch and its mirror, :87-103)
- * and waveform_difference.m:23-48 (cos-taper window over the whole axis), FP64.
+ * (fixed 100-200 s Hann window on the causal branch and its mirror, :87-103),
+ * waveform_difference.m:23-48 (cos-taper window over the whole axis),
+ * cc_time_shift.m:21-61 and amp_diff.m:22-66 (cos-taper windows over
+ * 100-200 s and -200 to -100 s, misfits and adjoint sources summed), FP64.
  *   measurement   FD2D_MEAS_*
  *   deriv_order   1 ('1st': misfit and adjoint source) or 2 ('2nd': the
  *                 Hessian adjoint source along du; misfit_n is set to 0)
@@ -305,7 +307,12 @@ int32_t fd2d_ctx_last_batch(const fd2d_ctx* ctx, int32_t* lanes, int32_t cap);
  *   misfit        out, n_rec (may be NULL)        adstf  out, n_rec-by-nt
  * The source/receiver positions of the MATLAB signature only feed commented-out
  * window choices there and are not arguments.  nt <= 20480. */
-enum { FD2D_MEAS_WAVEFORM_DIFFERENCE = 0, FD2D_MEAS_LOG_AMPLITUDE_RATIO = 1 };
+enum {
+  FD2D_MEAS_WAVEFORM_DIFFERENCE = 0,  /* tools/measurement/waveform_difference.m */
+  FD2D_MEAS_LOG_AMPLITUDE_RATIO = 1,  /* tools/measurement/log_amp_ratio.m */
+  FD2D_MEAS_CC_TIME_SHIFT = 2,        /* tools/measurement/cc_time_shift.m (first order only) */
+  FD2D_MEAS_AMPLITUDE_DIFFERENCE = 3  /* tools/measurement/amp_diff.m */
+};
 fd2d_status fd2d_make_adjoint_sources(fd2d_ctx* ctx, int32_t measurement, int32_t deriv_order, int32_t velocity,
                                       const double* u, const double* u_0, const double* du, int32_t n_rec,
                                       int32_t nt, const double* t, double* misfit, double* adstf);

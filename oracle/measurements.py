@@ -6,10 +6,15 @@ checker of the library's fd2d_make_adjoint_sources.
     make_adjoint_sources   tools/measurement/make_adjoint_sources.m:31-175
     log_amp_ratio          tools/measurement/log_amp_ratio.m:23-93
     waveform_difference    tools/measurement/waveform_difference.m:23-48
+    cc_time_shift          tools/measurement/cc_time_shift.m:21-61
+    amp_diff               tools/measurement/amp_diff.m:22-66
+    cross_correlation_td   tools/measurement/addons/cross_correlation_td.m:7-17
     get_window             tools/measurement/addons/get_window.m:1-35
 
-MATLAB's hann and trapz are restated from their documented definitions
-(symmetric Hann window; trapezoidal rule with unit spacing).  Pinned against
+MATLAB's hann, trapz and xcorr are restated from their documented
+definitions (symmetric Hann window; trapezoidal rule with unit spacing;
+xcorr(x, y)(m) = sum_n x(n + m) y(n) for lags m = -(N-1) .. N-1, a direct sum
+in ascending n).  Pinned against
 tests/golden/measurement_cases.npz (the reference's .m files run by the
 MATLAB-subset interpreter).
 """
@@ -96,6 +101,63 @@ def waveform_difference(u, u_0, du, win, t, deriv_order):
     return misfit, adstf[::-1]
 
 
+def xcorr(x, y):
+    """xcorr(x, y) of two real vectors of length N: lags -(N-1) .. N-1."""
+    x = np.asarray(x, dtype=np.float64).ravel()
+    y = np.asarray(y, dtype=np.float64).ravel()
+    n = x.size
+    out = np.zeros(2 * n - 1)
+    for m in range(-(n - 1), n):
+        acc = 0.0
+        for j in range(max(0, -m), min(n, n - m)):
+            acc = acc + x[j + m] * y[j]
+        out[m + n - 1] = acc
+    return out
+
+
+def cross_correlation_td(f, g, t):
+    from fd2d_noise_gb300.config import matlab_colon
+    n = np.asarray(f).size
+    dt = t[1] - t[0]
+    t_cc = matlab_colon(-(n - 1) * dt, dt, (n - 1) * dt)
+    return xcorr(g, f), t_cc
+
+
+def cc_time_shift(u, u_0, win, t):
+    if np.sum(u_0 == 0) == t.size:
+        T = 1.0
+    else:
+        cc, t_cc = cross_correlation_td(win * u, win * u_0, t)
+        T = t_cc[int(np.argmax(cc))]
+        if abs(T) > 3.5:
+            T = 0.0
+    misfit = T ** 2 / 2.0
+    dt = abs(t[1] - t[0])
+    nt = t.size
+    v = np.zeros(nt)
+    v[:nt - 1] = np.diff(u) / dt
+    adstf = T * (win ** 2 * v) / (np.sum((win * v) ** 2) * dt)
+    return misfit, adstf[::-1]
+
+
+def amp_diff(u, u_0, du, win, t, deriv_order):
+    dt = abs(t[1] - t[0])
+    energy_0 = np.sum((win * u_0) ** 2) * dt
+    measurement = (np.sum((win * u) ** 2) * dt - energy_0) / (energy_0 + EPS)
+    if deriv_order == "1st":
+        if np.sum(u_0 == 0) == t.size:
+            misfit = 1.0
+            adstf = 2 * u[::-1] / (np.sum(u ** 2) * dt)
+        else:
+            misfit = measurement ** 2 / 2
+            adstf = 2 * measurement * win ** 2 * u / np.sum((win * u_0) ** 2)
+    else:
+        misfit = None
+        adstf = (2 * measurement * win ** 2 * du / energy_0 * dt
+                 + 4 * win ** 2 * u / energy_0 ** 2 * np.sum(win ** 2 * u * du) * dt ** 2)
+    return misfit, adstf[::-1]
+
+
 def make_adjoint_sources(u, u_0, du, t, veldis, measurement, deriv_order):
     """[misfit_n, adstf] for n_rec-by-nt traces u, u_0, du."""
     t = np.asarray(t, dtype=np.float64).ravel()
@@ -127,6 +189,19 @@ def make_adjoint_sources(u, u_0, du, t, veldis, measurement, deriv_order):
         win = get_window(t, left, right, "cos_taper")
         if measurement == "waveform_difference":
             m, a = waveform_difference(u[n], u_0[n], du[n], win, t, deriv_order)
+        elif measurement in ("cc_time_shift", "amplitude_difference"):
+            if measurement == "cc_time_shift" and deriv_order != "1st":
+                raise ValueError("no Hessian vector products for traveltime measurements")
+            # the causal window, then [left, right] = swap(-left, -right)
+            win_a = get_window(t, -right, -left, "cos_taper")
+            if measurement == "cc_time_shift":
+                mc, ac = cc_time_shift(u[n], u_0[n], win, t)
+                ma, aa = cc_time_shift(u[n], u_0[n], win_a, t)
+            else:
+                mc, ac = amp_diff(u[n], u_0[n], du[n], win, t, deriv_order)
+                ma, aa = amp_diff(u[n], u_0[n], du[n], win_a, t, deriv_order)
+            m = mc + ma if deriv_order == "1st" else None
+            a = ac + aa
         elif measurement == "log_amplitude_ratio":
             win = get_window(t, left, right, "hann")
             m, a = log_amp_ratio(u[n], u_0[n], du[n], win, t, deriv_order)

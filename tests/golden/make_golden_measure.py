@@ -2,11 +2,12 @@
 
 TEST INFRASTRUCTURE.  Runs the unmodified reference sources
 tools/measurement/make_adjoint_sources.m, log_amp_ratio.m,
-waveform_difference.m and addons/get_window.m through the MATLAB-subset
+waveform_difference.m, cc_time_shift.m, amp_diff.m, addons/get_window.m,
+addons/cross_correlation_td.m and tools/addons/swap.m through the MATLAB-subset
 interpreter (mini_matlab.py) on seeded synthetic correlations and writes inputs
 and outputs to tests/golden/measurement_cases.npz.  MATLAB's closed built-ins
-used there (hann, trapz) are restated in mini_matlab.py from their documented
-definitions.
+used there (hann, trapz, xcorr) are restated in mini_matlab.py from their
+documented definitions.
 
     python tests/golden/make_golden_measure.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
 """
@@ -64,6 +65,36 @@ def run_cases(ref_root):
                     m, ad = I.call("make_adjoint_sources",
                                    [A(u), A(obs), A(du), A(t), veldis, meas, A(src), A(rec), order], nargout=2)
                     key = f"{meas}/{veldis}/{order}/{'zero' if zero_obs else 'obs'}"
+                    out[key + "/misfit"] = np.asarray(m)
+                    out[key + "/adstf"] = np.asarray(ad)
+                    print("  ", key, flush=True)
+    # cc_time_shift and amplitude_difference: observations that are the
+    # synthetics shifted by 0.8-2.5 s (inside the 3.5 s the time-shift
+    # measurement accepts) and scaled, plus noise
+    rng2 = np.random.default_rng(12)
+    us = np.zeros((n_rec, nt))
+    u0s = np.zeros((n_rec, nt))
+    for r in range(n_rec):
+        for sgn in (1.0, -1.0):
+            t0 = sgn * rng2.uniform(120.0, 180.0)
+            amp = rng2.uniform(0.5, 2.0)
+            shift, scale = rng2.uniform(0.8, 2.5), rng2.uniform(0.8, 1.25)
+            us[r] += amp * np.exp(-((t[0] - t0) / 12.0) ** 2) * np.cos(2 * np.pi * 0.05 * (t[0] - t0))
+            t1 = t0 + sgn * shift
+            u0s[r] += scale * amp * np.exp(-((t[0] - t1) / 12.0) ** 2) * np.cos(2 * np.pi * 0.05 * (t[0] - t1))
+        u0s[r] += 0.01 * rng2.standard_normal(nt)
+    us, u0s = np.asfortranarray(us), np.asfortranarray(u0s)
+    out["in/us"], out["in/u0s"] = us, u0s
+    for meas in ("cc_time_shift", "amplitude_difference"):
+        for veldis in ("dis", "vel"):
+            for order in ("1st", "2nd"):
+                for zero_obs in (False, True):
+                    if order == "2nd" and (zero_obs or meas == "cc_time_shift"):
+                        continue
+                    obs = np.zeros_like(u0s) if zero_obs else u0s
+                    m, ad = I.call("make_adjoint_sources",
+                                   [A(us), A(obs), A(du), A(t), veldis, meas, A(src), A(rec), order], nargout=2)
+                    key = f"{meas}/{veldis}/{order}/{'zero' if zero_obs else 'shift'}"
                     out[key + "/misfit"] = np.asarray(m)
                     out[key + "/adstf"] = np.asarray(ad)
                     print("  ", key, flush=True)

@@ -718,6 +718,13 @@ def massign_into(a: Optional[np.ndarray], subs, rhs) -> np.ndarray:
     k = len(subs)
     shape = effective_shape(a, k)
     idx = [index_list(s, shape[d]) for d, s in enumerate(subs)]
+    # A(1,:) = v into an empty (or new) A: the ':' dimension takes its length
+    # from v, as in MATLAB
+    empty_colon = [d for d, sb in enumerate(subs) if isinstance(sb, ColonAll) and shape[d] == 0]
+    if len(empty_colon) == 1 and rhs.size > 1:
+        rest = int(np.prod([ix.size for d, ix in enumerate(idx) if d != empty_colon[0]]))
+        if rest and rhs.size % rest == 0:
+            idx[empty_colon[0]] = np.arange(rhs.size // rest)
     need = [max(shape[d], (ix.max() + 1) if ix.size else 0) for d, ix in enumerate(idx)]
     if need != shape:
         if k < a.ndim and any(n != s for n, s in zip(need[:-1], shape[:-1])):
@@ -852,6 +859,25 @@ def b_trapz(y):
     return A(acc)
 
 
+def b_xcorr(x, y):
+    """xcorr(x, y) of two real vectors of length N: R(m) = sum_n x(n+m) y(n)
+    for lags m = -(N-1) .. N-1 (a row for row inputs), a direct sum in
+    ascending n."""
+    xv = A(x).reshape(-1, order="F")
+    yv = A(y).reshape(-1, order="F")
+    n = xv.size
+    if yv.size != n:
+        raise MatlabError("xcorr of vectors of different lengths")
+    out = np.zeros(2 * n - 1)
+    for m in range(-(n - 1), n):
+        acc = 0.0
+        for j in range(max(0, -m), min(n, n - m)):
+            acc = acc + xv[j + m] * yv[j]
+        out[m + n - 1] = acc
+    row = A(x).shape[0] == 1
+    return np.asfortranarray(out.reshape(1, -1) if row else out.reshape(-1, 1))
+
+
 def b_hann(n):
     """Symmetric Hann window (column): 0.5*(1 - cos(2*pi*k/(N-1))), k = 0..N-1."""
     N = int(scalar(n))
@@ -949,7 +975,7 @@ BUILTINS: Dict[str, Callable] = {
     "strcmp": lambda a, b: A(isinstance(a, str) and isinstance(b, str) and a == b),
     "fprintf": lambda *a: [],
     "error": lambda *a: (_ for _ in ()).throw(MatlabError(str(a[0]) if a else "error")),
-    "find": b_find_n, "max": b_max, "sum": b_sum, "diff": b_diff, "trapz": b_trapz, "hann": b_hann,
+    "find": b_find_n, "max": b_max, "xcorr": b_xcorr, "sum": b_sum, "diff": b_diff, "trapz": b_trapz, "hann": b_hann,
     "floor_": None,
 }
 del BUILTINS["floor_"]

@@ -1,5 +1,6 @@
 """Misfits and adjoint sources (tools/measurement/make_adjoint_sources.m:31-175,
-log_amp_ratio.m:23-93, waveform_difference.m:23-48) against the golden vectors
+log_amp_ratio.m:23-93, waveform_difference.m:23-48, cc_time_shift.m:21-61,
+amp_diff.m:22-66) against the golden vectors
 of the reference's own .m files (tests/golden/measurement_cases.npz): the
 numpy oracle on CPU, the library kernel on the GPU."""
 import os
@@ -15,8 +16,14 @@ CASES = sorted({k.rsplit("/", 1)[0] for k in GOLD.files if not k.startswith("in/
 
 def _inputs(key):
     meas, veldis, order, obs = key.split("/")
-    u0 = np.zeros_like(GOLD["in/u0"]) if obs == "zero" else GOLD["in/u0"]
-    return GOLD["in/u"], u0, GOLD["in/du"], GOLD["in/t"].ravel(), veldis, meas, order
+    # the time-shift and amplitude measurements use synthetics "us" and
+    # shifted, scaled observations "u0s"
+    shifted = meas in ("cc_time_shift", "amplitude_difference")
+    u = GOLD["in/us"] if shifted else GOLD["in/u"]
+    u0 = GOLD["in/u0s"] if shifted else GOLD["in/u0"]
+    if obs == "zero":
+        u0 = np.zeros_like(u0)
+    return u, u0, GOLD["in/du"], GOLD["in/t"].ravel(), veldis, meas, order
 
 
 def _close(got, want, tol):
