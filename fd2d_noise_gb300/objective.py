@@ -216,6 +216,50 @@ def _nonzero(a) -> bool:
     return a is not None and bool(np.any(np.asarray(a) != 0))
 
 
+def eval_hessian_vector_product_source(mu, rho, spectrum, source_dist, ref_stat, array, c_data, t,
+                                       source_dist_pert, *, cfg, veldis="dis",
+                                       measurement_source="log_amplitude_ratio",
+                                       measurement_structure="log_amplitude_ratio", weighting=0.5,
+                                       precision="fp32", device=0, backend: Optional[Backend] = None):
+    """Hessian of the 'source' inversion applied to a perturbation of the noise
+    distribution, summed over stations:
+    inversion/optlib_callback_fct/eval_hessian_vector_product_source.m:40-100 --
+    per station the Green function (no receivers), the correlations of the
+    reference distribution (zero when both measurements are waveform
+    differences, :60-72) and of the perturbation, the second-order adjoint
+    sources of both measurements mixed by the weighting, and one adjoint run in
+    mode 10 with the spectrum and the Green function (the source kernel of the
+    second-order adjoint field).  Returns nx-by-nz-by-planes FP64 (source
+    planes, then mu)."""
+    be = backend or device_backend(cfg, precision, device)
+    ref_stat = np.asarray(ref_stat, dtype=np.float64).reshape(-1, 2)
+    t = np.asarray(t, dtype=np.float64).ravel()
+    nt = t.size
+    n_rec = np.asarray(array).shape[0] - 1
+    c_data = np.asarray(c_data, dtype=np.float64)
+    both_wd = measurement_source == "waveform_difference" and measurement_structure == "waveform_difference"
+    H = None
+    for i in range(ref_stat.shape[0]):
+        src = ref_stat[i:i + 1]
+        rec = receivers_of(array, src)
+        data = c_data[i * n_rec:(i + 1) * n_rec]
+        G_fft, _, _ = be.forward1(mu, rho, src, np.zeros((0, 2)), 0, None, None)
+        if both_wd:
+            c_ref = 0.0 * data
+        else:
+            c_ref, _ = be.correlation(mu, rho, G_fft, spectrum, source_dist, rec, 0, None, None)
+            c_ref = np.asarray(c_ref).reshape(n_rec, nt)
+        c_pert, _ = be.correlation(mu, rho, G_fft, spectrum, source_dist_pert, rec, 0, None, None)
+        c_pert = np.asarray(c_pert).reshape(n_rec, nt)
+        _, a_s = be.measure(c_ref, data, c_pert, t, veldis, measurement_source, "2nd")
+        _, a_t = be.measure(c_ref, data, c_pert, t, veldis, measurement_structure, "2nd")
+        a2 = ((1.0 - weighting) * np.asarray(a_s) + weighting * np.asarray(a_t)).astype(np.complex128)
+        h, _, _, _ = be.adjoint(mu, rho, None, a2, rec, None, spectrum, None, G_fft, 10, None, None)
+        h = np.asarray(h, dtype=np.float64)
+        H = h if H is None else H + h
+    return H
+
+
 def eval_hessian_vector_product(mu, rho, spectrum, source_dist, ref_stat, array, c_data, t, dmu,
                                 source_dist_pert=None, *, cfg, type="structure", veldis="dis",
                                 measurement_source="log_amplitude_ratio",

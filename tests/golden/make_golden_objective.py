@@ -14,7 +14,8 @@ found, so every station computes its Green function.  Cases: the 'source',
 waveform-difference source measurement and a log-amplitude-ratio structure
 measurement mixed by the weighting; and eval_hessian_vector_product.m for the
 'structure' and 'joint' types (its model-space regularisation term set to
-zero, its Hessian map an identity).  Outputs go to
+zero, its Hessian map an identity) and eval_hessian_vector_product_source.m
+for the 'source' type.  Outputs go to
 tests/golden/objective_cases.npz.
 
     python tests/golden/make_golden_objective.py <path-to-reference-checkout> (or FD2D_REFERENCE set)
@@ -139,6 +140,22 @@ def main():
         Hm = I.call("eval_hessian_vector_product", [m, dm, "abcdefgh", usr_par], nargout=1)[0]
         out[f"hvp/{typ}/H"] = np.asarray(Hm, dtype=np.float64).reshape(m.shape, order="F")
         print(f"  hvp {typ}: |H| = {np.linalg.norm(Hm):.4g}", flush=True)
+    # eval_hessian_vector_product_source.m: a perturbation of the noise
+    # distribution (the mu plane of dm zero), the same measurement mix
+    cfg = cfg4()
+    dm = np.asfortranarray(np.concatenate([ds, 0 * p["dmu"][:, :, None]], axis=2))
+    usr_par = {"config": {"nx": A(float(cfg.nx)), "nz": A(float(cfg.nz))},
+               "data": {"t": np.asfortranarray(p["t"].reshape(1, -1)), "c_data": c_data},
+               "network": {"ref_stat": np.asfortranarray(p["ref"]), "array": np.asfortranarray(p["arr"])},
+               "type": "source", "veldis": "dis", "verbose": "no",
+               "measurement": {"source": "waveform_difference", "structure": "log_amplitude_ratio"},
+               "kernel": {"weighting": A(WEIGHTING)}}
+    sov = dict(ov)
+    sov["map_Hparameters_to_Hm"] = lambda H, *_: [np.asfortranarray(np.asarray(H).reshape(-1, 1, order="F"))]
+    I = Interpreter(paths, sov)
+    Hm = I.call("eval_hessian_vector_product_source", [m, dm, "abcdefgh", usr_par], nargout=1)[0]
+    out["hvp/source/H"] = np.asarray(Hm, dtype=np.float64).reshape(m.shape, order="F")
+    print(f"  hvp source: |H| = {np.linalg.norm(Hm):.4g}", flush=True)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({os.path.getsize(OUT) / 1e3:.1f} kB, {len(out)} arrays)")
 

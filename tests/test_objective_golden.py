@@ -1,6 +1,6 @@
 """The misfit/gradient and Hessian-vector orchestration against the
-reference's own inversion/optlib_callback_fct/eval_objective_and_gradient.m
-and eval_hessian_vector_product.m.
+reference's own inversion/optlib_callback_fct/eval_objective_and_gradient.m,
+eval_hessian_vector_product.m and eval_hessian_vector_product_source.m.
 
 tests/golden/objective_cases.npz holds what that file returns when the
 MATLAB-subset interpreter runs it (tests/golden/make_golden_objective.py) with
@@ -67,3 +67,40 @@ def test_hessian_vector_product_matches_reference(typ):
             assert not np.any(H[:, :, q])
         else:
             assert np.linalg.norm(H[:, :, q] - Hr[:, :, q]) <= 1e-12 * n, q
+
+
+def _source_hvp(backend, cfg, p):
+    from fd2d_noise_gb300.objective import eval_hessian_vector_product_source
+    return eval_hessian_vector_product_source(p["mu0"], p["rho"], p["spec"], p["sd"], GOLDEN["ref_stat"],
+                                              GOLDEN["array"], GOLDEN["c_data"], GOLDEN["t"], GOLDEN["hvp/ds"],
+                                              cfg=cfg, veldis="dis", measurement_source="waveform_difference",
+                                              measurement_structure="log_amplitude_ratio",
+                                              weighting=float(GOLDEN["weighting"]), backend=backend)
+
+
+def _close_planes(H, Hr, tol):
+    assert H.shape == Hr.shape
+    for q in range(H.shape[2]):
+        n = np.linalg.norm(Hr[:, :, q])
+        if n == 0:
+            assert not np.any(H[:, :, q]), q
+        else:
+            assert np.linalg.norm(H[:, :, q] - Hr[:, :, q]) <= tol * n, (q, np.linalg.norm(H[:, :, q] - Hr[:, :, q]) / n)
+
+
+def test_source_hessian_vector_product_matches_reference():
+    """eval_hessian_vector_product_source.m (Green function, correlations of
+    the reference and the perturbed distribution, second-order adjoint
+    sources, adjoint mode 10) on the oracle."""
+    cfg = cfg4()
+    p = problem(cfg)
+    _close_planes(_source_hvp(oracle_backend(cfg), cfg, p), GOLDEN["hvp/source/H"], 1e-12)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", 1e-4)])
+def test_gpu_source_hessian_vector_product(fd2d_lib, prec, tol):
+    from fd2d_noise_gb300.objective import gpu_backend
+    cfg = cfg4()
+    p = problem(cfg)
+    _close_planes(_source_hvp(gpu_backend(cfg, prec), cfg, p), GOLDEN["hvp/source/H"], tol)
