@@ -33,7 +33,7 @@ EXPORTED = [
     "fd2d_ctx_set_timing", "fd2d_ctx_timing", "fd2d_contract_f32",
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
     "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch", "fd2d_ctx_release", "fd2d_ctx_workspace_bytes",
-    "fd2d_gaussblur2d", "fd2d_ctx_set_chunks", "fd2d_ctx_set_tile_rows", "fd2d_ctx_last_tile_rows",
+    "fd2d_gaussblur2d", "fd2d_imfilter_circular", "fd2d_ctx_set_chunks", "fd2d_ctx_set_tile_rows", "fd2d_ctx_last_tile_rows",
     "fd2d_ctx_set_shared_gpu", "fd2d_device_free_bytes",
 ]
 TILE_ROWS_AUTO = 0
@@ -102,6 +102,7 @@ def load(path: str = LIB_PATH):
         L.fd2d_ctx_release.argtypes = [_vp, ctypes.POINTER(_i64)]
         L.fd2d_device_free_bytes.argtypes = [_i32, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]
         L.fd2d_gaussblur2d.argtypes = [_vp, _vp, _i32, _i32, _vp, _vp, ctypes.c_double, ctypes.c_double, _vp]
+        L.fd2d_imfilter_circular.argtypes = [_vp, _vp, _i32, _i32, _vp, _i32, _i32, _vp]
         L.fd2d_last_error.argtypes = [_vp]
         L.fd2d_last_error.restype = ctypes.c_char_p
         L.fd2d_query_sizes.argtypes = [_cfgp, _i32, ctypes.POINTER(FD2DSizes)]

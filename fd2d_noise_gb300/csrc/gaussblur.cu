@@ -9,6 +9,13 @@
 // The weights of each axis are formed once (n^2 exponentials); each pass then
 // gives every output element to one thread, which sums its in-range terms with
 // j ascending -- the reference's summation order.
+//
+// The 'ring' parameterisation (map_m_to_parameters.m:22-29,
+// map_gradparameters_to_gradm.m:27-35) smooths the structure plane with
+// imfilter(Y, h, 'circular') of MATLAB's Image Processing Toolbox instead:
+// correlation with h, output the size of Y, Y extended periodically, the centre
+// of h at floor((size(h)+1)/2).  k_imfilter_circular gives each output element
+// to one thread, adding the terms v-major, u-minor.
 #include "common.cuh"
 
 namespace fd2d {
@@ -62,6 +69,26 @@ __global__ void k_gb_pass2(const double* W2, const double* M, const double* w1, 
   GY[r + (int64_t)n1 * i] = acc / __dmul_rn(w1[r], w2[i]);
 }
 
+__device__ __forceinline__ int wrap_index(int k, int n) {
+  k %= n;
+  return k < 0 ? k + n : k;
+}
+
+// B(i, j) = sum_{v, u} h(u, v) Y((i + u - c1) mod n1, (j + v - c2) mod n2), all column-major.
+__global__ void k_imfilter_circular(const double* Y, int n1, int n2, const double* h, int m1, int m2,
+                                    double* B) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i >= n1 || j >= n2) return;
+  const int c1 = (m1 + 1) / 2 - 1, c2 = (m2 + 1) / 2 - 1;
+  double acc = 0.0;
+  for (int v = 0; v < m2; ++v) {
+    const double* col = Y + (int64_t)n1 * wrap_index(j + v - c2, n2);
+    for (int u = 0; u < m1; ++u)
+      acc = __dadd_rn(acc, __dmul_rn(h[u + (int64_t)m1 * v], col[wrap_index(i + u - c1, n1)]));
+  }
+  B[i + (int64_t)n1 * j] = acc;
+}
+
 }  // namespace
 }  // namespace fd2d
 
@@ -100,5 +127,24 @@ extern "C" fd2d_status fd2d_gaussblur2d(fd2d_ctx* ctx, const double* Y, int32_t 
   k_gb_pass2<<<dim3((n1 + B - 1) / B, n2), B, 0, s>>>(W2, M, w1, w2, n1, n2, (double*)out);
   FD2D_TRY(after_launch(ctx, "k_gb_pass2"));
   FD2D_TRY(stage_out(ctx, GY, out, nm * 8));
+  return finish_call(ctx);
+}
+
+extern "C" fd2d_status fd2d_imfilter_circular(fd2d_ctx* ctx, const double* Y, int32_t n1, int32_t n2,
+                                              const double* h, int32_t m1, int32_t m2, double* B) {
+  FD2D_TRY(check_ctx(ctx));
+  if (n1 < 1 || n2 < 1 || m1 < 1 || m2 < 1 || !Y || !h || !B)
+    return set_error(ctx, FD2D_ERR_ARG, "imfilter_circular needs n1, n2, m1, m2 >= 1 and arrays");
+  const size_t nm = (size_t)n1 * n2, hm = (size_t)m1 * m2;
+  const void *y, *hh;
+  FD2D_TRY(stage_in(ctx, "imf.Y", Y, nm * 8, &y));
+  FD2D_TRY(stage_in(ctx, "imf.h", h, hm * 8, &hh));
+  void* out;
+  FD2D_TRY(out_buffer(ctx, "imf.B", B, nm * 8, &out));
+  const int T = 128;
+  k_imfilter_circular<<<dim3((n1 + T - 1) / T, n2), T, 0, ctx->stream>>>((const double*)y, n1, n2,
+                                                                          (const double*)hh, m1, m2, (double*)out);
+  FD2D_TRY(after_launch(ctx, "k_imfilter_circular"));
+  FD2D_TRY(stage_out(ctx, B, out, nm * 8));
   return finish_call(ctx);
 }

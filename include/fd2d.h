@@ -325,6 +325,15 @@ fd2d_status fd2d_make_adjoint_sources(fd2d_ctx* ctx, int32_t measurement, int32_
 fd2d_status fd2d_gaussblur2d(fd2d_ctx* ctx, const double* Y, int32_t n1, int32_t n2, const double* x1,
                              const double* x2, double sigma1, double sigma2, double* GY);
 
+/* B = imfilter(Y, h, 'circular') -- the structure-plane smoothing of the 'ring'
+ * parameterisation (inversion/optlib_callback_fct/map_m_to_parameters.m:28,
+ * map_gradparameters_to_gradm.m:34), FP64: correlation with the m1-by-m2
+ * kernel h, output n1-by-n2 like Y, Y extended periodically, the centre of h at
+ * floor((size(h)+1)/2) (1-based).  Arrays are column-major and follow the
+ * context's memspace. */
+fd2d_status fd2d_imfilter_circular(fd2d_ctx* ctx, const double* Y, int32_t n1, int32_t n2, const double* h,
+                                   int32_t m1, int32_t m2, double* B);
+
 /* ---- building block ----------------------------------------------------------
  * R[n*ldr + m] = sum_{k<Kd} A[k*lda + m] * B[k*ldb + n]  for m < M, n < N:
  * the split-TF32 tensor-core contraction behind the on-the-fly DFT

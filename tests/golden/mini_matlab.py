@@ -1026,11 +1026,15 @@ class Interpreter:
                 sh.append(1)
             out = sh[:nargout - 1] + [int(np.prod(sh[nargout - 1:]))]
             return [A(float(d)) for d in out]
-        if name == "find" and nargout == 2 and len(args) == 1:
-            # [row, col] = find(A): 1-based subscripts of the nonzeros, column-major order
+        if name == "find" and nargout == 2 and len(args) in (1, 2, 3):
+            # [row, col] = find(A[, k[, 'first'|'last']]): 1-based subscripts of
+            # the nonzeros, column-major order, the first (or last) k of them
             a = A(args[0])
             a = a.reshape(a.shape[0], -1, order="F")
             lin = np.nonzero(a.reshape(-1, order="F") != 0)[0]
+            if len(args) > 1:
+                k = int(scalar(args[1]))
+                lin = lin[-k:] if len(args) > 2 and str(args[2]) == "last" else lin[:k]
             r, c = lin % a.shape[0] + 1.0, lin // a.shape[0] + 1.0
             return [r.reshape(-1, 1), c.reshape(-1, 1)]
         if name in BUILTINS:
