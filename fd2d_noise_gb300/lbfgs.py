@@ -3,6 +3,8 @@
     optlib_lbfgs   inversion/optlib/optlib_lbfgs.m:1-210
     optlib_wolfe   inversion/optlib/optlib_wolfe.m:1-159
     defaults       inversion/optlib/optlib_init_default_parameters_lbfgs.m
+    restore        inversion/optlib_callback_fct/optlib_restore_lbfgs_information.m:20-54
+    model history  inversion/optlib_callback_fct/new_iteration.m:31 (usr_par.model(it+1) = model)
 
 Vectors are torch FP64 tensors on the device of ``m0`` (CUDA or CPU); the
 callbacks receive and return tensors of that device: ``fun(m) -> (j, g)``
@@ -10,12 +12,26 @@ callbacks receive and return tensors of that device: ``fun(m) -> (j, g)``
 ``fun_g(m) -> g`` (eval_grad_objective).  The iteration log, the stopping rules
 (relative gradient norm, iteration cap, stagnation over
 ``successive_iterations``) and the curvature / descent-angle safeguards are
-the reference's; file output and the restore of earlier iterations are not.
+the reference's.
+
+``Result.models`` is the reference's ``usr_par.model``: one entry per iteration
+(``m``, ``objective``, ``gradient``, ``normg``), entry ``it`` written when
+iteration ``it`` ends.  Passing it back as ``stored`` warm-starts a new run as
+optlib_restore_lbfgs_information.m does: entry 0 becomes the new start, and up
+to five of the remaining most recent entries (all but the last) seed the
+curvature pairs, ``rho`` and the initial scaling.  The restored ring pointer is
+the reference's (``l = ln = l_history``): the first new pair overwrites the
+newest restored one, and the recursion visits the restored pairs in the
+reference's order.
+
+``Options.output_file`` appends the reference's iteration table
+(iterations_lbfgs.tab: one line per iteration, the descent-angle and curvature
+warnings and the termination line) in its format; None writes no file.
 """
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from typing import Callable, Optional
+from typing import Callable, List, Optional
 
 import numpy as np
 
@@ -39,6 +55,10 @@ class Options:
     successive_change: float = 1e0
     successive_iterations: int = 5
     bisection_max: int = 5
+    output_file: Optional[str] = None  # the reference writes 'iterations_lbfgs.tab'
+
+
+NUM_MOD_GRAD_STORED = 5  # optlib_restore_lbfgs_information.m:21
 
 
 @dataclass
@@ -48,6 +68,44 @@ class Result:
     objective: float
     gradient: object
     history: list = field(default_factory=list)  # (it, objective, ||g||, sigma, step)
+    models: list = field(default_factory=list)   # usr_par.model: dicts m, objective, gradient, normg
+
+
+def _num(fmt: str, v: float) -> str:
+    """One number as MATLAB's fprintf writes it (NaN and Inf spelt its way)."""
+    v = float(v)
+    if v != v:
+        return "NaN"
+    if v in (float("inf"), float("-inf")):
+        return "Inf" if v > 0 else "-Inf"
+    return fmt % v
+
+
+class _Table:
+    """The iteration table of optlib_lbfgs.m:11,25,112,169,188,198-204."""
+
+    def __init__(self, path: Optional[str]):
+        self.f = open(path, "a+") if path else None
+
+    def write(self, text: str):
+        if self.f:
+            self.f.write(text)
+
+    def close(self):
+        if self.f:
+            self.f.close()
+
+
+def restore_lbfgs_information(models: List[dict]):
+    """(previous_models, previous_gradients) as lists, oldest first, the
+    newest last: entries end-1-maxprev .. end-2 of ``models`` (all but the
+    last, at most NUM_MOD_GRAD_STORED)."""
+    nprev = len(models) - 1
+    if nprev <= 0:
+        return [], []
+    maxprev = min(nprev, NUM_MOD_GRAD_STORED)
+    picked = [models[len(models) - 1 - iprev] for iprev in range(maxprev, 0, -1)]
+    return [e["m"] for e in picked], [e["gradient"] for e in picked]
 
 
 def wolfe(xj, s, stg, f, delta, theta, sig0, try_larger, fun, fun_j, fun_g, bisection_max=5):
@@ -100,22 +158,60 @@ def wolfe(xj, s, stg, f, delta, theta, sig0, try_larger, fun, fun_j, fun_g, bise
 
 
 def lbfgs(m0, fun: Callable, fun_j: Optional[Callable] = None, fun_g: Optional[Callable] = None,
-          options: Optional[Options] = None) -> Result:
+          options: Optional[Options] = None, stored: Optional[List[dict]] = None) -> Result:
     import torch
     o = options or Options()
     fun_j = fun_j or (lambda x: fun(x)[0])
     fun_g = fun_g or (lambda x: fun(x)[1])
+    table = _Table(o.output_file)
+    try:
+        return _lbfgs(m0, fun, fun_j, fun_g, o, list(stored or []), table, torch)
+    finally:
+        table.close()
+
+
+def _new_iteration(models: list, it: int, m, j: float, g, normg: float):
+    entry = dict(m=m, objective=float(j), gradient=g, normg=normg)
+    if it < len(models):
+        models[it] = entry
+    else:
+        models.append(entry)
+
+
+def _lbfgs(m0, fun, fun_j, fun_g, o: Options, models: list, table: _Table, torch) -> Result:
     m = m0.to(torch.float64).clone()
     j, g = fun(m)
     normg0 = float(torch.linalg.norm(g))
     normg = normg0
+    _new_iteration(models, 0, m, j, g, normg)
+    table.write("it=%d   j=%s   ||g||=%s  \n" % (0, _num("%e", j), _num("%e", normg)))
     hist = [(0, float(j), normg, None, None)]
-    n, lmax = m.numel(), o.max_memory
-    P = torch.zeros((lmax, n), dtype=torch.float64, device=m.device)
-    D = torch.zeros_like(P)
-    rho = [0.0] * lmax
-    ga = [0.0] * lmax
-    l, ln, gak = 0, 1, 1.0  # ln is the reference's 1-based ring position
+    n = m.numel()
+    prev_m, prev_g = restore_lbfgs_information(models)
+    l_history = len(prev_m)
+    if l_history > 0:
+        lmax = max(o.max_memory, l_history)
+        P = torch.zeros((lmax, n), dtype=torch.float64, device=m.device)
+        D = torch.zeros_like(P)
+        rho = [0.0] * lmax
+        ga = [0.0] * lmax
+        for i in range(1, l_history):
+            P[i - 1] = prev_m[i - 1].to(m) - prev_m[i].to(m)
+            D[i - 1] = prev_g[i - 1].to(m) - prev_g[i].to(m)
+        P[l_history - 1] = prev_m[l_history - 1].to(m) - m
+        D[l_history - 1] = prev_g[l_history - 1].to(m) - g
+        for i in range(l_history):
+            rho[i] = _div(1.0, float(torch.dot(D[i], P[i])))
+        dl = D[l_history - 1]
+        gak = _div(float(torch.dot(dl, P[l_history - 1])), float(torch.linalg.norm(dl)) ** 2)
+        l = ln = min(lmax, l_history)
+    else:
+        lmax = o.max_memory
+        P = torch.zeros((lmax, n), dtype=torch.float64, device=m.device)
+        D = torch.zeros_like(P)
+        rho = [0.0] * lmax
+        ga = [0.0] * lmax
+        l, ln, gak = 0, 1, 1.0  # ln is the reference's 1-based ring position
     it = 0
     flag = None
     while normg > o.tolerance * normg0 and it < o.max_iterations:
@@ -139,12 +235,17 @@ def lbfgs(m0, fun: Callable, fun_j: Optional[Callable] = None, fun_g: Optional[C
         step = "LBFGS"
         stg = float(torch.dot(s, g))
         if _div(stg, normg * float(torch.linalg.norm(s))) < o.sufficient_decrease_angle:
+            table.write("\tWarning: Bad angle of search direction. Use steepest descent instead.\n")
             s = g.clone()  # bad angle: steepest descent
             stg = float(torch.dot(s, g))
             step = "Grad"
         sigma0 = o.init_step_length if it == 1 else 1.0
         sigma, mn, jn, gn, _ = wolfe(m, s, stg, float(j), o.wolfe_delta, o.wolfe_theta, sigma0,
                                      o.wolfe_try_to_increase_step_length, fun, fun_j, fun_g, o.bisection_max)
+        normgn = float(torch.linalg.norm(gn))
+        table.write("it=%d   j=%s   ||g||=%s   sigma=%s ||s||=%s  step=%s\n"
+                    % (it, _num("%e", jn), _num("%e", normgn), _num("%6.5f", sigma),
+                       _num("%e", float(torch.linalg.norm(s))), step))
         d = g - gn
         p = m - mn
         dtp = float(torch.dot(d, p))
@@ -155,9 +256,20 @@ def lbfgs(m0, fun: Callable, fun_j: Optional[Callable] = None, fun_g: Optional[C
             l = min(l + 1, lmax)
             ln = ln % lmax + 1
             gak = _div(dtp, float(torch.dot(d, d)))
+        else:
+            table.write("\tWarning: Bad angle of search direction. Update of BFGS curvature information "
+                        "skipped.\n")
         m, j, g = mn, jn, gn
-        normg = float(torch.linalg.norm(g))
+        normg = normgn
+        _new_iteration(models, it, m, j, g, normg)
         hist.append((it, float(j), normg, sigma, step))
-    if flag is None:
-        flag = 0 if normg <= o.tolerance * normg0 else 1
-    return Result(flag, m, float(j), g, hist)
+    if flag is None:  # optlib_lbfgs.m:197-206 (a NaN gradient norm ends the loop with flag 2)
+        flag = 0 if normg <= o.tolerance * normg0 else (1 if it >= o.max_iterations else 2)
+    if flag == 0:
+        table.write("Successful termination with ||g||<%s*min(1,||g0||):\n" % _num("%e", o.tolerance))
+    elif flag == 1:
+        table.write("Maximum number of iterations reached.\n")
+    else:
+        table.write("Improvement of misfit over %d iterations smaller than %s.\n"
+                    % (o.successive_iterations, _num("%f", o.successive_change)))
+    return Result(flag, m, float(j), g, hist, models)

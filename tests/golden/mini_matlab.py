@@ -953,7 +953,7 @@ BUILTINS: Dict[str, Callable] = {
     "isempty": lambda x: A(A(x).size == 0),
     "isscalar": lambda x: A(A(x).size == 1),
     "all": lambda x: A(bool(np.all(A(x) != 0))),
-    "numel": lambda x: A(float(A(x).size)),
+    "numel": lambda x: A(float(len(x) if isinstance(x, list) else 1 if isinstance(x, dict) else A(x).size)),
     "pi": lambda: A(np.pi),
     "complex": lambda x, y=None: np.asfortranarray(A(x).astype(np.complex128) + (0 if y is None else 1j * A(y))),
     "num2str": lambda x: str(int(scalar(x))) if float(scalar(x)).is_integer() else repr(float(scalar(x))),
@@ -1186,6 +1186,8 @@ class Interpreter:
             return v[e[2]]
         if kind == "end":
             base, d, k = self._end_stack[-1]
+            if isinstance(base, list):  # struct array
+                return A(float(len(base)))
             a = A(base)
             if k == 1:
                 return A(float(a.size))
@@ -1240,7 +1242,12 @@ class Interpreter:
             if f[0] == "field":
                 base = self.eval(f, env)
                 if isinstance(base, list):  # struct array (list of dicts), one 1-based index
-                    return base[int(scalar(self.eval(e[2][0], env))) - 1]
+                    self._end_stack.append((base, 0, 1))
+                    try:
+                        k = int(scalar(self.eval(e[2][0], env)))
+                    finally:
+                        self._end_stack.pop()
+                    return base[k - 1]
             if f[0] == "id":
                 args = [self.eval(a, env) for a in e[2]]
                 r = self.call(f[1], args, nargout=max(nargout, 1))

@@ -51,3 +51,19 @@ LBFGS_CASES = [
     ("quad_tight", quadratic, [1.0, -2.0, 3.0, -4.0, 5.0],
      dict(verbose=0, tolerance=1e-10, successive_change=0.0, init_step_length=0.01)),
 ]
+
+# Warm restarts (optlib_restore_lbfgs_information.m): name, function, start,
+# options of the first run, options of the run restarted from its final model
+# with its stored iterations.  Histories of 7 (five pairs restored), 2 (one
+# pair) and 7 entries with max_memory 3 (lmax = max(3, 5) = 5).
+RESTART_CASES = [
+    ("restart_rosen", rosenbrock, [-1.2, 1.0],
+     dict(verbose=0, max_iterations=6, successive_change=0.0),
+     dict(verbose=0, tolerance=1e-8, max_iterations=60, successive_change=0.0)),
+    ("restart_rosen_short", rosenbrock, [0.5, 0.2],
+     dict(verbose=0, max_iterations=1, successive_change=0.0),
+     dict(verbose=0, max_iterations=12, successive_change=0.0)),
+    ("restart_quad_mem3", quadratic, [1.0, -2.0, 3.0, -4.0, 5.0],
+     dict(verbose=0, max_iterations=6, successive_change=0.0, max_memory=3),
+     dict(verbose=0, tolerance=1e-9, max_iterations=40, successive_change=0.0, max_memory=3)),
+]
