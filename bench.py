@@ -619,6 +619,9 @@ def config1_run(dev):
         c = corr.cpu().numpy().reshape(nr, cfg.ntc, order="F")
         out[prec] = {"value": gpt / (ms / 1e3) / 1e9, "unit": "Gpt-updates/s", "ms": ms,
                      "rel_l2_correlations_vs_oracle": float(np.linalg.norm(c - co) / np.linalg.norm(co))}
+        if prec == "fp32":
+            out[prec]["steps_per_launch"] = sess.ctx.last_time_depth()
+            out[prec]["tile_rows"] = sess.ctx.last_tile_rows()
         if prec == "fp64":
             out[prec]["roofline"] = fp64_roofline(cfg, ms, w.spectrum.shape[1])
         sess.ctx.close()

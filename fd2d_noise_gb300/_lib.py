@@ -34,7 +34,7 @@ EXPORTED = [
     "fd2d_forward1_seismograms_noalloc", "fd2d_correlation_batch", "fd2d_ctx_set_memory_budget",
     "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch", "fd2d_ctx_release", "fd2d_ctx_workspace_bytes",
     "fd2d_gaussblur2d", "fd2d_imfilter_circular", "fd2d_ctx_set_chunks", "fd2d_ctx_set_tile_rows", "fd2d_ctx_last_tile_rows",
-    "fd2d_ctx_set_shared_gpu", "fd2d_device_free_bytes",
+    "fd2d_ctx_set_shared_gpu", "fd2d_device_free_bytes", "fd2d_ctx_set_time_depth", "fd2d_ctx_last_time_depth",
 ]
 TILE_ROWS_AUTO = 0
 TILE_ROWS_RULE = -1
@@ -97,6 +97,8 @@ def load(path: str = LIB_PATH):
         L.fd2d_ctx_set_tile_rows.argtypes = [_vp, _i32]
         L.fd2d_ctx_set_shared_gpu.argtypes = [_vp, _i32]
         L.fd2d_ctx_last_tile_rows.argtypes = [_vp]
+        L.fd2d_ctx_set_time_depth.argtypes = [_vp, _i32]
+        L.fd2d_ctx_last_time_depth.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.restype = _i64
         L.fd2d_ctx_release.argtypes = [_vp, ctypes.POINTER(_i64)]
@@ -202,6 +204,14 @@ class Context:
 
     def last_tile_rows(self) -> int:
         return int(self.L.fd2d_ctx_last_tile_rows(self.h))
+
+    def set_time_depth(self, depth: int):
+        """Steps per launch of the FP32 Green and correlation loops at orders 2
+        and 4: 1 or 2 forced, 0 timed per grid when the stream is idle."""
+        check(self.L.fd2d_ctx_set_time_depth(self.h, int(depth)), self.h)
+
+    def last_time_depth(self) -> int:
+        return int(self.L.fd2d_ctx_last_time_depth(self.h))
 
     def last_batch(self):
         """Lane counts of the launch groups of the last batch."""

@@ -148,6 +148,9 @@ struct fd2d_ctx {
   int32_t tile_rows = 0;       // step-kernel tile rows: 0 timed per grid, -1 size rule, 16 or 32 forced
   int32_t last_tile_rows = 0;  // tile rows of the last FP32 time loop set up
   std::map<uint64_t, int> tile_choice;  // tuned tile rows by (grid, order, lanes)
+  int32_t time_depth = 0;               // steps per launch: 0 timed per grid (orders 2, 4), 1 or 2 forced
+  int32_t last_time_depth = 0;          // steps per launch of the last FP32 time loop set up
+  std::map<uint64_t, int> depth_choice;  // tuned steps per launch by (grid, order, lanes, tile rows)
   int32_t concurrent_groups = 0;        // lane groups a batch runs side by side (set while planning)
   int32_t shared_gpu = 0;               // other work shares the GPU (fd2d_ctx_set_shared_gpu)
   std::vector<cudaStream_t> side_streams;

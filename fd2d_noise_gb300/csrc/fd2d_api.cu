@@ -910,6 +910,15 @@ extern "C" fd2d_status fd2d_ctx_set_tile_rows(fd2d_ctx* ctx, int32_t rows) {
 
 extern "C" int32_t fd2d_ctx_last_tile_rows(const fd2d_ctx* ctx) { return ctx ? ctx->last_tile_rows : 0; }
 
+extern "C" fd2d_status fd2d_ctx_set_time_depth(fd2d_ctx* ctx, int32_t depth) {
+  if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
+  if (depth < 0 || depth > 2) return set_error(ctx, FD2D_ERR_ARG, "time depth must be 0 (timed), 1 or 2");
+  ctx->time_depth = depth;
+  return FD2D_OK;
+}
+
+extern "C" int32_t fd2d_ctx_last_time_depth(const fd2d_ctx* ctx) { return ctx ? ctx->last_time_depth : 0; }
+
 extern "C" fd2d_status fd2d_ctx_set_shared_gpu(fd2d_ctx* ctx, int32_t shared) {
   if (!ctx) return set_error(nullptr, FD2D_ERR_ARG, "ctx is NULL");
   ctx->shared_gpu = shared ? 1 : 0;

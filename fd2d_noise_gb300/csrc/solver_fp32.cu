@@ -591,6 +591,354 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
   step_tile<R, HU, HI, TZ, false>(G, M, S, L, G.c);
 }
 
+// ---- two time steps per launch (time blocking, orders 2 and 4) ---------------------
+// One CTA advances its 32 x TZ tile by two time steps.  It loads one box of
+// every array -- x from x0-8 (56 points), z from z0-6 (TZ+12 rows), the same
+// origin for all -- and recomputes the first step on a ring wide enough for
+// the second:
+//   A  v1 on x in [x0-4, x0+39], z in [z0-4, z0+TZ+4]   (needs stresses to x0-6 .. x0+40)
+//   B  s1 on x in [x0-4, x0+35], z in [z0-3, z0+TZ+2]   (step-1 outputs on the tile)
+//   C  v2 on x in [x0-4, x0+35], z in [z0-1, z0+TZ+1]
+//   D  s2, v2, u2 on the tile, stored
+// For R <= 2 the values each phase needs lie inside what the previous phase
+// computed (v2 on the tile needs s1 on [x0-3, x0+33], which needs v1 on
+// [x0-4, x0+35]; in z likewise); points computed beyond that are never read.
+// Every point is updated by the same rounded operations as in step_tile, and
+// points outside the grid come out zero (all their inputs are the tensor
+// maps' zero fill), so fields, seismograms and snapshots are bit for bit those
+// of two launches of k32_step.
+constexpr int TB_W = 56;  // box width (floats)
+constexpr int TB_X = 8;   // box starts at x0 - TB_X
+constexpr int TB_Z = 6;   // and z0 - TB_Z
+
+template <int TZ_, bool HU, bool HI>
+struct Tile2 {
+  static constexpr int TZ = TZ_;
+  static constexpr int H = TZ + 2 * TB_Z;
+  static constexpr int NT = (TX / 4) * TZ < 256 ? (TX / 4) * TZ : 256;
+  static constexpr int A = (TB_W * H + 31) / 32 * 32;  // floats per box array (128-byte multiples)
+  static constexpr int O_SXY = 0, O_SZY = A, O_V = 2 * A, O_B = 3 * A, O_T = 4 * A, O_MU = 5 * A;
+  static constexpr int O_I = 6 * A;  // injection planes of step 1 and step 2
+  static constexpr int O_U = O_I + (HI ? 2 * A : 0);
+  static constexpr int TOTAL = O_U + (HU ? TX * TZ : 0);
+  static constexpr int BYTES = TOTAL * 4 + 128;
+  // phase ranges (box quads of 4 points, box rows)
+  static constexpr int QA0 = 1, QA1 = 11, RA0 = 2, RA1 = TZ + 10;
+  static constexpr int QB0 = 1, QB1 = 10, RB0 = 3, RB1 = TZ + 8;
+  static constexpr int QC0 = 1, QC1 = 10, RC0 = 5, RC1 = TZ + 7;
+};
+
+struct alignas(64) StepMaps2 {
+  CUtensorMap sxy, szy, v, b, taper, dtmu, inj, u;
+};
+
+struct Step2 {
+  Step32 s[2];  // steps n and n+1; outputs (vo, sxyo, szyo, uo) of s[1]
+};
+
+// v = (v + DS*b) * taper on one 4-wide item of box row r, box column c0 (R <= 2).
+template <int R, bool EDGE>
+__device__ __forceinline__ void tb_v_item(const Grid32& G, const float* cf, float* s_v, const float* s_sxy,
+                                          const float* s_szy, const float* s_b, const float* s_t, const float* s_i,
+                                          int r, int c0, int bx, int bz, const int* s_src, int nbs, float amp) {
+  constexpr int W = TB_W;
+  const int gz = bz + r;
+  const bool zin = gz >= R && gz <= G.nz - R - 1;
+  float xs[12];
+  {
+    const float4* rowp = reinterpret_cast<const float4*>(s_sxy + r * W + c0 - 4);
+#pragma unroll
+    for (int h = 0; h < 3; ++h) {
+      const float4 f = rowp[h];
+      xs[4 * h] = f.x; xs[4 * h + 1] = f.y; xs[4 * h + 2] = f.z; xs[4 * h + 3] = f.w;
+    }
+  }
+  float zs[2 * R][4];
+#pragma unroll
+  for (int k = 0; k < 2 * R; ++k) {
+    // zs[k] holds szy(gz + k - R)
+    const float4 f = *reinterpret_cast<const float4*>(s_szy + (r - R + k) * W + c0);
+    zs[k][0] = f.x; zs[k][1] = f.y; zs[k][2] = f.z; zs[k][3] = f.w;
+  }
+  float dsv[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int gx = bx + c0 + e;
+    float ax = 0.f;
+#pragma unroll
+    for (int m = 1; m <= R; ++m) ax = __fmaf_rn(cf[m - 1], __fsub_rn(xs[e + 3 + m], xs[e + 4 - m]), ax);
+    float az = 0.f;
+#pragma unroll
+    for (int m = 1; m <= R; ++m) az = __fmaf_rn(cf[m - 1], __fsub_rn(zs[R + m - 1][e], zs[R - m][e]), az);
+    float ds = (!EDGE || (gx >= R && gx <= G.nx - R - 1)) ? __fmul_rn(ax, G.inv_dx) : 0.f;
+    ds = (!EDGE || zin) ? __fmaf_rn(az, G.inv_dz, ds) : ds;
+    dsv[e] = ds;
+  }
+  const int idx0 = r * W + c0;
+  for (int qq = 0; qq < nbs; ++qq) {
+    const int d = s_src[qq] - idx0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (d == e) dsv[e] = __fadd_rn(dsv[e], amp);
+  }
+  const float4 v4 = *reinterpret_cast<const float4*>(s_v + idx0);
+  const float4 b4 = *reinterpret_cast<const float4*>(s_b + idx0);
+  const float4 t4 = *reinterpret_cast<const float4*>(s_t + idx0);
+  float4 i4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (s_i) i4 = *reinterpret_cast<const float4*>(s_i + idx0);
+  const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
+  const float tt[4] = {t4.x, t4.y, t4.z, t4.w}, ii[4] = {i4.x, i4.y, i4.z, i4.w};
+  float out[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const float ds = s_i ? __fadd_rn(dsv[e], ii[e]) : dsv[e];
+    // a taper of exactly 1 leaves the product unchanged, as step_tile's skip of it
+    out[e] = __fmul_rn(__fmaf_rn(ds, bb[e], vv[e]), tt[e]);
+  }
+  *reinterpret_cast<float4*>(s_v + idx0) = make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// sxy += mu*dx_v(v), szy += mu*dz_v(v) on one 4-wide item (stresses out of the
+// operator's range keep their value); returns the item's v in vn.
+template <int R, bool EDGE>
+__device__ __forceinline__ void tb_s_item(const Grid32& G, const float* cf, const float* s_v, const float* s_sxy,
+                                          const float* s_szy, const float* s_mu, int r, int c0, int bx, int bz,
+                                          float nsx[4], float nsz[4], float vn[4]) {
+  constexpr int W = TB_W;
+  const int j = bz + r;
+  float vx[12];
+  {
+    const float4* rowp = reinterpret_cast<const float4*>(s_v + r * W + c0 - 4);
+#pragma unroll
+    for (int h = 0; h < 3; ++h) {
+      const float4 f = rowp[h];
+      vx[4 * h] = f.x; vx[4 * h + 1] = f.y; vx[4 * h + 2] = f.z; vx[4 * h + 3] = f.w;
+    }
+  }
+  float vz[2 * R][4];  // box rows r - R + 1 .. r + R
+#pragma unroll
+  for (int k = 0; k < 2 * R; ++k) {
+    const float4 f = *reinterpret_cast<const float4*>(s_v + (r - R + 1 + k) * W + c0);
+    vz[k][0] = f.x; vz[k][1] = f.y; vz[k][2] = f.z; vz[k][3] = f.w;
+  }
+  const float4 mu4 = *reinterpret_cast<const float4*>(s_mu + r * W + c0);
+  const float4 sx4 = *reinterpret_cast<const float4*>(s_sxy + r * W + c0);
+  const float4 sz4 = *reinterpret_cast<const float4*>(s_szy + r * W + c0);
+  const float mu[4] = {mu4.x, mu4.y, mu4.z, mu4.w}, sxo[4] = {sx4.x, sx4.y, sx4.z, sx4.w};
+  const float szo[4] = {sz4.x, sz4.y, sz4.z, sz4.w};
+  const bool zin = j >= R - 1 && j <= G.nz - R - 1;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int i = bx + c0 + e;
+    vn[e] = vx[e + 4];
+    float ax = 0.f, az = 0.f;
+#pragma unroll
+    for (int m = 1; m <= R; ++m) ax = __fmaf_rn(cf[m - 1], __fsub_rn(vx[e + m + 4], vx[e - m + 5]), ax);
+#pragma unroll
+    for (int m = 1; m <= R; ++m) az = __fmaf_rn(cf[m - 1], __fsub_rn(vz[R - 1 + m][e], vz[R - m][e]), az);
+    nsx[e] = (!EDGE || (i >= R - 1 && i <= G.nx - R - 1)) ? __fmaf_rn(mu[e], __fmul_rn(ax, G.inv_dx), sxo[e]) : sxo[e];
+    nsz[e] = (!EDGE || zin) ? __fmaf_rn(mu[e], __fmul_rn(az, G.inv_dz), szo[e]) : szo[e];
+  }
+}
+
+// Outputs of one step at a tile item: DFT snapshot and receivers of the new
+// field (u with displacement, else v).
+__device__ __forceinline__ void tb_outputs(const Grid32& G, const Step32& S, bool edge, int lane, int64_t lo,
+                                           int i0, int j, int l0, const float nu[4], const float vn[4],
+                                           const int2* s_rec, int nrec) {
+  if (S.snap_dft && (!edge || j < G.nz)) {
+    const int64_t ps_ = lo + i0 + (int64_t)G.P * j;
+    if (!edge || i0 + 3 < G.nx) {
+      *reinterpret_cast<float4*>(S.snap_dft + ps_) = make_float4(nu[0], nu[1], nu[2], nu[3]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (i0 + e < G.nx) S.snap_dft[ps_ + e] = nu[e];
+    }
+  }
+  if (S.nrec) {
+    double* seis = S.seis_col + lane * S.seis_lane;
+    for (int q = 0; q < nrec; ++q) {
+      const int2 e = s_rec[q];
+      const int d = e.y - l0;
+      if (d >= 0 && d < 4) {
+        const float xu = d == 0 ? nu[0] : d == 1 ? nu[1] : d == 2 ? nu[2] : nu[3];
+        const float xv = d == 0 ? vn[0] : d == 1 ? vn[1] : d == 2 ? vn[2] : vn[3];
+        seis[e.x] = (double)(S.rec_u ? xu : xv);
+      }
+    }
+  }
+}
+
+template <int R, bool HU, bool HI, int TZ>
+__global__ __launch_bounds__(Tile2<TZ, HU, HI>::NT) void k32_step2(Grid32 G, const __grid_constant__ StepMaps2 M,
+                                                                    Step2 Q) {
+  using T = Tile2<TZ, HU, HI>;
+  constexpr int NT = T::NT, W = TB_W;
+  static_assert(R <= 2, "two steps per launch need R <= 2 (orders 2 and 4)");
+  extern __shared__ __align__(128) unsigned char sm_raw[];
+  float* sm = reinterpret_cast<float*>(sm_raw + ((128u - (smem_u32(sm_raw) & 127u)) & 127u));
+  __shared__ __align__(8) uint64_t bar[1];
+  __shared__ int s_src[MAX_BOX_SRC];
+  __shared__ int s_nsrc;
+  __shared__ int2 s_rec[MAX_TILE_REC];
+  __shared__ int s_nrec;
+  const Step32& S0 = Q.s[0];
+  const Step32& S1 = Q.s[1];
+  const int tid = threadIdx.x;
+  const int lane = blockIdx.z, x0 = blockIdx.x * TX, z0 = blockIdx.y * TZ;
+  const int bx = x0 - TB_X, bz = z0 - TB_Z;
+  const int64_t lo = (int64_t)lane * G.ps;
+  const int t = blockIdx.x + G.ntx * (blockIdx.y + G.ntz * lane);
+  const float* cf = G.c;
+  const bool inj0 = HI && S0.inj_plane >= 0, inj1 = HI && S1.inj_plane >= 0;
+  if (tid == 0) {
+    s_nsrc = 0;
+    s_nrec = 0;
+    mbar_init(&bar[0], 1);
+    fence_mbar_init();
+    const uint32_t box = 4u * W * T::H;
+    uint32_t bytes = 6u * box + (inj0 ? box : 0u) + (inj1 ? box : 0u) + (HU ? 4u * TX * TZ : 0u);
+    mbar_expect_tx(&bar[0], bytes);
+    // coefficients and injection planes are not written by the time loop
+    tma_load_3d(sm + T::O_B, &M.b, bx, bz, lane, &bar[0]);
+    tma_load_3d(sm + T::O_T, &M.taper, bx, bz, lane, &bar[0]);
+    tma_load_3d(sm + T::O_MU, &M.dtmu, bx, bz, lane, &bar[0]);
+    if (inj0) tma_load_3d(sm + T::O_I, &M.inj, bx, bz, S0.inj_plane * G.S + lane, &bar[0]);
+    if (inj1) tma_load_3d(sm + T::O_I + T::A, &M.inj, bx, bz, S1.inj_plane * G.S + lane, &bar[0]);
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    tma_load_3d(sm + T::O_SXY, &M.sxy, bx, bz, lane, &bar[0]);
+    tma_load_3d(sm + T::O_SZY, &M.szy, bx, bz, lane, &bar[0]);
+    tma_load_3d(sm + T::O_V, &M.v, bx, bz, lane, &bar[0]);
+    if (HU) tma_load_3d(sm + T::O_U, &M.u, x0, z0, lane, &bar[0]);
+  }
+  __syncthreads();
+  if (S0.nrec && tid < 32 && S0.tile_rec) {
+    const int2 se = S0.tile_rec[t];
+    if (tid == 0) {
+      s_nrec = se.y <= MAX_TILE_REC ? se.y : MAX_TILE_REC;
+      if (se.y > MAX_TILE_REC) set_error_flag(G.err, 1);  // the host pairs steps only below this
+    }
+    for (int q = tid; q < se.y && q < MAX_TILE_REC; q += 32) s_rec[q] = S0.rec_ent[se.x + q];
+  }
+  {
+    const int2* src_xy = S0.src_xy + (int64_t)lane * S0.nsrc;
+    for (int k = tid; k < S0.nsrc; k += NT) {
+      const int2 q = src_xy[k];
+      if (q.x >= bx && q.x < bx + W && q.y >= bz && q.y < bz + T::H) {
+        const int slot = atomicAdd(&s_nsrc, 1);
+        if (slot < MAX_BOX_SRC) s_src[slot] = (q.y - bz) * W + (q.x - bx);
+        else set_error_flag(G.err, 1);  // the host pairs steps only below this
+      }
+    }
+  }
+  bool ok = true;
+  if (tid < 32) ok = mbar_wait_bounded_sleep(&bar[0], 0);
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) {
+      set_error_flag(G.err, 1);
+      mbar_wait_bounded_sleep(&bar[0], 0, 100000000ull);  // let started copies land (bounded)
+    }
+    return;
+  }
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  const int nbs = min(s_nsrc, MAX_BOX_SRC), nrec = s_nrec;
+  float* s_sxy = sm + T::O_SXY;
+  float* s_szy = sm + T::O_SZY;
+  float* s_v = sm + T::O_V;
+  const float* s_b = sm + T::O_B;
+  const float* s_t = sm + T::O_T;
+  const float* s_mu = sm + T::O_MU;
+  float* s_u = sm + T::O_U;
+  const float* s_i0 = inj0 ? sm + T::O_I : nullptr;
+  const float* s_i1 = inj1 ? sm + T::O_I + T::A : nullptr;
+  // every computed point (phase A reaches furthest) inside the operators' ranges
+  const bool edge = !(x0 - 4 >= R && x0 + 40 + R <= G.nx && z0 - 4 >= R && z0 + TZ + 5 + R <= G.nz);
+  auto run = [&](auto edge_tag) {
+    constexpr bool EDGE = decltype(edge_tag)::value;
+    constexpr int NQA = T::QA1 - T::QA0 + 1, NQB = T::QB1 - T::QB0 + 1, NQC = T::QC1 - T::QC0 + 1;
+    // A: v1
+    for (int it = tid; it < NQA * (T::RA1 - T::RA0 + 1); it += NT)
+      tb_v_item<R, EDGE>(G, cf, s_v, s_sxy, s_szy, s_b, s_t, s_i0, T::RA0 + it / NQA, 4 * (T::QA0 + it % NQA), bx,
+                         bz, s_src, nbs, S0.amp_const);
+    __syncthreads();
+    // B: s1 (in place: an item reads its own old stresses only); step-1 outputs on the tile
+    for (int it = tid; it < NQB * (T::RB1 - T::RB0 + 1); it += NT) {
+      const int r = T::RB0 + it / NQB, c0 = 4 * (T::QB0 + it % NQB);
+      float nsx[4], nsz[4], vn[4];
+      tb_s_item<R, EDGE>(G, cf, s_v, s_sxy, s_szy, s_mu, r, c0, bx, bz, nsx, nsz, vn);
+      *reinterpret_cast<float4*>(s_sxy + r * W + c0) = make_float4(nsx[0], nsx[1], nsx[2], nsx[3]);
+      *reinterpret_cast<float4*>(s_szy + r * W + c0) = make_float4(nsz[0], nsz[1], nsz[2], nsz[3]);
+      const int tr = r - TB_Z, tq = c0 / 4 - TB_X / 4;  // tile row and quad
+      if (tr >= 0 && tr < TZ && tq >= 0 && tq < TX / 4) {
+        const int j = z0 + tr, i0 = x0 + 4 * tq;
+        float nu[4];
+        if (HU) {
+          float* up = s_u + tr * TX + 4 * tq;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) nu[e] = __fmaf_rn(vn[e], G.dt, up[e]);
+          *reinterpret_cast<float4*>(up) = make_float4(nu[0], nu[1], nu[2], nu[3]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) nu[e] = vn[e];
+        }
+        if (!EDGE || (j < G.nz && i0 < G.nx))
+          tb_outputs(G, S0, EDGE, lane, lo, i0, j, tr * TX + 4 * tq, nu, vn, s_rec, nrec);
+      }
+    }
+    __syncthreads();
+    // C: v2
+    for (int it = tid; it < NQC * (T::RC1 - T::RC0 + 1); it += NT)
+      tb_v_item<R, EDGE>(G, cf, s_v, s_sxy, s_szy, s_b, s_t, s_i1, T::RC0 + it / NQC, 4 * (T::QC0 + it % NQC), bx,
+                         bz, s_src, nbs, S1.amp_const);
+    __syncthreads();
+    // D: s2, u2 and the stores of the tile
+    for (int it = tid; it < (TX / 4) * TZ; it += NT) {
+      const int tq = it % (TX / 4), tr = it / (TX / 4);
+      const int j = z0 + tr, i0 = x0 + 4 * tq;
+      if (EDGE && (j >= G.nz || i0 >= G.nx)) continue;
+      const int r = tr + TB_Z, c0 = 4 * tq + TB_X;
+      float nsx[4], nsz[4], vn[4], nu[4];
+      tb_s_item<R, EDGE>(G, cf, s_v, s_sxy, s_szy, s_mu, r, c0, bx, bz, nsx, nsz, vn);
+      if (HU) {
+        const float* up = s_u + tr * TX + 4 * tq;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) nu[e] = __fmaf_rn(vn[e], G.dt, up[e]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) nu[e] = vn[e];
+      }
+      const int64_t p = lo + i0 + (int64_t)G.P * j;
+      if (!EDGE || i0 + 3 < G.nx) {
+        *reinterpret_cast<float4*>(S1.vo + p) = make_float4(vn[0], vn[1], vn[2], vn[3]);
+        if (!EDGE || i0 + 3 <= G.nx - 2) {
+          *reinterpret_cast<float4*>(S1.sxyo + p) = make_float4(nsx[0], nsx[1], nsx[2], nsx[3]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (i0 + e <= G.nx - 2) S1.sxyo[p + e] = nsx[e];
+        }
+        if (!EDGE || j <= G.nz - 2) *reinterpret_cast<float4*>(S1.szyo + p) = make_float4(nsz[0], nsz[1], nsz[2], nsz[3]);
+        if (HU) *reinterpret_cast<float4*>(S1.uo + p) = make_float4(nu[0], nu[1], nu[2], nu[3]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (i0 + e >= G.nx) break;
+          S1.vo[p + e] = vn[e];
+          if (i0 + e <= G.nx - 2) S1.sxyo[p + e] = nsx[e];
+          if (j <= G.nz - 2) S1.szyo[p + e] = nsz[e];
+          if (HU) S1.uo[p + e] = nu[e];
+        }
+      }
+      tb_outputs(G, S1, EDGE, lane, lo, i0, j, tr * TX + 4 * tq, nu, vn, s_rec, nrec);
+    }
+  };
+  if (edge)
+    run(std::true_type{});
+  else
+    run(std::false_type{});
+}
+
 // ---- multi-geometry step -----------------------------------------------------------
 // Solves on grids of different sizes (the reference stations of a batch, one
 // configuration each) advance together, one launch per time step.  Their
@@ -864,6 +1212,7 @@ struct Run {
   bool pdl = true;
   int t1[N_TILE_ROWS][4] = {};  // per tile shape: all-ones taper tile range (Grid32::t1x0..)
   const float* inj_planes = nullptr;  // injection planes (set_inj_map)
+  int inj_n_planes = 0;
   int2* rec_xy = nullptr;
   int2* src_xy = nullptr;
   int2* tile_rec = nullptr;  // per (lane, tile): {first entry, count}
@@ -872,6 +1221,10 @@ struct Run {
   int64_t ps = 0;   // pitched plane size P*nz rounded up to 128
   int S = 1;        // lanes; every internal array holds S planes (lane l at l*ps)
   int64_t lanes_ps() const { return (int64_t)S * ps; }
+  // two steps per launch (k32_step2): chosen by tune_time_depth; maps2 valid when depth == 2
+  int depth = 1;
+  int max_tile_rec = 0;  // most receivers of one (lane, tile)
+  StepMaps2 maps2[2];
 };
 
 // Step launches carry the programmatic-stream-serialization attribute: a step
@@ -934,6 +1287,27 @@ fd2d_status step_attributes_r(fd2d_ctx* ctx) {
   return step_attributes_t<R, 32>(ctx);
 }
 
+template <int R, int TZ>
+fd2d_status step2_attributes_t(fd2d_ctx* ctx) {
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step2<R, false, false, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile2<TZ, false, false>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step2<R, false, true, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile2<TZ, false, true>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step2<R, true, false, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile2<TZ, true, false>::BYTES));
+  FD2D_CUDA(ctx, cudaFuncSetAttribute(k32_step2<R, true, true, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Tile2<TZ, true, true>::BYTES));
+  return FD2D_OK;
+}
+
+template <int R>
+fd2d_status step2_attributes_r(fd2d_ctx* ctx) {
+  FD2D_TRY((step2_attributes_t<R, 16>(ctx)));
+  FD2D_TRY((step2_attributes_t<R, 30>(ctx)));
+  FD2D_TRY((step2_attributes_t<R, 40>(ctx)));
+  return step2_attributes_t<R, 32>(ctx);
+}
+
 // Opt the step kernels in to their dynamic shared memory (once per device,
 // before any capture on it).
 PerDeviceOnce g_step_attributes;
@@ -942,7 +1316,9 @@ fd2d_status step_attributes(fd2d_ctx* ctx) {
     FD2D_TRY(step_attributes_r<1>(ctx));
     FD2D_TRY(step_attributes_r<2>(ctx));
     FD2D_TRY(step_attributes_r<3>(ctx));
-    return step_attributes_r<4>(ctx);
+    FD2D_TRY(step_attributes_r<4>(ctx));
+    FD2D_TRY(step2_attributes_r<1>(ctx));
+    return step2_attributes_r<2>(ctx);
   });
 }
 
@@ -961,6 +1337,64 @@ fd2d_status launch_step(fd2d_ctx* ctx, const Run& r, int par, Step32 s) {
     default: launch_step_r<4>(ctx, r, par, s); break;
   }
   return after_launch(ctx, "k32_step");
+}
+
+template <int R, bool HU, bool HI, int TZ>
+void launch_step2_t(fd2d_ctx* ctx, const Run& r, int par, const Step2& q) {
+  using T = Tile2<TZ, HU, HI>;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = r.sgrid;
+  cfg.blockDim = dim3(T::NT);
+  cfg.dynamicSmemBytes = T::BYTES;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = r.pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k32_step2<R, HU, HI, TZ>, r.G, r.maps2[par], q);
+}
+
+template <int R, bool HU, bool HI>
+void launch_step2_v(fd2d_ctx* ctx, const Run& r, int par, const Step2& q) {
+  if (r.tz == 16) launch_step2_t<R, HU, HI, 16>(ctx, r, par, q);
+  else if (r.tz == 30) launch_step2_t<R, HU, HI, 30>(ctx, r, par, q);
+  else if (r.tz == 40) launch_step2_t<R, HU, HI, 40>(ctx, r, par, q);
+  else launch_step2_t<R, HU, HI, 32>(ctx, r, par, q);
+}
+
+template <int R>
+void launch_step2_r(fd2d_ctx* ctx, const Run& r, int par, const Step2& q) {
+  const bool hi = q.s[0].inj_plane >= 0 || q.s[1].inj_plane >= 0;
+  if (q.s[0].has_u) {
+    if (hi) launch_step2_v<R, true, true>(ctx, r, par, q);
+    else launch_step2_v<R, true, false>(ctx, r, par, q);
+  } else {
+    if (hi) launch_step2_v<R, false, true>(ctx, r, par, q);
+    else launch_step2_v<R, false, false>(ctx, r, par, q);
+  }
+}
+
+// Steps n and n+1 (s0, s1) in one launch: the fields of read buffer `par` are
+// advanced twice and written to buffer 1 - par.
+fd2d_status launch_step2(fd2d_ctx* ctx, const Run& r, int par, Step32 s0, Step32 s1) {
+  if (r.R > 2 || r.depth != 2 || s0.snap_pre || s1.snap_pre || s0.amp || s1.amp)
+    return set_error(ctx, FD2D_ERR_UNSUPPORTED, "two-step launch of an unsupported step");
+  Step2 q;
+  for (int k = 0; k < 2; ++k) {
+    Step32& s = k ? s1 : s0;
+    s.inj_base = r.inj_planes;
+    s.tile_rec = r.tile_rec;
+    s.rec_ent = r.rec_ent;
+    s.vo = r.v[1 - par];
+    s.sxyo = r.sxy[1 - par];
+    s.szyo = r.szy[1 - par];
+    s.uo = r.u[1 - par];
+    q.s[k] = s;
+  }
+  if (r.R == 1) launch_step2_r<1>(ctx, r, par, q);
+  else launch_step2_r<2>(ctx, r, par, q);
+  return after_launch(ctx, "k32_step2");
 }
 
 #define FD2D_DISPATCH_R(R_, KERNEL, ...)                                                 \
@@ -999,11 +1433,36 @@ fd2d_status make_maps(fd2d_ctx* ctx, Run& r) {
 }
 
 // Injection planes are [event][lane] planes of stride ps: lane l of event j is plane j*S + l.
+// Tensor maps of the two-step kernel: one box (TB_W x TZ+12) for every array, u
+// by tile.
+fd2d_status make_maps2(fd2d_ctx* ctx, Run& r) {
+  const int nx = r.G.nx, nz = r.G.nz, P = r.G.P, H = r.tz + 2 * TB_Z, S = r.S;
+  const int64_t ps = r.ps;
+  for (int q = 0; q < 2; ++q) {
+    StepMaps2& m = r.maps2[q];
+    FD2D_TRY(make_tmap_f32(ctx, &m.sxy, r.sxy[q], nx, nz, P, TB_W, H, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.szy, r.szy[q], nx, nz, P, TB_W, H, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.v, r.v[q], nx, nz, P, TB_W, H, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.u, r.u[q] ? r.u[q] : r.v[q], nx, nz, P, TX, r.tz, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.b, r.b, nx, nz, P, TB_W, H, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.taper, r.taper, nx, nz, P, TB_W, H, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.dtmu, r.dtmu, nx, nz, P, TB_W, H, S, ps));
+    FD2D_TRY(make_tmap_f32(ctx, &m.inj, r.inj_planes ? r.inj_planes : r.b, nx, nz, P, TB_W, H,
+                           r.inj_planes ? r.inj_n_planes : S, ps));
+  }
+  return FD2D_OK;
+}
+
 fd2d_status set_inj_map(fd2d_ctx* ctx, Run& r, const float* planes, int n_planes) {
   const int BH = r.tz + 2 * r.R - 1, BWa = TX + 8;
   r.inj_planes = planes;
+  r.inj_n_planes = n_planes;
   for (int q = 0; q < 2; ++q)
     FD2D_TRY(make_tmap_f32(ctx, &r.maps[q].inj, planes, r.G.nx, r.G.nz, r.G.P, BWa, BH, n_planes, r.ps));
+  if (r.depth == 2)
+    for (int q = 0; q < 2; ++q)
+      FD2D_TRY(make_tmap_f32(ctx, &r.maps2[q].inj, planes, r.G.nx, r.G.nz, r.G.P, TB_W, r.tz + 2 * TB_Z, n_planes,
+                             r.ps));
   return FD2D_OK;
 }
 
@@ -1215,7 +1674,11 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
 
 // Buffers, coefficient planes and tensor maps of S lanes a[0..S-1] (solves of
 // one geometry with the same numbers of sources and receivers).
-fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S, bool with_u, Run& r) {
+fd2d_status tune_time_depth(fd2d_ctx* ctx, Run& r, int nsrc, const int* crowded);
+
+// two_step: the loop may advance two steps per launch (tune_time_depth decides)
+fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S, bool with_u, Run& r,
+                     bool two_step = false) {
   const int nx = g.nx, nz = g.nz;
   const int P = (nx + 31) / 32 * 32;
   for (int l = 1; l < S; ++l)
@@ -1279,15 +1742,142 @@ fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S
   FD2D_TRY(step_attributes(ctx));
   FD2D_TRY(contract_prepare(ctx));
   FD2D_TRY(tune_tile_rows(ctx, r));
+  r.depth = 1;
+  if (two_step) {
+    // receivers per tile for every shape: two steps per launch keep at most
+    // MAX_TILE_REC of them per tile
+    int crowded[N_TILE_ROWS];
+    for (int c = 0; c < N_TILE_ROWS; ++c) {
+      std::vector<int2> table, ent;
+      build_tile_receivers(nx, nz, TILE_ROWS[c], a, S, table, ent);
+      int m = 0;
+      for (const int2& e : table) m = std::max(m, e.y);
+      crowded[c] = m > MAX_TILE_REC;
+    }
+    FD2D_TRY(tune_time_depth(ctx, r, (int)a[0].src_idx.size(), crowded));
+  }
   ctx->last_tile_rows = r.tz;
+  ctx->last_time_depth = r.depth;
   {
     // receivers grouped by step tile, so each CTA finds its own in one read
     std::vector<int2> table, ent;
     build_tile_receivers(nx, nz, r.tz, a, S, table, ent);
+    r.max_tile_rec = 0;
+    for (const int2& e : table) r.max_tile_rec = std::max(r.max_tile_rec, e.y);
     FD2D_TRY(upload(ctx, "f32.tile_rec", table, &r.tile_rec));
     FD2D_TRY(upload(ctx, "f32.rec_ent", ent, &r.rec_ent));
   }
-  return set_tiling(ctx, r);
+  FD2D_TRY(set_tiling(ctx, r));
+  return r.depth == 2 ? make_maps2(ctx, r) : FD2D_OK;
+}
+
+// Time steps per launch of this run, 1 or 2 (k32_step2), and with them the tile
+// shape.  Two steps per launch need FD order 2 or 4, at most MAX_BOX_SRC point
+// sources and at most MAX_TILE_REC receivers per tile (crowded[c]: shape c has
+// more).  Forced by fd2d_ctx_set_time_depth (or FD2D_TIME_DEPTH), with the
+// tile shape tune_tile_rows chose.  Otherwise, on an idle stream with the GPU to
+// itself, 24 steps are timed one per launch on that shape and two per launch
+// on every shape (on the run's zeroed fields, zeroed again after), and the
+// fastest is kept if it beats one step per launch by more than 1 %,
+// remembered per grid, order, lane count and kind.  A forced tile shape is
+// kept.  One step per launch otherwise.  The tile tables and tensor maps of
+// the result are set up by the caller.
+fd2d_status tune_time_depth(fd2d_ctx* ctx, Run& r, int nsrc, const int* crowded) {
+  r.depth = 1;
+  int forced = ctx->time_depth;
+  if (forced == 0) {
+    const char* e = std::getenv("FD2D_TIME_DEPTH");
+    if (e) forced = std::atoi(e);
+  }
+  int ci = 0;
+  for (int c = 0; c < N_TILE_ROWS; ++c)
+    if (TILE_ROWS[c] == r.tz) ci = c;
+  if (r.R > 2 || nsrc > MAX_BOX_SRC || forced == 1) return FD2D_OK;
+  if (forced == 2) {
+    r.depth = crowded[ci] ? 1 : 2;
+    return FD2D_OK;
+  }
+  int forced_rows = ctx->tile_rows;
+  if (forced_rows == FD2D_TILE_ROWS_AUTO) {
+    const char* e = std::getenv("FD2D_TILE_ROWS");
+    if (e) forced_rows = std::atoi(e);
+  }
+  const bool rows_fixed = forced_rows != FD2D_TILE_ROWS_AUTO;
+  const bool with_u = r.u[0] != nullptr;
+  Sig key;
+  key.add(r.G.nx); key.add(r.G.nz); key.add(r.R); key.add(r.S); key.add((int)with_u); key.add(r.tz);
+  key.add((int)rows_fixed); key.bytes(crowded, sizeof(int) * N_TILE_ROWS);
+  auto it = ctx->depth_choice.find(key.h);
+  if (it != ctx->depth_choice.end()) {
+    r.depth = it->second / 100;
+    r.tz = it->second % 100;
+    return FD2D_OK;
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  FD2D_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
+  bool idle = cs == cudaStreamCaptureStatusNone && ctx->concurrent_groups <= 1 && !ctx->shared_gpu;
+  if (idle) {
+    idle = cudaStreamQuery(ctx->stream) == cudaSuccess;
+    cudaGetLastError();  // a busy stream answers cudaErrorNotReady
+  }
+  if (!idle) return FD2D_OK;
+  constexpr int WARM = 4, TIMED = 24;
+  const int tz1 = r.tz;
+  cudaEvent_t e0, e1;
+  FD2D_CUDA(ctx, cudaEventCreate(&e0));
+  FD2D_CUDA(ctx, cudaEventCreate(&e1));
+  fd2d_status st = FD2D_OK;
+  Step32 s{};
+  s.inj_plane = -1;
+  s.has_u = with_u;
+  s.src_xy = r.src_xy;
+  s.rec_xy = r.rec_xy;
+  // candidates: (depth 1, the chosen shape), then depth 2 on each eligible shape
+  float best_ms = 0.f;
+  int best_d = 1, best_tz = tz1;
+  for (int c = -1; c < N_TILE_ROWS && st == FD2D_OK; ++c) {
+    const int d = c < 0 ? 1 : 2;
+    if (d == 2 && (crowded[c] || (rows_fixed && TILE_ROWS[c] != tz1))) continue;
+    r.tz = c < 0 ? tz1 : TILE_ROWS[c];
+    r.depth = d;
+    if ((st = set_tiling(ctx, r)) != FD2D_OK) break;
+    if (d == 2 && (st = make_maps2(ctx, r)) != FD2D_OK) break;
+    auto steps = [&](int n) {
+      for (int k = 0; k < n && st == FD2D_OK; k += d)
+        st = d == 1 ? launch_step(ctx, r, (k / d) & 1, s) : launch_step2(ctx, r, (k / d) & 1, s, s);
+    };
+    steps(WARM);
+    cudaEventRecord(e0, ctx->stream);
+    steps(TIMED);
+    cudaEventRecord(e1, ctx->stream);
+    if (st != FD2D_OK) break;
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      st = set_error(ctx, FD2D_ERR_CUDA, "time-depth timing failed");
+      break;
+    }
+    if (c < 0) {
+      best_ms = ms;
+    } else if (ms < 0.99f * best_ms) {
+      best_ms = ms;
+      best_d = 2;
+      best_tz = r.tz;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != FD2D_OK) return st;
+  const size_t bytes = (size_t)r.lanes_ps() * 4;
+  for (int q = 0; q < 2; ++q) {
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.v[q], 0, bytes, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.sxy[q], 0, bytes, ctx->stream));
+    FD2D_CUDA(ctx, cudaMemsetAsync(r.szy[q], 0, bytes, ctx->stream));
+    if (with_u) FD2D_CUDA(ctx, cudaMemsetAsync(r.u[q], 0, bytes, ctx->stream));
+  }
+  r.depth = best_d;
+  r.tz = best_tz;
+  ctx->depth_choice[key.h] = best_d * 100 + best_tz;
+  return FD2D_OK;
 }
 
 // Frequency-band weights (interpol_matrix) on the device.
@@ -1490,6 +2080,9 @@ fd2d_status dft_flush(fd2d_ctx* ctx, const Run& r, const Geometry& g, Dft& d) {
   return FD2D_OK;
 }
 
+// whether the next dft_push ends a chunk (and contracts it)
+bool dft_would_flush(const Dft& d) { return d.filled + 1 == d.T || d.done + d.filled + 1 == d.n_events; }
+
 fd2d_status dft_push(fd2d_ctx* ctx, const Run& r, const Geometry& g, Dft& d) {
   ++d.filled;
   if (d.filled == d.T || d.done + d.filled == d.n_events) return dft_flush(ctx, r, g, d);
@@ -1504,6 +2097,8 @@ void sig_run(Sig& sg, const Run& r) {
   sg.bytes(r.maps, sizeof(r.maps));
   sg.add(r.sgrid.x); sg.add(r.sgrid.y); sg.add(r.sgrid.z); sg.add(r.pgrid.x); sg.add(r.pgrid.y);
   sg.add(r.R); sg.add(r.tz); sg.add((int)r.pdl); sg.add(r.inj_planes); sg.add(r.rec_xy); sg.add(r.src_xy); sg.add(r.np); sg.add(r.ps);
+  sg.add(r.depth);
+  if (r.depth == 2) sg.bytes(r.maps2, sizeof(r.maps2));
 }
 
 void sig_args(Sig& sg, const Geometry& g, const SolveArgs& a) {
@@ -1570,7 +2165,7 @@ fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs
   FD2D_TRY(lane_stride_of(ctx, S, seis.data(), &seis_lane));
   if (g_lane != gi_lane) return set_error(ctx, FD2D_ERR_ARG, "lane spectra strides differ");
   Run r;
-  FD2D_TRY(init_run(ctx, g, al, S, false, r));
+  FD2D_TRY(init_run(ctx, g, al, S, false, r, a.dmu == nullptr));
   const int nt = g.nt, K = g.K;
   const int64_t np = r.np;
   // DFT events: steps n with mod(n+nt-1, freq_samp) == 0; coefficient of step n is
@@ -1613,10 +2208,38 @@ fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs
     const int64_t np = r.np;
     int i_fw_out = 0, i_fw_in = 0, par = 0;
     const int tl = timer_begin(ctx, ctx->stream);  // whole loop; contractions are timed inside it
+    auto pre = [&](int n) { return a.mode != 0 && (n + nt - 1) % g.fw == 0; };
+    auto is_dft_step = [&](int n) { return (n + nt - 1) % g.fs == 0; };
     for (int n = 1; n <= nt; ++n) {
+      // two steps in one launch when nothing has to happen between them: no
+      // wavefield snapshot before either step, no DFT contraction after the first
+      if (r.depth == 2 && !born && n < nt && !pre(n) && !pre(n + 1) &&
+          !(is_dft_step(n) && dft_would_flush(dd))) {
+        Step32 s2[2] = {};
+        for (int k = 0; k < 2; ++k) {
+          Step32& s = s2[k];
+          s.inj_plane = -1;
+          s.src_xy = r.src_xy;
+          s.nsrc = (int)a.src_idx.size();
+          s.amp_const = 1.0e9f;
+          s.rec_xy = r.rec_xy;
+          s.nrec = nr;
+          s.seis_col = a.seis + (size_t)nr * (n + k - 1);
+          s.seis_lane = seis_lane;
+        }
+        const bool d0 = is_dft_step(n), d1 = is_dft_step(n + 1);
+        if (d0) s2[0].snap_dft = dft_slot(r, dd);
+        if (d1) s2[1].snap_dft = dd.snaps + (size_t)(dd.filled + (d0 ? 1 : 0)) * r.lanes_ps();
+        FD2D_TRY(launch_step2(ctx, r, par, s2[0], s2[1]));
+        if (d0) FD2D_TRY(dft_push(ctx, r, g, dd));
+        if (d1) FD2D_TRY(dft_push(ctx, r, g, dd));
+        par ^= 1;
+        ++n;
+        continue;
+      }
       Step32 s{};
       s.inj_plane = -1;
-      if (a.mode != 0 && (n + nt - 1) % g.fw == 0) s.snap_pre = a.G_out + (size_t)np * (i_fw_out++);
+      if (pre(n)) s.snap_pre = a.G_out + (size_t)np * (i_fw_out++);
       if (born) {
         FD2D_DISPATCH_R(r.R, k32_born_pre, r.G, r.sxy[par], r.szy[par], dtdmu, a.G_in + (size_t)np * (i_fw_in++));
         FD2D_TRY(after_launch(ctx, "k32_born_pre"));
@@ -1625,7 +2248,7 @@ fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs
         s.nsrc = (int)a.src_idx.size();
         s.amp_const = 1.0e9f;  // stf = 1.0e9*ones(1,nt), code/run_forward1_green.m:64
       }
-      const bool is_dft = (n + nt - 1) % g.fs == 0;
+      const bool is_dft = is_dft_step(n);
       if (is_dft) s.snap_dft = dft_slot(r, dd);
       s.rec_xy = r.rec_xy;
       s.nrec = nr;
@@ -1655,7 +2278,7 @@ fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveA
   int64_t seis_lane = 0;
   FD2D_TRY(lane_stride_of(ctx, S, seis.data(), &seis_lane));
   Run r;
-  FD2D_TRY(init_run(ctx, g, al, S, true, r));
+  FD2D_TRY(init_run(ctx, g, al, S, true, r, a.dmu == nullptr));
   const int ntc = g.ntc;
   double *M, *spec;
   FD2D_TRY(interp_dev(ctx, g, &M));
@@ -1680,11 +2303,12 @@ fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveA
     const int64_t np = r.np;
     int i_fw_out = 0, par = 0, ev = 0;
     const int tl = timer_begin(ctx, ctx->stream);
+    auto pre = [&](int n) { return a.mode != 0 && n % g.fw == 0; };
     for (int n = 1; n <= ntc; ++n) {
       Step32 s{};
       s.inj_plane = -1;
       s.has_u = 1;
-      if (a.mode != 0 && n % g.fw == 0) {
+      if (pre(n)) {
         s.snap_pre = a.C_out + (size_t)np * (i_fw_out++);
         s.snap_pre_u = 1;
       }
@@ -1694,6 +2318,19 @@ fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveA
       s.seis_col = a.seis + (size_t)nr * (n - 1);
       s.seis_lane = seis_lane;
       s.rec_u = 1;  // u does not depend on this step's Born stress correction
+      // two steps in one launch when no snapshot precedes either and the next
+      // step's injection plane (if any) is already resident
+      if (r.depth == 2 && !born && n < ntc && !pre(n) && !pre(n + 1) &&
+          ((n + 1) % g.fs != 0 || (ev >= ij.first && ev < ij.first + ij.count))) {
+        Step32 s1 = s;
+        s1.inj_plane = -1;
+        if ((n + 1) % g.fs == 0) s1.inj_plane = ev++ - ij.first;
+        s1.seis_col = a.seis + (size_t)nr * n;
+        FD2D_TRY(launch_step2(ctx, r, par, s, s1));
+        par ^= 1;
+        ++n;
+        continue;
+      }
       FD2D_TRY(launch_step(ctx, r, par, s));
       par ^= 1;
       if (born && n != ntc) {

@@ -132,6 +132,20 @@ fd2d_status fd2d_ctx_set_chunks(fd2d_ctx* ctx, int32_t max_snapshots, int32_t ma
 fd2d_status fd2d_ctx_set_tile_rows(fd2d_ctx* ctx, int32_t rows);
 /* Tile rows used by the last FP32 time loop this context set up (0: none yet). */
 int32_t fd2d_ctx_last_tile_rows(const fd2d_ctx* ctx);
+/* Time steps per launch of the FP32 Green-function and correlation loops at FD
+ * orders 2 and 4: 1 or 2 to force, 0 (default) to time both once per context
+ * for each grid, order, lane count and tile shape when the stream is idle and
+ * keep the faster (one step per launch otherwise).  Two steps per launch
+ * recompute the first step on a wider halo ring -- more arithmetic for half
+ * the launches, which pays where a launch leaves most SMs idle (small grids);
+ * the fields, seismograms and spectra are bit for bit those of one step per
+ * launch.  Steps that store wavefield snapshots (modes != 0), Born runs, the
+ * adjoint loop, order 6/8 and the multi-geometry batch run one step per
+ * launch.  The environment variable FD2D_TIME_DEPTH forces a depth for
+ * contexts left at 0. */
+fd2d_status fd2d_ctx_set_time_depth(fd2d_ctx* ctx, int32_t depth);
+/* Steps per launch chosen for the last FP32 time loop this context set up (0: none yet). */
+int32_t fd2d_ctx_last_time_depth(const fd2d_ctx* ctx);
 /* Declare that other work (other contexts, processes or streams) runs on the
  * GPU beside this context's solves (1) or not (0, default).  Shared: time steps
  * are launched without programmatic early launch (a waiting step would hold

@@ -1,0 +1,162 @@
+"""Two time steps per launch (k32_step2, FD orders 2 and 4).
+
+The Green-function and correlation loops may advance two steps in one launch,
+recomputing the first step on a wider halo ring.  Every point is updated by
+the same rounded operations, so spectra, seismograms, correlations and stored
+wavefields must be bit for bit those of one step per launch -- on edge and
+interior tiles, with point sources, receivers, DFT snapshots on either step of
+a pair (freq_samp 1 puts them on both), injection planes, stored wavefields
+(mode 1, whose steps run singly), an odd number of steps, lanes, and every
+tile shape.  The time-depth tuner picks one depth per grid and keeps it;
+orders 6/8 and tiles with more receivers than the kernel keeps run one step
+per launch.
+"""
+import numpy as np
+import pytest
+
+from tests.problems import media, noise_source, small_cfg, stations
+
+pytestmark = pytest.mark.gpu
+
+
+def _green_corr(cfg, mu, rho, spec, sd, src, rec, mode=0):
+    from fd2d_noise_gb300 import solvers
+    G, G_out, s_g = solvers.run_forward1_green(mu, rho, src, rec, mode, cfg=cfg, precision="fp32")
+    c, C_out = solvers.run_forward2_correlation(mu, rho, G, spec, sd, rec, mode, cfg=cfg, precision="fp32")
+    return [G, s_g, c] + ([G_out, C_out] if mode else [])
+
+
+def _with_depths(cfg, seed, depths=(1, 2), rows=None, mode=0, n_rec=6, rec=None):
+    from fd2d_noise_gb300 import _lib, solvers
+    mu, rho = media(cfg, seed=seed)
+    spec, sd = noise_source(cfg, seed=seed)
+    src = stations(cfg, 1, seed=10 + seed)
+    if rec is None:
+        # receivers within a few wavelengths of the source, so every trace is nonzero
+        off = np.random.default_rng(20 + seed).uniform(-12, 12, (n_rec, 2)) * np.array([cfg.dx, cfg.dz])
+        rec = np.clip(src + off, [2 * cfg.dx, 2 * cfg.dz], [cfg.Lx - 2 * cfg.dx, cfg.Lz - 2 * cfg.dz])
+    ctx = _lib.Context(0, _lib.PREC_FP32)
+    out, used = {}, {}
+    try:
+        with solvers.bound_context(ctx):
+            if rows:
+                ctx.set_tile_rows(rows)
+            for d in depths:
+                ctx.set_time_depth(d)
+                out[d] = _green_corr(cfg, mu, rho, spec, sd, src, rec, mode)
+                used[d] = ctx.last_time_depth()
+    finally:
+        ctx.close()
+    return out, used
+
+
+CASES = [
+    # nx, nz, nt, fs: ragged edges everywhere; an odd nt ends on a single step
+    dict(nx=70, nz=52, nt=61, fs=1),
+    dict(nx=150, nz=141, nt=90, fs=3),  # interior tiles without edge selects
+    dict(nx=257, nz=200, nt=50, fs=5),
+]
+
+
+@pytest.mark.parametrize("order", [2, 4])
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_two_steps_per_launch_are_bit_identical(fd2d_lib, order, case):
+    cfg = small_cfg(K=8, order=order, **CASES[case])
+    out, used = _with_depths(cfg, seed=3 + case)
+    assert used == {1: 1, 2: 2}
+    for a, b in zip(out[1], out[2]):
+        assert np.abs(a).max() > 0
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("rows", [16, 30, 40])
+def test_every_tile_shape(fd2d_lib, rows):
+    cfg = small_cfg(nx=130, nz=97, nt=40, K=6, fs=2, order=4)
+    out, used = _with_depths(cfg, seed=9, rows=rows)
+    assert used[2] == 2
+    for a, b in zip(out[1], out[2]):
+        assert np.array_equal(a, b)
+
+
+def test_stored_wavefields_split_the_pairs(fd2d_lib):
+    """Mode 1 stores single(v) / single(u) before every fw-th step: those steps
+    run singly, the others in pairs, and everything matches."""
+    cfg = small_cfg(nx=96, nz=88, nt=47, K=6, fs=2, fw=3, order=4)
+    out, used = _with_depths(cfg, seed=12, mode=1)
+    assert used[2] == 2
+    for a, b in zip(out[1], out[2]):
+        assert np.array_equal(a, b)
+
+
+def test_lanes_of_a_batch(fd2d_lib):
+    """Reference stations of one geometry as lanes of one launch, two steps per launch."""
+    import torch
+    from fd2d_noise_gb300 import _lib
+    from fd2d_noise_gb300.device import DeviceSession, to_device
+    cfg = small_cfg(nx=120, nz=100, nt=55, K=8, fs=5, order=4)
+    jobs = []
+    for seed in range(3):
+        mu, rho = media(cfg, seed=seed)
+        spec, sd = noise_source(cfg, seed=seed)
+        src = stations(cfg, 1, seed=30 + seed)
+        off = np.random.default_rng(40 + seed).uniform(-10, 10, (5, 2)) * np.array([cfg.dx, cfg.dz])
+        rec = np.clip(src + off, [2 * cfg.dx, 2 * cfg.dz], [cfg.Lx - 2 * cfg.dx, cfg.Lz - 2 * cfg.dz])
+        jobs.append(dict(cfg=cfg, mu=to_device(mu, np.float64), rho=to_device(rho, np.float64),
+                         spectrum=to_device(spec, np.float64), source_dist=to_device(sd, np.float64),
+                         src=to_device(src, np.float64), rec=to_device(rec, np.float64), nr=5,
+                         out=torch.zeros(5 * cfg.ntc, dtype=torch.float64, device="cuda")))
+    res = {}
+    for d in (1, 2):
+        sess = DeviceSession(cfg, 0, "fp32")
+        _lib.check(sess.ctx.L.fd2d_ctx_set_time_depth(sess.ctx.h, d), sess.ctx.h)
+        for j in jobs:
+            j["out"].zero_()
+        sess.correlation_batch(jobs)
+        sess.ctx.synchronize()
+        assert sess.ctx.last_batch() == [3]
+        assert sess.ctx.last_time_depth() == d
+        res[d] = [j["out"].cpu().numpy().copy() for j in jobs]
+        sess.ctx.close()
+    for a, b in zip(res[1], res[2]):
+        assert np.abs(a).max() > 0 and np.array_equal(a, b)
+
+
+def test_order_8_and_crowded_tiles_run_one_step_per_launch(fd2d_lib):
+    cfg8 = small_cfg(nx=90, nz=80, nt=30, K=4, fs=2, order=8)
+    _, used = _with_depths(cfg8, seed=1, depths=(2,))
+    assert used[2] == 1
+    # 40 receivers in one 32-point-wide tile: more than the kernel keeps per tile
+    cfg = small_cfg(nx=90, nz=80, nt=30, K=4, fs=2, order=4)
+    x = np.linspace(20e3, 60e3, 40)
+    rec = np.column_stack([x, np.full(40, 40e3)])
+    out, used = _with_depths(cfg, seed=2, rec=rec)
+    assert used == {1: 1, 2: 1}
+    for a, b in zip(out[1], out[2]):
+        assert np.array_equal(a, b)
+
+
+def test_tuner_keeps_its_choice(fd2d_lib):
+    """Left at 0 the depth is timed once per grid (on an idle stream) and kept;
+    the timed trial steps leave no trace in the results."""
+    from fd2d_noise_gb300 import _lib, solvers
+    cfg = small_cfg(nx=100, nz=90, nt=40, K=6, fs=2, order=4)
+    mu, rho = media(cfg, seed=7)
+    spec, sd = noise_source(cfg, seed=7)
+    src, rec = stations(cfg, 1, seed=70), stations(cfg, 4, seed=71)
+    ctx = _lib.Context(0, _lib.PREC_FP32)
+    try:
+        assert ctx.last_time_depth() == 0
+        with solvers.bound_context(ctx):
+            a = _green_corr(cfg, mu, rho, spec, sd, src, rec)
+            first = ctx.last_time_depth()
+            assert first in (1, 2)
+            b = _green_corr(cfg, mu, rho, spec, sd, src, rec)
+            assert ctx.last_time_depth() == first
+            ctx.set_time_depth(1)
+            c = _green_corr(cfg, mu, rho, spec, sd, src, rec)
+        for x, y, z in zip(a, b, c):
+            assert np.array_equal(x, y) and np.array_equal(x, z)
+        with pytest.raises(_lib.FD2DError):
+            ctx.set_time_depth(3)
+    finally:
+        ctx.close()
