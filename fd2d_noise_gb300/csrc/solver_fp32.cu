@@ -1576,8 +1576,9 @@ int step_ctas(int R, int tz) {
 // Forced by fd2d_ctx_set_tile_rows (or FD2D_TILE_ROWS).  Otherwise, when the
 // context's stream is idle and no other lane group of a batch runs beside this
 // one, every shape is timed once per context on this run's freshly zeroed
-// fields -- steps of the run's kind (with or without the displacement u) with
-// no sources, receivers or snapshots -- and the fastest is kept for later runs
+// fields -- 24 steps of the run's kind (with or without the displacement u)
+// with no sources, receivers or snapshots, in three rounds of which the
+// fastest counts -- and the fastest shape is kept for later runs
 // of the same grid, order, lane count and kind if it beats the size rule's
 // shape by more than 1 %.  When timing would
 // stall queued or concurrent work, or during a stream capture, the size rule
@@ -1627,30 +1628,35 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
     r.tz = rule;
     return FD2D_OK;
   }
-  constexpr int WARM = 3, TIMED = 24;
+  // ROUNDS rounds over the shapes, the fastest round of each shape counts
+  // (timings of a few microseconds per step vary from round to round)
+  constexpr int WARM = 3, TIMED = 24, ROUNDS = 3;
   cudaEvent_t e0, e1;
   FD2D_CUDA(ctx, cudaEventCreate(&e0));
   FD2D_CUDA(ctx, cudaEventCreate(&e1));
   float ms_of[N_TILE_ROWS] = {};
   fd2d_status st = FD2D_OK;
-  for (int c = 0; c < N_TILE_ROWS; ++c) {
-    r.tz = TILE_ROWS[c];
-    if ((st = set_tiling(ctx, r)) != FD2D_OK) break;
-    Step32 s{};
-    s.inj_plane = -1;
-    s.has_u = with_u;
-    s.src_xy = r.src_xy;
-    s.rec_xy = r.rec_xy;
-    for (int n = 0; n < WARM && st == FD2D_OK; ++n) st = launch_step(ctx, r, n & 1, s);
-    cudaEventRecord(e0, ctx->stream);
-    for (int n = 0; n < TIMED && st == FD2D_OK; ++n) st = launch_step(ctx, r, n & 1, s);
-    cudaEventRecord(e1, ctx->stream);
-    if (st != FD2D_OK) break;
-    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms_of[c], e0, e1) != cudaSuccess) {
-      st = set_error(ctx, FD2D_ERR_CUDA, "tile-row timing failed");
-      break;
+  for (int round = 0; round < ROUNDS && st == FD2D_OK; ++round)
+    for (int c = 0; c < N_TILE_ROWS; ++c) {
+      r.tz = TILE_ROWS[c];
+      if ((st = set_tiling(ctx, r)) != FD2D_OK) break;
+      Step32 s{};
+      s.inj_plane = -1;
+      s.has_u = with_u;
+      s.src_xy = r.src_xy;
+      s.rec_xy = r.rec_xy;
+      for (int n = 0; n < WARM && st == FD2D_OK; ++n) st = launch_step(ctx, r, n & 1, s);
+      cudaEventRecord(e0, ctx->stream);
+      for (int n = 0; n < TIMED && st == FD2D_OK; ++n) st = launch_step(ctx, r, n & 1, s);
+      cudaEventRecord(e1, ctx->stream);
+      if (st != FD2D_OK) break;
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        st = set_error(ctx, FD2D_ERR_CUDA, "tile-row timing failed");
+        break;
+      }
+      ms_of[c] = round == 0 ? ms : std::min(ms_of[c], ms);
     }
-  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != FD2D_OK) return st;
@@ -1777,8 +1783,9 @@ fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S
 // more).  Forced by fd2d_ctx_set_time_depth (or FD2D_TIME_DEPTH), with the
 // tile shape tune_tile_rows chose.  Otherwise, on an idle stream with the GPU to
 // itself, 24 steps are timed one per launch on that shape and two per launch
-// on every shape (on the run's zeroed fields, zeroed again after), and the
-// fastest is kept if it beats one step per launch by more than 1 %,
+// on every shape (on the run's zeroed fields, zeroed again after; the fastest
+// of three rounds counts), and the fastest is kept if it beats one step per
+// launch by more than 1 %,
 // remembered per grid, order, lane count and kind.  A forced tile shape is
 // kept.  One step per launch otherwise.  The tile tables and tensor maps of
 // the result are set up by the caller.
@@ -1821,7 +1828,7 @@ fd2d_status tune_time_depth(fd2d_ctx* ctx, Run& r, int nsrc, const int* crowded)
     cudaGetLastError();  // a busy stream answers cudaErrorNotReady
   }
   if (!idle) return FD2D_OK;
-  constexpr int WARM = 4, TIMED = 24;
+  constexpr int WARM = 4, TIMED = 24, ROUNDS = 3;
   const int tz1 = r.tz;
   cudaEvent_t e0, e1;
   FD2D_CUDA(ctx, cudaEventCreate(&e0));
@@ -1832,38 +1839,41 @@ fd2d_status tune_time_depth(fd2d_ctx* ctx, Run& r, int nsrc, const int* crowded)
   s.has_u = with_u;
   s.src_xy = r.src_xy;
   s.rec_xy = r.rec_xy;
-  // candidates: (depth 1, the chosen shape), then depth 2 on each eligible shape
-  float best_ms = 0.f;
+  // candidates: (depth 1, the chosen shape), then depth 2 on each eligible
+  // shape; ROUNDS rounds, the fastest round of each candidate counts
+  float ms_of[N_TILE_ROWS + 1] = {};
+  for (int round = 0; round < ROUNDS && st == FD2D_OK; ++round)
+    for (int c = -1; c < N_TILE_ROWS && st == FD2D_OK; ++c) {
+      const int d = c < 0 ? 1 : 2;
+      if (d == 2 && (crowded[c] || (rows_fixed && TILE_ROWS[c] != tz1))) continue;
+      r.tz = c < 0 ? tz1 : TILE_ROWS[c];
+      r.depth = d;
+      if ((st = set_tiling(ctx, r)) != FD2D_OK) break;
+      if (d == 2 && (st = make_maps2(ctx, r)) != FD2D_OK) break;
+      auto steps = [&](int n) {
+        for (int k = 0; k < n && st == FD2D_OK; k += d)
+          st = d == 1 ? launch_step(ctx, r, (k / d) & 1, s) : launch_step2(ctx, r, (k / d) & 1, s, s);
+      };
+      steps(WARM);
+      cudaEventRecord(e0, ctx->stream);
+      steps(TIMED);
+      cudaEventRecord(e1, ctx->stream);
+      if (st != FD2D_OK) break;
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        st = set_error(ctx, FD2D_ERR_CUDA, "time-depth timing failed");
+        break;
+      }
+      ms_of[c + 1] = round == 0 ? ms : std::min(ms_of[c + 1], ms);
+    }
+  float best_ms = ms_of[0];
   int best_d = 1, best_tz = tz1;
-  for (int c = -1; c < N_TILE_ROWS && st == FD2D_OK; ++c) {
-    const int d = c < 0 ? 1 : 2;
-    if (d == 2 && (crowded[c] || (rows_fixed && TILE_ROWS[c] != tz1))) continue;
-    r.tz = c < 0 ? tz1 : TILE_ROWS[c];
-    r.depth = d;
-    if ((st = set_tiling(ctx, r)) != FD2D_OK) break;
-    if (d == 2 && (st = make_maps2(ctx, r)) != FD2D_OK) break;
-    auto steps = [&](int n) {
-      for (int k = 0; k < n && st == FD2D_OK; k += d)
-        st = d == 1 ? launch_step(ctx, r, (k / d) & 1, s) : launch_step2(ctx, r, (k / d) & 1, s, s);
-    };
-    steps(WARM);
-    cudaEventRecord(e0, ctx->stream);
-    steps(TIMED);
-    cudaEventRecord(e1, ctx->stream);
-    if (st != FD2D_OK) break;
-    float ms = 0.f;
-    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-      st = set_error(ctx, FD2D_ERR_CUDA, "time-depth timing failed");
-      break;
-    }
-    if (c < 0) {
-      best_ms = ms;
-    } else if (ms < 0.99f * best_ms) {
-      best_ms = ms;
+  for (int c = 0; c < N_TILE_ROWS; ++c)
+    if (ms_of[c + 1] > 0.f && ms_of[c + 1] < 0.99f * best_ms) {
+      best_ms = ms_of[c + 1];
       best_d = 2;
-      best_tz = r.tz;
+      best_tz = TILE_ROWS[c];
     }
-  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != FD2D_OK) return st;
