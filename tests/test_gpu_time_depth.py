@@ -55,6 +55,7 @@ CASES = [
     dict(nx=70, nz=52, nt=61, fs=1),
     dict(nx=150, nz=141, nt=90, fs=3),  # interior tiles without edge selects
     dict(nx=257, nz=200, nt=50, fs=5),
+    dict(nx=33, nz=17, nt=21, fs=2),  # grid smaller than one loaded box
 ]
 
 
@@ -160,3 +161,28 @@ def test_tuner_keeps_its_choice(fd2d_lib):
             ctx.set_time_depth(3)
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("name", ["plain_cpu_300", "structure_512"])
+def test_full_size_workloads_are_bit_identical(fd2d_lib, name):
+    """Configuration 1 (300², nt 1200, mode 0) and the structure-kernel grid
+    (512², nt 2500, Green and correlation runs in mode 1 with fw 5, whose
+    stored steps split the pairs) with one and two steps per launch."""
+    from fd2d_noise_gb300 import _lib, solvers
+    from fd2d_noise_gb300.workloads import WORKLOADS
+    w = WORKLOADS[name]()
+    mode = 1 if name == "structure_512" else 0
+    ctx = _lib.Context(0, _lib.PREC_FP32)
+    out = {}
+    try:
+        with solvers.bound_context(ctx):
+            for d in (1, 2):
+                ctx.set_time_depth(d)
+                out[d] = _green_corr(w.cfg, w.mu, w.rho, w.spectrum, w.source_dist, w.ref_stations, w.receivers,
+                                     mode)
+                assert ctx.last_time_depth() == d
+    finally:
+        ctx.close()
+    for a, b in zip(out[1], out[2]):
+        assert np.abs(a).max() > 0
+        assert np.array_equal(a, b)
