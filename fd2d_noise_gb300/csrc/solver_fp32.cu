@@ -274,15 +274,27 @@ __device__ __forceinline__ void step_tile(const Grid32& G, const StepMaps& M, co
         s_nrec = -1;  // no tables: search the receiver list after the update
       }
     }
-    for (int k = tid; k < S.nsrc; k += NT) {
-      const int2 q = src_xy[k];
-      if (q.x >= vx0 && q.x < vx0 + W && q.y >= bz0 && q.y < bz0 + T::BH) {
-        const int slot = atomicAdd(&s_nsrc, 1);
-        if (slot < MAX_BOX_SRC) {
+    // point sources in the box, listed by warp 0 in source order (the
+    // reference's order of addition, so the sums are reproducible)
+    if (tid < 32 && S.nsrc) {
+      int base = 0;
+      for (int k0 = 0; k0 < S.nsrc; k0 += 32) {
+        const int k = k0 + tid;
+        int2 q = make_int2(0, 0);
+        bool in = false;
+        if (k < S.nsrc) {
+          q = src_xy[k];
+          in = q.x >= vx0 && q.x < vx0 + W && q.y >= bz0 && q.y < bz0 + T::BH;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, in);
+        const int slot = base + __popc(m & ((1u << tid) - 1u));
+        if (in && slot < MAX_BOX_SRC) {
           s_src[slot] = (q.y - bz0) * W + (q.x - vx0);
           s_amp[slot] = amp ? (float)amp[k] : S.amp_const;
         }
+        base += __popc(m);
       }
+      if (tid == 0) s_nsrc = base;
     }
     // one warp waits for the top part of the tile (suspending); the others
     // wait at the barrier
@@ -640,7 +652,8 @@ struct Step2 {
 template <int R, bool EDGE>
 __device__ __forceinline__ void tb_v_item(const Grid32& G, const float* cf, float* s_v, const float* s_sxy,
                                           const float* s_szy, const float* s_b, const float* s_t, const float* s_i,
-                                          int r, int c0, int bx, int bz, const int* s_src, int nbs, float amp) {
+                                          int r, int c0, int bx, int bz, const int* s_src, const float* s_amp,
+                                          int nbs) {
   constexpr int W = TB_W;
   const int gz = bz + r;
   const bool zin = gz >= R && gz <= G.nz - R - 1;
@@ -679,7 +692,7 @@ __device__ __forceinline__ void tb_v_item(const Grid32& G, const float* cf, floa
     const int d = s_src[qq] - idx0;
 #pragma unroll
     for (int e = 0; e < 4; ++e)
-      if (d == e) dsv[e] = __fadd_rn(dsv[e], amp);
+      if (d == e) dsv[e] = __fadd_rn(dsv[e], s_amp[qq]);
   }
   const float4 v4 = *reinterpret_cast<const float4*>(s_v + idx0);
   const float4 b4 = *reinterpret_cast<const float4*>(s_b + idx0);
@@ -780,6 +793,7 @@ __global__ __launch_bounds__(Tile2<TZ, HU, HI>::NT) void k32_step2(Grid32 G, con
   float* sm = reinterpret_cast<float*>(sm_raw + ((128u - (smem_u32(sm_raw) & 127u)) & 127u));
   __shared__ __align__(8) uint64_t bar[1];
   __shared__ int s_src[MAX_BOX_SRC];
+  __shared__ float s_amp0[MAX_BOX_SRC], s_amp1[MAX_BOX_SRC];  // amplitudes of steps 1 and 2
   __shared__ int s_nsrc;
   __shared__ int2 s_rec[MAX_TILE_REC];
   __shared__ int s_nrec;
@@ -821,15 +835,30 @@ __global__ __launch_bounds__(Tile2<TZ, HU, HI>::NT) void k32_step2(Grid32 G, con
     }
     for (int q = tid; q < se.y && q < MAX_TILE_REC; q += 32) s_rec[q] = S0.rec_ent[se.x + q];
   }
-  {
+  if (tid < 32 && S0.nsrc) {
+    // point sources in the box, in source order (as step_tile)
     const int2* src_xy = S0.src_xy + (int64_t)lane * S0.nsrc;
-    for (int k = tid; k < S0.nsrc; k += NT) {
-      const int2 q = src_xy[k];
-      if (q.x >= bx && q.x < bx + W && q.y >= bz && q.y < bz + T::H) {
-        const int slot = atomicAdd(&s_nsrc, 1);
-        if (slot < MAX_BOX_SRC) s_src[slot] = (q.y - bz) * W + (q.x - bx);
-        else set_error_flag(G.err, 1);  // the host pairs steps only below this
+    int base = 0;
+    for (int k0 = 0; k0 < S0.nsrc; k0 += 32) {
+      const int k = k0 + tid;
+      int2 q = make_int2(0, 0);
+      bool in = false;
+      if (k < S0.nsrc) {
+        q = src_xy[k];
+        in = q.x >= bx && q.x < bx + W && q.y >= bz && q.y < bz + T::H;
       }
+      const unsigned m = __ballot_sync(0xffffffffu, in);
+      const int slot = base + __popc(m & ((1u << tid) - 1u));
+      if (in && slot < MAX_BOX_SRC) {
+        s_src[slot] = (q.y - bz) * W + (q.x - bx);
+        s_amp0[slot] = S0.amp ? (float)S0.amp[(int64_t)lane * S0.nsrc + k] : S0.amp_const;
+        s_amp1[slot] = S1.amp ? (float)S1.amp[(int64_t)lane * S1.nsrc + k] : S1.amp_const;
+      }
+      base += __popc(m);
+    }
+    if (tid == 0) {
+      s_nsrc = base;
+      if (base > MAX_BOX_SRC) set_error_flag(G.err, 1);  // the host pairs steps only below this
     }
   }
   bool ok = true;
@@ -860,7 +889,7 @@ __global__ __launch_bounds__(Tile2<TZ, HU, HI>::NT) void k32_step2(Grid32 G, con
     // A: v1
     for (int it = tid; it < NQA * (T::RA1 - T::RA0 + 1); it += NT)
       tb_v_item<R, EDGE>(G, cf, s_v, s_sxy, s_szy, s_b, s_t, s_i0, T::RA0 + it / NQA, 4 * (T::QA0 + it % NQA), bx,
-                         bz, s_src, nbs, S0.amp_const);
+                         bz, s_src, s_amp0, nbs);
     __syncthreads();
     // B: s1 (in place: an item reads its own old stresses only); step-1 outputs on the tile
     for (int it = tid; it < NQB * (T::RB1 - T::RB0 + 1); it += NT) {
@@ -890,7 +919,7 @@ __global__ __launch_bounds__(Tile2<TZ, HU, HI>::NT) void k32_step2(Grid32 G, con
     // C: v2
     for (int it = tid; it < NQC * (T::RC1 - T::RC0 + 1); it += NT)
       tb_v_item<R, EDGE>(G, cf, s_v, s_sxy, s_szy, s_b, s_t, s_i1, T::RC0 + it / NQC, 4 * (T::QC0 + it % NQC), bx,
-                         bz, s_src, nbs, S1.amp_const);
+                         bz, s_src, s_amp1, nbs);
     __syncthreads();
     // D: s2, u2 and the stores of the tile
     for (int it = tid; it < (TX / 4) * TZ; it += NT) {
@@ -1378,7 +1407,7 @@ void launch_step2_r(fd2d_ctx* ctx, const Run& r, int par, const Step2& q) {
 // Steps n and n+1 (s0, s1) in one launch: the fields of read buffer `par` are
 // advanced twice and written to buffer 1 - par.
 fd2d_status launch_step2(fd2d_ctx* ctx, const Run& r, int par, Step32 s0, Step32 s1) {
-  if (r.R > 2 || r.depth != 2 || s0.snap_pre || s1.snap_pre || s0.amp || s1.amp)
+  if (r.R > 2 || r.depth != 2 || s0.snap_pre || s1.snap_pre || s0.nsrc != s1.nsrc || s0.src_xy != s1.src_xy)
     return set_error(ctx, FD2D_ERR_UNSUPPORTED, "two-step launch of an unsupported step");
   Step2 q;
   for (int k = 0; k < 2; ++k) {
@@ -2369,7 +2398,7 @@ fd2d_status fp32_correlation(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& 
 
 fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
   Run r;
-  FD2D_TRY(init_run(ctx, g, &a, 1, true, r));
+  FD2D_TRY(init_run(ctx, g, &a, 1, true, r, !(a.dmu != nullptr && a.n_C_in == g.ntc)));
   const int ntc = g.ntc, K = g.K, mode = a.mode;
   const int64_t np = r.np;
   const int ncol = g.nb == 0 ? 1 : g.nb;
@@ -2487,6 +2516,38 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
       s.nrec = nr;
       s.seis_col = a.seis + (size_t)nr * (n - 1);
       s.rec_u = 1;
+      // two steps in one launch when nothing has to happen between them: no
+      // stored u before the second, no K_mu term and no DFT contraction after
+      // the first, and the second step's injection plane (if any) resident
+      if (r.depth == 2 && !born && n < nt_loop && !s.snap_pre && !(save_u && (n + 1) % g.fw == 0) &&
+          !(have_fwd && a.n_u_fwd >= i_fw_in + 1 && n % g.fw == 0) && !(is_dft && dft_would_flush(d))) {
+        Step32 s1 = s;
+        s1.inj_plane = -1;
+        bool can = true;
+        if (stf2d) {
+          s1.amp = a.stf_re + (size_t)d0 * n;
+        } else if (inj.n_events && j_inj < inj.n_events && inj.step_of_event[j_inj] == n + 1) {
+          can = j_inj >= inj.first && j_inj < inj.first + inj.count;
+          if (can) s1.inj_plane = j_inj++ - inj.first;
+        }
+        if (can) {
+          const bool is_dft1 = d.n_events && (n + 1) % g.fs == 0;
+          s1.snap_dft = is_dft1 ? d.snaps + (size_t)(d.filled + (is_dft ? 1 : 0)) * r.lanes_ps() : nullptr;
+          s1.seis_col = a.seis + (size_t)nr * n;
+          FD2D_TRY(launch_step2(ctx, r, par, s, s1));
+          par ^= 1;
+          if (is_dft) FD2D_TRY(dft_push(ctx, r, g, d));
+          if (have_fwd && a.n_u_fwd >= i_fw_in + 1 && (n + 1) % g.fw == 0) {
+            const float* uf = a.u_fwd + (size_t)np * (a.n_u_fwd - 1 - i_fw_in);
+            FD2D_DISPATCH_R(r.R, k32_kmu, r.G, r.u[par], uf, Kmu, (float)g.fw);
+            FD2D_TRY(after_launch(ctx, "k32_kmu"));
+            ++i_fw_in;
+          }
+          if (is_dft1) FD2D_TRY(dft_push(ctx, r, g, d));
+          ++n;
+          continue;
+        }
+      }
       FD2D_TRY(launch_step(ctx, r, par, s));
       par ^= 1;
       if (born && n != ntc) {

@@ -132,17 +132,18 @@ fd2d_status fd2d_ctx_set_chunks(fd2d_ctx* ctx, int32_t max_snapshots, int32_t ma
 fd2d_status fd2d_ctx_set_tile_rows(fd2d_ctx* ctx, int32_t rows);
 /* Tile rows used by the last FP32 time loop this context set up (0: none yet). */
 int32_t fd2d_ctx_last_tile_rows(const fd2d_ctx* ctx);
-/* Time steps per launch of the FP32 Green-function and correlation loops at FD
- * orders 2 and 4: 1 or 2 to force, 0 (default) to time both once per context
- * for each grid, order, lane count and tile shape when the stream is idle and
- * keep the faster (one step per launch otherwise).  Two steps per launch
+/* Time steps per launch of the FP32 time loops at FD orders 2 and 4: 1 or 2
+ * to force, 0 (default) to time both, with every tile shape, once per context
+ * for each grid, order, lane count and kind when the stream is idle and keep
+ * the fastest (one step per launch otherwise).  Two steps per launch
  * recompute the first step on a wider halo ring -- more arithmetic for half
  * the launches, which pays where a launch leaves most SMs idle (small grids);
- * the fields, seismograms and spectra are bit for bit those of one step per
- * launch.  Steps that store wavefield snapshots (modes != 0), Born runs, the
- * adjoint loop, order 6/8 and the multi-geometry batch run one step per
- * launch.  The environment variable FD2D_TIME_DEPTH forces a depth for
- * contexts left at 0. */
+ * the fields, seismograms, spectra and kernels are bit for bit those of one
+ * step per launch.  The Green-function, correlation and adjoint loops pair
+ * steps; steps with something in between (a stored wavefield, a K_mu term, a
+ * DFT or injection chunk boundary) run singly, and Born runs, order 6/8 and
+ * the multi-geometry batch run one step per launch.  The environment variable
+ * FD2D_TIME_DEPTH forces a depth for contexts left at 0. */
 fd2d_status fd2d_ctx_set_time_depth(fd2d_ctx* ctx, int32_t depth);
 /* Steps per launch chosen for the last FP32 time loop this context set up (0: none yet). */
 int32_t fd2d_ctx_last_time_depth(const fd2d_ctx* ctx);

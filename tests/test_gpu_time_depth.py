@@ -186,3 +186,40 @@ def test_full_size_workloads_are_bit_identical(fd2d_lib, name):
     for a, b in zip(out[1], out[2]):
         assert np.abs(a).max() > 0
         assert np.array_equal(a, b)
+
+
+def test_adjoint_runs_are_bit_identical(fd2d_lib):
+    """The structure-kernel sequence: Green and correlation runs in mode 1
+    (stored wavefields), adjoint mode 1 (point adjoint sources with per-step
+    amplitudes, two of them on one node, K_mu against the stored correlation
+    wavefield every fw steps, the DFT of u) and adjoint mode 0 (the field source
+    of that spectrum, K_s and K_mu) -- one and two steps per launch."""
+    from fd2d_noise_gb300 import _lib, solvers
+    cfg = small_cfg(nx=110, nz=96, nt=57, K=8, fs=3, fw=4, order=4)
+    mu, rho = media(cfg, seed=21)
+    spec, sd = noise_source(cfg, seed=21)
+    src = stations(cfg, 1, seed=22)
+    off = np.random.default_rng(23).uniform(-10, 10, (5, 2)) * np.array([cfg.dx, cfg.dz])
+    rec = np.clip(src + off, [2 * cfg.dx, 2 * cfg.dz], [cfg.Lx - 2 * cfg.dx, cfg.Lz - 2 * cfg.dz])
+    rec = np.vstack([rec, rec[2:3]])  # two adjoint sources on one node
+    stf = np.random.default_rng(24).standard_normal((rec.shape[0], cfg.ntc)).astype(np.complex128)
+    out = {}
+    for d in (1, 2):
+        ctx = _lib.Context(0, _lib.PREC_FP32)
+        try:
+            with solvers.bound_context(ctx):
+                ctx.set_time_depth(d)
+                G, G_out, _ = solvers.run_forward1_green(mu, rho, src, rec, 1, cfg=cfg, precision="fp32")
+                _, C_out = solvers.run_forward2_correlation(mu, rho, G, spec, sd, rec, 1, cfg=cfg, precision="fp32")
+                K1, S1, _, s1 = solvers.run_noise_adjoint(mu, rho, C_out, stf, rec, rec, None, None, None, 1,
+                                                          cfg=cfg, precision="fp32")
+                assert ctx.last_time_depth() == d
+                K0, _, _, s0 = solvers.run_noise_adjoint(mu, rho, G_out, S1, None, rec, spec, sd, G, 0, cfg=cfg,
+                                                         precision="fp32")
+                assert ctx.last_time_depth() == d
+                out[d] = [K1, S1, s1, K0, s0]
+        finally:
+            ctx.close()
+    for a, b in zip(out[1], out[2]):
+        assert np.abs(a).max() > 0
+        assert np.array_equal(a, b)
