@@ -1607,12 +1607,13 @@ int step_ctas(int R, int tz) {
 // one, every shape is timed once per context on this run's freshly zeroed
 // fields -- 24 steps of the run's kind (with or without the displacement u)
 // with no sources, receivers or snapshots, in three rounds of which the
-// fastest counts -- and the fastest shape is kept for later runs
-// of the same grid, order, lane count and kind if it beats the size rule's
-// shape by more than 1 %.  When timing would
-// stall queued or concurrent work, or during a stream capture, the size rule
-// decides: the fewest waves of CTAs (tiles over resident CTAs per SM x SMs),
-// the shortest tiles among equals.  The step time is set by the waves: on
+// fastest counts -- and the fastest shape is kept for later runs of the same
+// grid, order, lane count and kind if it beats the size rule's shape by more
+// than 3 % (plain timed steps differ from real loops, with sources,
+// receivers, snapshots and kernel terms, by about that much).  When timing
+// would stall queued or concurrent work, or during a stream capture, the size
+// rule decides: the fewest waves of CTAs (tiles over resident CTAs per SM x
+// SMs), the shortest tiles among equals.  The step time is set by the waves: on
 // GB300 a 600x600 Green step takes ~5.5 us for any tile count up to one wave
 // and ~7.7 us just past it.
 fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
@@ -1702,7 +1703,7 @@ fd2d_status tune_tile_rows(fd2d_ctx* ctx, Run& r) {
     if (ms_of[c] < ms_of[best]) best = c;
     if (TILE_ROWS[c] == rule) ri = c;
   }
-  r.tz = ms_of[best] < 0.99f * ms_of[ri] ? TILE_ROWS[best] : rule;
+  r.tz = ms_of[best] < 0.97f * ms_of[ri] ? TILE_ROWS[best] : rule;
   ctx->tile_choice[key.h] = r.tz;
   return FD2D_OK;
 }
@@ -1813,8 +1814,8 @@ fd2d_status init_run(fd2d_ctx* ctx, const Geometry& g, const SolveArgs* a, int S
 // tile shape tune_tile_rows chose.  Otherwise, on an idle stream with the GPU to
 // itself, 24 steps are timed one per launch on that shape and two per launch
 // on every shape (on the run's zeroed fields, zeroed again after; the fastest
-// of three rounds counts), and the fastest is kept if it beats one step per
-// launch by more than 1 %,
+// of three rounds counts); two steps per launch are kept if they beat one step
+// per launch by more than 1 %, on another shape only if by 3 % more,
 // remembered per grid, order, lane count and kind.  A forced tile shape is
 // kept.  One step per launch otherwise.  The tile tables and tensor maps of
 // the result are set up by the caller.
@@ -1895,10 +1896,20 @@ fd2d_status tune_time_depth(fd2d_ctx* ctx, Run& r, int nsrc, const int* crowded)
       }
       ms_of[c + 1] = round == 0 ? ms : std::min(ms_of[c + 1], ms);
     }
+  // two steps per launch on the tile tuner's shape if faster by 1 %; another
+  // shape only if faster still by 3 % (plain timed steps favour large tiles a
+  // little more than loops with sources, receivers and K_mu terms do)
   float best_ms = ms_of[0];
   int best_d = 1, best_tz = tz1;
+  int c1 = -1;
   for (int c = 0; c < N_TILE_ROWS; ++c)
-    if (ms_of[c + 1] > 0.f && ms_of[c + 1] < 0.99f * best_ms) {
+    if (TILE_ROWS[c] == tz1) c1 = c;
+  if (c1 >= 0 && ms_of[c1 + 1] > 0.f && ms_of[c1 + 1] < 0.99f * best_ms) {
+    best_ms = ms_of[c1 + 1];
+    best_d = 2;
+  }
+  for (int c = 0; c < N_TILE_ROWS; ++c)
+    if (c != c1 && ms_of[c + 1] > 0.f && ms_of[c + 1] < (best_d == 2 ? 0.97f : 0.99f) * best_ms) {
       best_ms = ms_of[c + 1];
       best_d = 2;
       best_tz = TILE_ROWS[c];
