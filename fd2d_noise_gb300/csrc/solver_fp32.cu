@@ -482,9 +482,13 @@ __device__ __forceinline__ void step_tile(const Grid32& G, const StepMaps& M, co
             vx[4 * h] = f.x; vx[4 * h + 1] = f.y; vx[4 * h + 2] = f.z; vx[4 * h + 3] = f.w;
           }
         }
-        float vz[2 * R][4];  // box rows rr - R + 1 .. rr + R
+        float vz[2 * R][4];  // box rows rr - R + 1 .. rr + R; row rr is vx[4..7]
 #pragma unroll
         for (int k = 0; k < 2 * R; ++k) {
+          if (k == R - 1) {
+            vz[k][0] = vx[4]; vz[k][1] = vx[5]; vz[k][2] = vx[6]; vz[k][3] = vx[7];
+            continue;
+          }
           const float4 f = *reinterpret_cast<const float4*>(s_vn + (rr - R + 1 + k) * W + cv);
           vz[k][0] = f.x; vz[k][1] = f.y; vz[k][2] = f.z; vz[k][3] = f.w;
         }
