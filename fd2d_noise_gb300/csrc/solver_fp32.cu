@@ -657,7 +657,7 @@ template <int R, bool EDGE>
 __device__ __forceinline__ void tb_v_item(const Grid32& G, const float* cf, float* s_v, const float* s_sxy,
                                           const float* s_szy, const float* s_b, const float* s_t, const float* s_i,
                                           int r, int c0, int bx, int bz, const int* s_src, const float* s_amp,
-                                          int nbs) {
+                                          int nbs, float* snap_v, int tz) {
   constexpr int W = TB_W;
   const int gz = bz + r;
   const bool zin = gz >= R && gz <= G.nz - R - 1;
@@ -705,6 +705,14 @@ __device__ __forceinline__ void tb_v_item(const Grid32& G, const float* cf, floa
   if (s_i) i4 = *reinterpret_cast<const float4*>(s_i + idx0);
   const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
   const float tt[4] = {t4.x, t4.y, t4.z, t4.w}, ii[4] = {i4.x, i4.y, i4.z, i4.w};
+  if (snap_v && r >= TB_Z && r < TB_Z + tz && c0 >= TB_X && c0 < TB_X + TX) {
+    // single(v) before the update at the tile's own points (mode != 0 snapshots)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int gx = bx + c0 + e;
+      if (!EDGE || (gx < G.nx && gz < G.nz)) snap_v[gx + (int64_t)G.nx * gz] = vv[e];
+    }
+  }
   float out[4];
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
@@ -893,7 +901,7 @@ __global__ __launch_bounds__(Tile2<TZ, HU, HI>::NT) void k32_step2(Grid32 G, con
     // A: v1
     for (int it = tid; it < NQA * (T::RA1 - T::RA0 + 1); it += NT)
       tb_v_item<R, EDGE>(G, cf, s_v, s_sxy, s_szy, s_b, s_t, s_i0, T::RA0 + it / NQA, 4 * (T::QA0 + it % NQA), bx,
-                         bz, s_src, s_amp0, nbs);
+                         bz, s_src, s_amp0, nbs, S0.snap_pre_u ? nullptr : S0.snap_pre, TZ);
     __syncthreads();
     // B: s1 (in place: an item reads its own old stresses only); step-1 outputs on the tile
     for (int it = tid; it < NQB * (T::RB1 - T::RB0 + 1); it += NT) {
@@ -908,6 +916,12 @@ __global__ __launch_bounds__(Tile2<TZ, HU, HI>::NT) void k32_step2(Grid32 G, con
         float nu[4];
         if (HU) {
           float* up = s_u + tr * TX + 4 * tq;
+          if (S0.snap_pre && S0.snap_pre_u) {
+            // single(u) before step 1 (mode != 0 snapshots)
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if (!EDGE || (i0 + e < G.nx && j < G.nz)) S0.snap_pre[i0 + e + (int64_t)G.nx * j] = up[e];
+          }
 #pragma unroll
           for (int e = 0; e < 4; ++e) nu[e] = __fmaf_rn(vn[e], G.dt, up[e]);
           *reinterpret_cast<float4*>(up) = make_float4(nu[0], nu[1], nu[2], nu[3]);
@@ -923,7 +937,7 @@ __global__ __launch_bounds__(Tile2<TZ, HU, HI>::NT) void k32_step2(Grid32 G, con
     // C: v2
     for (int it = tid; it < NQC * (T::RC1 - T::RC0 + 1); it += NT)
       tb_v_item<R, EDGE>(G, cf, s_v, s_sxy, s_szy, s_b, s_t, s_i1, T::RC0 + it / NQC, 4 * (T::QC0 + it % NQC), bx,
-                         bz, s_src, s_amp1, nbs);
+                         bz, s_src, s_amp1, nbs, S1.snap_pre_u ? nullptr : S1.snap_pre, TZ);
     __syncthreads();
     // D: s2, u2 and the stores of the tile
     for (int it = tid; it < (TX / 4) * TZ; it += NT) {
@@ -935,6 +949,12 @@ __global__ __launch_bounds__(Tile2<TZ, HU, HI>::NT) void k32_step2(Grid32 G, con
       tb_s_item<R, EDGE>(G, cf, s_v, s_sxy, s_szy, s_mu, r, c0, bx, bz, nsx, nsz, vn);
       if (HU) {
         const float* up = s_u + tr * TX + 4 * tq;
+        if (S1.snap_pre && S1.snap_pre_u) {
+          // single(u) before step 2
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (!EDGE || i0 + e < G.nx) S1.snap_pre[i0 + e + (int64_t)G.nx * j] = up[e];
+        }
 #pragma unroll
         for (int e = 0; e < 4; ++e) nu[e] = __fmaf_rn(vn[e], G.dt, up[e]);
       } else {
@@ -1411,7 +1431,8 @@ void launch_step2_r(fd2d_ctx* ctx, const Run& r, int par, const Step2& q) {
 // Steps n and n+1 (s0, s1) in one launch: the fields of read buffer `par` are
 // advanced twice and written to buffer 1 - par.
 fd2d_status launch_step2(fd2d_ctx* ctx, const Run& r, int par, Step32 s0, Step32 s1) {
-  if (r.R > 2 || r.depth != 2 || s0.snap_pre || s1.snap_pre || s0.nsrc != s1.nsrc || s0.src_xy != s1.src_xy)
+  if (r.R > 2 || r.depth != 2 || s0.nsrc != s1.nsrc || s0.src_xy != s1.src_xy ||
+      (s0.snap_pre && s0.snap_pre_u != s0.has_u) || (s1.snap_pre && s1.snap_pre_u != s1.has_u))
     return set_error(ctx, FD2D_ERR_UNSUPPORTED, "two-step launch of an unsupported step");
   Step2 q;
   for (int k = 0; k < 2; ++k) {
@@ -2265,14 +2286,14 @@ fd2d_status fp32_forward1_plan(fd2d_ctx* ctx, const Geometry& g, const SolveArgs
     auto pre = [&](int n) { return a.mode != 0 && (n + nt - 1) % g.fw == 0; };
     auto is_dft_step = [&](int n) { return (n + nt - 1) % g.fs == 0; };
     for (int n = 1; n <= nt; ++n) {
-      // two steps in one launch when nothing has to happen between them: no
-      // wavefield snapshot before either step, no DFT contraction after the first
-      if (r.depth == 2 && !born && n < nt && !pre(n) && !pre(n + 1) &&
-          !(is_dft_step(n) && dft_would_flush(dd))) {
+      // two steps in one launch when nothing has to happen between them (no DFT
+      // contraction after the first); snapshots before either step are taken in it
+      if (r.depth == 2 && !born && n < nt && !(is_dft_step(n) && dft_would_flush(dd))) {
         Step32 s2[2] = {};
         for (int k = 0; k < 2; ++k) {
           Step32& s = s2[k];
           s.inj_plane = -1;
+          if (pre(n + k)) s.snap_pre = a.G_out + (size_t)np * (i_fw_out++);
           s.src_xy = r.src_xy;
           s.nsrc = (int)a.src_idx.size();
           s.amp_const = 1.0e9f;
@@ -2372,13 +2393,15 @@ fd2d_status fp32_correlation_plan(fd2d_ctx* ctx, const Geometry& g, const SolveA
       s.seis_col = a.seis + (size_t)nr * (n - 1);
       s.seis_lane = seis_lane;
       s.rec_u = 1;  // u does not depend on this step's Born stress correction
-      // two steps in one launch when no snapshot precedes either and the next
-      // step's injection plane (if any) is already resident
-      if (r.depth == 2 && !born && n < ntc && !pre(n) && !pre(n + 1) &&
+      // two steps in one launch when the next step's injection plane (if any) is
+      // already resident; snapshots before either step are taken in it
+      if (r.depth == 2 && !born && n < ntc &&
           ((n + 1) % g.fs != 0 || (ev >= ij.first && ev < ij.first + ij.count))) {
         Step32 s1 = s;
         s1.inj_plane = -1;
         if ((n + 1) % g.fs == 0) s1.inj_plane = ev++ - ij.first;
+        s1.snap_pre = pre(n + 1) ? a.C_out + (size_t)np * (i_fw_out++) : nullptr;
+        s1.snap_pre_u = 1;
         s1.seis_col = a.seis + (size_t)nr * n;
         FD2D_TRY(launch_step2(ctx, r, par, s, s1));
         par ^= 1;
@@ -2532,10 +2555,11 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
       s.seis_col = a.seis + (size_t)nr * (n - 1);
       s.rec_u = 1;
       // two steps in one launch when nothing has to happen between them: no
-      // stored u before the second, no K_mu term and no DFT contraction after
-      // the first, and the second step's injection plane (if any) resident
-      if (r.depth == 2 && !born && n < nt_loop && !s.snap_pre && !(save_u && (n + 1) % g.fw == 0) &&
-          !(have_fwd && a.n_u_fwd >= i_fw_in + 1 && n % g.fw == 0) && !(is_dft && dft_would_flush(d))) {
+      // K_mu term and no DFT contraction after the first, and the second step's
+      // injection plane (if any) resident; stored u before either step is
+      // taken in it
+      if (r.depth == 2 && !born && n < nt_loop && !(have_fwd && a.n_u_fwd >= i_fw_in + 1 && n % g.fw == 0) &&
+          !(is_dft && dft_would_flush(d))) {
         Step32 s1 = s;
         s1.inj_plane = -1;
         bool can = true;
@@ -2546,6 +2570,8 @@ fd2d_status fp32_adjoint(fd2d_ctx* ctx, const Geometry& g, const SolveArgs& a) {
           if (can) s1.inj_plane = j_inj++ - inj.first;
         }
         if (can) {
+          s1.snap_pre = (save_u && (n + 1) % g.fw == 0) ? a.C_out + (size_t)np * (i_fw_out++) : nullptr;
+          s1.snap_pre_u = 1;
           const bool is_dft1 = d.n_events && (n + 1) % g.fs == 0;
           s1.snap_dft = is_dft1 ? d.snaps + (size_t)(d.filled + (is_dft ? 1 : 0)) * r.lanes_ps() : nullptr;
           s1.seis_col = a.seis + (size_t)nr * n;

@@ -140,9 +140,9 @@ int32_t fd2d_ctx_last_tile_rows(const fd2d_ctx* ctx);
  * the launches, which pays where a launch leaves most SMs idle (small grids);
  * the fields, seismograms, spectra and kernels are bit for bit those of one
  * step per launch.  The Green-function, correlation and adjoint loops pair
- * steps; steps with something in between (a stored wavefield, a K_mu term, a
- * DFT or injection chunk boundary) run singly, and Born runs, order 6/8 and
- * the multi-geometry batch run one step per launch.  The environment variable
+ * steps (stored wavefields are taken inside a pair); steps with something in
+ * between (a K_mu term, a DFT or injection chunk boundary) run singly, and
+ * Born runs, order 6/8 and the multi-geometry batch run one step per launch.  The environment variable
  * FD2D_TIME_DEPTH forces a depth for contexts left at 0. */
 fd2d_status fd2d_ctx_set_time_depth(fd2d_ctx* ctx, int32_t depth);
 /* Steps per launch chosen for the last FP32 time loop this context set up (0: none yet). */

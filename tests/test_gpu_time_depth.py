@@ -6,8 +6,8 @@ the same rounded operations, so spectra, seismograms, correlations and stored
 wavefields must be bit for bit those of one step per launch -- on edge and
 interior tiles, with point sources, receivers, DFT snapshots on either step of
 a pair (freq_samp 1 puts them on both), injection planes, stored wavefields
-(mode 1, whose steps run singly), an odd number of steps, lanes, and every
-tile shape.  The time-depth tuner picks one depth per grid and keeps it;
+(modes 1, 11: single(v) or single(u) before either step of a pair), an odd
+number of steps, lanes, and every tile shape.  The time-depth tuner picks one depth per grid and keeps it;
 orders 6/8 and tiles with more receivers than the kernel keeps run one step
 per launch.
 """
@@ -79,9 +79,9 @@ def test_every_tile_shape(fd2d_lib, rows):
         assert np.array_equal(a, b)
 
 
-def test_stored_wavefields_split_the_pairs(fd2d_lib):
-    """Mode 1 stores single(v) / single(u) before every fw-th step: those steps
-    run singly, the others in pairs, and everything matches."""
+def test_stored_wavefields_inside_pairs(fd2d_lib):
+    """Mode 1 stores single(v) / single(u) before every fw-th step (fw 3: on
+    the first and on the second step of pairs); everything matches."""
     cfg = small_cfg(nx=96, nz=88, nt=47, K=6, fs=2, fw=3, order=4)
     out, used = _with_depths(cfg, seed=12, mode=1)
     assert used[2] == 2
@@ -192,8 +192,9 @@ def test_adjoint_runs_are_bit_identical(fd2d_lib):
     """The structure-kernel sequence: Green and correlation runs in mode 1
     (stored wavefields), adjoint mode 1 (point adjoint sources with per-step
     amplitudes, two of them on one node, K_mu against the stored correlation
-    wavefield every fw steps, the DFT of u) and adjoint mode 0 (the field source
-    of that spectrum, K_s and K_mu) -- one and two steps per launch."""
+    wavefield every fw steps, the DFT of u), adjoint mode 0 (the field source
+    of that spectrum, K_s and K_mu) and adjoint mode 11 (u stored every fw
+    steps) -- one and two steps per launch."""
     from fd2d_noise_gb300 import _lib, solvers
     cfg = small_cfg(nx=110, nz=96, nt=57, K=8, fs=3, fw=4, order=4)
     mu, rho = media(cfg, seed=21)
@@ -217,7 +218,10 @@ def test_adjoint_runs_are_bit_identical(fd2d_lib):
                 K0, _, _, s0 = solvers.run_noise_adjoint(mu, rho, G_out, S1, None, rec, spec, sd, G, 0, cfg=cfg,
                                                          precision="fp32")
                 assert ctx.last_time_depth() == d
-                out[d] = [K1, S1, s1, K0, s0]
+                # mode 11: u stored before every fw-th step
+                K11, _, U11, s11 = solvers.run_noise_adjoint(mu, rho, C_out, stf, rec, rec, None, None, None, 11,
+                                                             cfg=cfg, precision="fp32")
+                out[d] = [K1, S1, s1, K0, s0, K11, U11, s11, G_out, C_out]
         finally:
             ctx.close()
     for a, b in zip(out[1], out[2]):
