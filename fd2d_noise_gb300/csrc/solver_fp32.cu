@@ -617,8 +617,9 @@ __global__ __launch_bounds__(Tile<R, HU, HI, TZ>::NT, Tile<R, HU, HI, TZ>::MINB)
 //   C  v2 on x in [x0-4, x0+35], z in [z0-1, z0+TZ+1]
 //   D  s2, v2, u2 on the tile, stored
 // For R <= 2 the values each phase needs lie inside what the previous phase
-// computed (v2 on the tile needs s1 on [x0-3, x0+33], which needs v1 on
-// [x0-4, x0+35]; in z likewise); points computed beyond that are never read.
+// computed (at R = 2, s2 on the tile needs v2 on [x0-1, x0+33], which needs s1
+// on [x0-3, x0+34], which needs v1 on [x0-4, x0+36]; in z likewise); points
+// computed beyond that are never read.
 // Every point is updated by the same rounded operations as in step_tile, and
 // points outside the grid come out zero (all their inputs are the tensor
 // maps' zero fill), so fields, seismograms and snapshots are bit for bit those
