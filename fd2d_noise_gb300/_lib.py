@@ -35,6 +35,7 @@ EXPORTED = [
     "fd2d_make_adjoint_sources", "fd2d_ctx_last_batch", "fd2d_ctx_release", "fd2d_ctx_workspace_bytes",
     "fd2d_gaussblur2d", "fd2d_imfilter_circular", "fd2d_ctx_set_chunks", "fd2d_ctx_set_tile_rows", "fd2d_ctx_last_tile_rows",
     "fd2d_ctx_set_shared_gpu", "fd2d_device_free_bytes", "fd2d_ctx_set_time_depth", "fd2d_ctx_last_time_depth",
+    "fd2d_check_bounded_wait",
 ]
 TILE_ROWS_AUTO = 0
 TILE_ROWS_RULE = -1
@@ -98,6 +99,7 @@ def load(path: str = LIB_PATH):
         L.fd2d_ctx_set_shared_gpu.argtypes = [_vp, _i32]
         L.fd2d_ctx_last_tile_rows.argtypes = [_vp]
         L.fd2d_ctx_set_time_depth.argtypes = [_vp, _i32]
+        L.fd2d_check_bounded_wait.argtypes = [_vp, _i64]
         L.fd2d_ctx_last_time_depth.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.argtypes = [_vp]
         L.fd2d_ctx_workspace_bytes.restype = _i64

@@ -145,6 +145,12 @@ int32_t fd2d_ctx_last_tile_rows(const fd2d_ctx* ctx);
  * Born runs, order 6/8 and the multi-geometry batch run one step per launch.  The environment variable
  * FD2D_TIME_DEPTH forces a depth for contexts left at 0. */
 fd2d_status fd2d_ctx_set_time_depth(fd2d_ctx* ctx, int32_t depth);
+/* Diagnostic of the bounded device-side waits: runs a kernel whose mbarrier
+ * wait nothing completes, bounded by limit_us (1 .. 2e6) microseconds of
+ * %globaltimer -- the wait every kernel of the library uses, there with a
+ * 2 s limit.  It gives up, flags the context, and the call returns
+ * FD2D_ERR_TIMEOUT after about limit_us; the context stays usable. */
+fd2d_status fd2d_check_bounded_wait(fd2d_ctx* ctx, int64_t limit_us);
 /* Steps per launch chosen for the last FP32 time loop this context set up (0: none yet). */
 int32_t fd2d_ctx_last_time_depth(const fd2d_ctx* ctx);
 /* Declare that other work (other contexts, processes or streams) runs on the
