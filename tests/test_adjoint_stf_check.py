@@ -11,7 +11,11 @@ the time reversal of a difference changes its sign.  The oracle reproduces
 that sign (its adjoint sources match the reference's own to 1e-13), so the
 test pins the ratio -1 rather than correcting it; for the waveform
 difference the ratio stays up to 1e-3 away from -1 as h falls, a remainder
-this check does not pin.
+this check does not pin.  The amplitude difference (amp_diff.m, the measurement
+inversion/run_tests.m checks) passes the same way.  The cross-correlation time
+shift is not checked: its misfit T^2/2 takes T at the discrete maximum of the
+cross-correlation, so it does not change under small perturbations, while its
+adjoint source is the continuous traveltime sensitivity (cc_time_shift.m:44-52).
 """
 import os
 
@@ -21,7 +25,7 @@ import pytest
 from oracle import measurements as om
 
 GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "measurement_cases.npz"))
-MEASUREMENTS = ("log_amplitude_ratio", "waveform_difference")
+MEASUREMENTS = ("log_amplitude_ratio", "waveform_difference", "amplitude_difference")
 
 
 def _check(meas, veldis, hs):
