@@ -231,3 +231,26 @@ def test_oracle_source_hessian_matches_gradient_differences(measurement, tol):
     fd = float(np.sum((grad(p["sd"] + h * ds1) - grad(p["sd"])) / h * ds2))
     assert pred != 0
     assert abs(fd - pred) <= tol * abs(fd), (fd, pred)
+
+
+def test_oracle_gradient_with_amplitude_difference_matches_finite_differences():
+    """The structure gradient with the amplitude-difference measurement
+    (tools/measurement/amp_diff.m) against finite differences of its misfit."""
+    cfg = cfg4()
+    p = problem(cfg)
+    be = oracle_backend(cfg)
+    kw = dict(cfg=cfg, type="structure", measurement_source="amplitude_difference",
+              measurement_structure="amplitude_difference", weighting=1.0, backend=be)
+    _, _, c_data = eval_objective_and_gradient(p["mu_true"], p["rho"], p["spec"], p["sd"], p["ref"], p["arr"],
+                                               np.zeros((3, cfg.ntc)), p["t"], only_objective=True, **kw)
+    j0, g, _ = eval_objective_and_gradient(p["mu0"], p["rho"], p["spec"], p["sd"], p["ref"], p["arr"], c_data,
+                                           p["t"], **kw)
+    pred = float(np.sum(g[:, :, -1] * p["dmu"]))
+    errs = []
+    for h in (1e-2, 1e-4):
+        j1, _, _ = eval_objective_and_gradient(p["mu0"] + h * p["dmu"], p["rho"], p["spec"], p["sd"], p["ref"],
+                                               p["arr"], c_data, p["t"], only_objective=True, **kw)
+        fd = (j1 - j0) / h
+        errs.append(abs(fd - pred) / abs(fd))
+    assert j0 > 0 and pred != 0
+    assert errs[0] < 1e-2 and errs[1] < 1e-3 and errs[1] < errs[0], errs
