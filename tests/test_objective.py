@@ -254,3 +254,34 @@ def test_oracle_gradient_with_amplitude_difference_matches_finite_differences():
         errs.append(abs(fd - pred) / abs(fd))
     assert j0 > 0 and pred != 0
     assert errs[0] < 1e-2 and errs[1] < 1e-3 and errs[1] < errs[0], errs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("measurement", ["amplitude_difference", "cc_time_shift"])
+def test_gpu_objective_with_other_measurements_matches_oracle(fd2d_lib, measurement):
+    """The structure misfit, gradient and correlations with the amplitude
+    difference and the cross-correlation time shift measured on the GPU
+    (k64_measure) and the solvers in both forms, against the oracle."""
+    from fd2d_noise_gb300.objective import device_backend
+    cfg = cfg4()
+    p = problem(cfg)
+    be = oracle_backend(cfg)
+    kw = dict(cfg=cfg, type="structure", measurement_source=measurement, measurement_structure=measurement,
+              weighting=1.0)
+    mu_true = p["mu_true"]
+    if measurement == "cc_time_shift":
+        # a 10 % anomaly: time shifts of a whole sample (2 s), inside the 3.5 s cut-off
+        mu_true = p["mu0"] + 2.0 * (p["mu_true"] - p["mu0"])
+    _, _, c_data = eval_objective_and_gradient(mu_true, p["rho"], p["spec"], p["sd"], p["ref"], p["arr"],
+                                               np.zeros((3, cfg.ntc)), p["t"], only_objective=True, backend=be,
+                                               **kw)
+    jr, gr, cr = eval_objective_and_gradient(p["mu0"], p["rho"], p["spec"], p["sd"], p["ref"], p["arr"], c_data,
+                                             p["t"], backend=be, **kw)
+    assert jr > 0
+    for prec, tol in (("fp64", 1e-10), ("fp32", 1e-4)):
+        j, g, c = eval_objective_and_gradient(p["mu0"], p["rho"], p["spec"], p["sd"], p["ref"], p["arr"], c_data,
+                                              p["t"], backend=device_backend(cfg, prec), **kw)
+        assert abs(j - jr) <= tol * abs(jr), (prec, j, jr)
+        assert np.linalg.norm(c - cr) <= tol * np.linalg.norm(cr), prec
+        n = np.linalg.norm(gr[:, :, -1])
+        assert n > 0 and np.linalg.norm(g[:, :, -1] - gr[:, :, -1]) <= tol * n, prec
